@@ -1,0 +1,228 @@
+/*
+ * gbnufft: Gaussian-gridding NUFFT for NVIDIA GB300 (sm_103a), C ABI.
+ *
+ * Drop-in engine behind mripy's NUFFT function API (peng-cao/mripy
+ * fft/nufft_func.py, fft/nufft_func_cuda.py) and NUFFT operator classes
+ * (pics/operators_class.py, pics/operators_cuda_class.py).  Every entry point
+ * takes plain pointers, sizes and a cudaStream_t, returns an int status
+ * (GBN_OK == 0) and throws nothing.  Device pointers are marked "device";
+ * the gbn_nufft*_gaussker and *_host entry points take host pointers.
+ *
+ * Conventions shared with the reference (nufft_func.py):
+ *  - coordinates x_j are radians; they are scaled by df and wrapped mod 2*pi;
+ *  - nspread, oversampled grid nf and tau follow _compute_{1,2,3}d_grid_params
+ *    (nufft_func.py:198-249; the 3-D operator clamps nspread to [3, 6]);
+ *  - type-1 (adjoint)  F_k = (1/M) sum_j c_j exp(+s i k.x_j),  s = sign(iflag);
+ *  - type-2 (forward)  c_j = sum_k F_k exp(-s i k.x_j);
+ *  - type-21 (normal)  (1/M) A^H D A F, D = dcf (3-D) or identity;
+ *  - image index i <-> frequency k = i - m/2 (m//2 in Python), row-major
+ *    (x slowest, then y, then z), as numpy arrays of shape (ms, mt[, mu]).
+ * Arithmetic: complex64 data, FP32 stencil arithmetic and accumulation; FP64
+ * only for coordinate reduction, parameter and deapodisation-table set-up.
+ */
+#ifndef GBNUFFT_H
+#define GBNUFFT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef GBN_STREAM_T_DEFINED
+#define GBN_STREAM_T_DEFINED
+typedef struct CUstream_st *gbn_stream_t; /* == cudaStream_t; NULL = legacy default stream */
+#endif
+
+/* status codes */
+#define GBN_OK 0
+#define GBN_ERR_ARG 1       /* invalid argument (shape, size, pointer, parameter) */
+#define GBN_ERR_ALLOC 2     /* device or pinned-host allocation failed */
+#define GBN_ERR_CUDA 3      /* CUDA runtime error (message via gbn_last_error) */
+#define GBN_ERR_CUFFT 4     /* cuFFT error */
+#define GBN_ERR_STATE 5     /* call order: e.g. transform before gbn_set_points */
+#define GBN_ERR_CAPACITY 6  /* size beyond a documented limit */
+#define GBN_ERR_INTERNAL 7  /* unexpected host-side failure */
+
+#define GBN_COORD_F32 0
+#define GBN_COORD_F64 1
+
+#define GBN_FFT_FORWARD (-1) /* exp(-i ...), numpy.fft.fftn, unnormalised */
+#define GBN_FFT_INVERSE (+1) /* exp(+i ...), unnormalised                  */
+
+typedef struct gbn_plan gbn_plan;   /* opaque */
+typedef struct gbn_graph gbn_graph; /* opaque captured CUDA graph */
+
+typedef struct {
+    int32_t dim;            /* 1, 2 or 3 */
+    int32_t ms, mt, mu;     /* image size along x, y, z (unused dims: 1) */
+    double eps;             /* requested accuracy; selects nspread, ratio, tau */
+    int32_t max_nspread;    /* 0 = no clamp (1-D/2-D); 6 = the 3-D reference clamp */
+    int32_t iflag;          /* sign convention (see above) */
+    double df;              /* coordinate scale */
+    int32_t n_coil;         /* instances that share one trajectory (coils) */
+    int32_t n_traj;         /* trajectory groups (frames/slices), ragged sample counts */
+    /* tuning (0 = library default; the autotuner fills these) */
+    int32_t spread_tile[3]; /* output tile of the spread kernel, cells per dim */
+    int32_t interp_tile[3]; /* home bin of the interp kernel, cells per dim */
+    int32_t max_subproblem; /* samples per thread block before a bin is split */
+    int32_t coil_group;     /* coils per thread block: 1, 2, 4 or 8 */
+    int32_t threads;        /* threads per block for spread/interp: 128, 256 or 512 */
+} gbn_plan_desc;
+
+typedef struct {
+    int32_t nspread;        /* half-width: 2*nspread taps per dimension */
+    int32_t nf[3];          /* oversampled grid per dim (1 beyond dim) */
+    double tau;             /* Gaussian g(x) = exp(-x^2 / (4 tau)) */
+    int64_t n_samples;      /* total samples over all trajectory groups */
+    int64_t grid_cells;     /* nf1*nf2*nf3 */
+    int64_t n_inst;         /* n_traj * n_coil */
+    int64_t spread_subproblems;
+    int64_t interp_subproblems;
+    int64_t spread_entries; /* (sample, tile) pairs in the spread lists */
+    int32_t spread_tile[3];
+    int32_t interp_tile[3];
+    int32_t coil_group;
+    int32_t threads;
+    int64_t device_bytes;   /* device memory held by the plan */
+} gbn_plan_info;
+
+/* element strides (in complex64 elements) of a strided complex array */
+typedef struct {
+    int64_t traj_stride;    /* between trajectory groups (images only) */
+    int64_t coil_stride;    /* between coils */
+    int64_t elem_stride;    /* between pixels (row-major pixel index) or samples */
+} gbn_layout;
+
+/* ---- library ------------------------------------------------------------ */
+int gbn_version(void);
+const char *gbn_status_string(int status);
+/* copies the calling thread's last error message into buf (NUL-terminated) */
+int gbn_last_error(char *buf, int len);
+
+/* nspread, nf, tau from eps exactly as _compute_{1,2,3}d_grid_params
+ * (fft/nufft_func.py:198-249); max_nspread > 0 applies the 3-D clamp to [3, max]. */
+int gbn_grid_params(int dim, int ms, int mt, int mu, double eps, int max_nspread, int *nspread,
+                    int64_t nf[3], double *tau);
+
+/* ---- plans (replace the per-call set-up inside nufft{1,2,3}d{1,2,21}_gaussker) */
+int gbn_plan_create(const gbn_plan_desc *desc, gbn_plan **out);
+int gbn_plan_destroy(gbn_plan *plan);
+int gbn_plan_get_info(const gbn_plan *plan, gbn_plan_info *out);
+
+/* Sorts the samples into spatial bins (device coordinates, float32 or float64,
+ * x/y/z each of length traj_offsets[n_traj]; unused dims may be NULL).
+ * traj_offsets is a HOST array of n_traj+1 prefix offsets.  Allocates and
+ * synchronises the stream once; call before capturing a graph. */
+int gbn_set_points(gbn_plan *plan, int coord_dtype, const void *x, const void *y, const void *z,
+                   const int64_t *traj_offsets, gbn_stream_t stream);
+
+/* the plan's own oversampled grid buffer, (n_inst, nf1, nf2, nf3) complex64 (device) */
+void *gbn_plan_grid(gbn_plan *plan);
+
+/* ---- stages ------------------------------------------------------------- */
+/* spread: grid[inst] = sum_j c_j g(x_j - h m), output-stationary tiles
+ * (build_grid_{2,3}d1_fast, fft/nufft_func.py:550-582, 863-911).  Every cell of
+ * the grid is written.  c: device samples with layout (coil_stride, elem_stride);
+ * the sample index is global over trajectory groups. */
+int gbn_spread(gbn_plan *plan, const void *c, gbn_layout c_layout, void *grid, gbn_stream_t stream);
+
+/* interp: c_j = w_j * sum_m grid[m] g(x_j - h m) (build_grid_{2,3}d2_fast,
+ * nufft_func.py:607-639, 985-1032) WITHOUT the reference's 1/N, which
+ * gbn_pad_deapod folds in; weight (device float per sample) may be NULL. */
+int gbn_interp(gbn_plan *plan, const void *grid, void *c, gbn_layout c_layout, const float *weight,
+               gbn_stream_t stream);
+
+/* batched in-place C2C FFT of the grid over all instances (cuFFT). */
+int gbn_fft(gbn_plan *plan, void *grid, int direction, gbn_stream_t stream);
+
+/* image -> zero-padded grid with (pi/tau)^(d/2) exp(tau|k|^2) / N
+ * (nufft_func.py:751-764) */
+int gbn_pad_deapod(gbn_plan *plan, const void *img, gbn_layout img_layout, void *grid,
+                   gbn_stream_t stream);
+/* grid -> image with (1/M) (pi/tau)^(d/2) exp(tau|k|^2) / N (nufft_func.py:728-738) */
+int gbn_crop_deapod(gbn_plan *plan, const void *grid, void *img, gbn_layout img_layout,
+                    gbn_stream_t stream);
+
+/* ---- whole transforms (device buffers) ------------------------------------ */
+/* type-1: nufft{1,2,3}d1_gaussker (nufft_func.py:438, 702, 1167; _cuda twins
+ * nufft_func_cuda.py:581, 1463).  weight (device float per sample, may be NULL)
+ * multiplies the samples first: NUFFT3d.backward's density_weighting
+ * (pics/operators_class.py:341-349) fused into the spread. */
+int gbn_type1(gbn_plan *plan, const void *c, gbn_layout c_layout, const float *weight, void *img,
+              gbn_layout img_layout, gbn_stream_t stream);
+/* type-2: nufft{1,2,3}d2_gaussker (nufft_func.py:470, 741, 1209; nufft_func_cuda.py:609, 1512) */
+int gbn_type2(gbn_plan *plan, const void *img, gbn_layout img_layout, void *c, gbn_layout c_layout,
+              gbn_stream_t stream);
+/* type-21: nufft{1,2,3}d21_gaussker (nufft_func.py:506, 780, 1261; nufft_func_cuda.py:639, 1562);
+ * dcf (device float per sample) may be NULL. */
+int gbn_type21(gbn_plan *plan, const void *img, gbn_layout img_layout, void *out,
+               gbn_layout out_layout, const float *dcf, gbn_stream_t stream);
+
+/* ---- SENSE-fused operators (joint2operators(espirit, NUFFT), pics/operators_class.py:437-514) */
+/* kdata[coil] = A (S_coil . x); x: one image per trajectory group; sens: (n_coil, pixels) */
+int gbn_sense_forward(gbn_plan *plan, const void *x, gbn_layout x_layout, const void *sens,
+                      gbn_layout sens_layout, void *kdata, gbn_layout k_layout, gbn_stream_t stream);
+/* x = sum_coil conj(S_coil) . type1(dcf . kdata[coil]); dcf may be NULL */
+int gbn_sense_adjoint(gbn_plan *plan, const void *kdata, gbn_layout k_layout, const float *dcf,
+                      const void *sens, gbn_layout sens_layout, void *x, gbn_layout x_layout,
+                      gbn_stream_t stream);
+/* x_out = S^H type21(S x) with dcf (may be NULL): the CG-SENSE / FISTA normal operator */
+int gbn_sense_normal(gbn_plan *plan, const void *x, gbn_layout x_layout, const void *sens,
+                     gbn_layout sens_layout, const float *dcf, void *x_out, gbn_layout out_layout,
+                     gbn_stream_t stream);
+
+/* ---- differentiation ------------------------------------------------------ */
+/* grad_xyz[j*dim + d] = df * Re( sum_coil conj(grad_c[j,coil]) dc_j/dx_{j,d} ) for c = interp(grid)
+ * with the analytic derivative of the Gaussian weights (device float (M, dim)). */
+int gbn_interp_grad_coords(gbn_plan *plan, const void *grid, const void *grad_c, gbn_layout c_layout,
+                           float *grad_xyz, gbn_stream_t stream);
+
+/* ---- CUDA graphs ------------------------------------------------------------ */
+/* Captures gbn_sense_normal (sens != NULL) or gbn_type21 (sens == NULL) with fixed
+ * pointers into a graph; replay with gbn_graph_launch on any stream. */
+int gbn_graph_capture_normal(gbn_plan *plan, const void *x, gbn_layout x_layout, const void *sens,
+                             gbn_layout sens_layout, const float *dcf, void *x_out,
+                             gbn_layout out_layout, gbn_graph **out);
+int gbn_graph_launch(gbn_graph *graph, gbn_stream_t stream);
+int gbn_graph_destroy(gbn_graph *graph);
+
+/* ---- host-buffer entry points (the reference's numpy-in / numpy-out calls) ---- */
+/* One call = H2D of the inputs, the transform, D2H of the result, on the plan's
+ * staging buffers (pinned host memory recommended for the caller's arrays).
+ * Layouts are the reference's: image (ms, mt[, mu], n_coil) coil-last per
+ * trajectory group, samples (M_total, n_coil) coil-last; complex64. */
+int gbn_type1_host(gbn_plan *plan, const void *h_c, void *h_img, gbn_stream_t stream);
+int gbn_type2_host(gbn_plan *plan, const void *h_img, void *h_c, gbn_stream_t stream);
+int gbn_type21_host(gbn_plan *plan, const void *h_img, void *h_out, const float *h_dcf,
+                    gbn_stream_t stream);
+
+/* One-shot calls with the reference's signatures (host float64 coordinates,
+ * complex64 data coil-last, ntrail coils): plan, sort, transform, free.
+ * nufft2d1_gaussker fft/nufft_func.py:702 / nufft_func_cuda.py:581 */
+int gbn_nufft2d1_gaussker(const double *x, const double *y, const void *c, int64_t M, int32_t ntrail,
+                          int32_t ms, int32_t mt, double df, double eps, int32_t iflag, void *out);
+/* nufft2d2_gaussker fft/nufft_func.py:741 / nufft_func_cuda.py:609 */
+int gbn_nufft2d2_gaussker(const double *x, const double *y, const void *Fk, int64_t M, int32_t ntrail,
+                          int32_t ms, int32_t mt, double df, double eps, int32_t iflag, void *out);
+/* nufft2d21_gaussker fft/nufft_func.py:780 / nufft_func_cuda.py:639 */
+int gbn_nufft2d21_gaussker(const double *x, const double *y, const void *Fk, int64_t M, int32_t ntrail,
+                           int32_t ms, int32_t mt, double df, double eps, int32_t iflag, void *out);
+/* nufft3d1_gaussker fft/nufft_func.py:1167 / nufft_func_cuda.py:1463 */
+int gbn_nufft3d1_gaussker(const double *x, const double *y, const double *z, const void *c, int64_t M,
+                          int32_t ntrail, int32_t ms, int32_t mt, int32_t mu, double df, double eps,
+                          int32_t iflag, void *out);
+/* nufft3d2_gaussker fft/nufft_func.py:1209 / nufft_func_cuda.py:1512 */
+int gbn_nufft3d2_gaussker(const double *x, const double *y, const double *z, const void *Fk, int64_t M,
+                          int32_t ntrail, int32_t ms, int32_t mt, int32_t mu, double df, double eps,
+                          int32_t iflag, void *out);
+/* nufft3d21_gaussker fft/nufft_func.py:1261 / nufft_func_cuda.py:1562 (dcf may be NULL) */
+int gbn_nufft3d21_gaussker(const double *x, const double *y, const double *z, const void *Fk,
+                           int64_t M, int32_t ntrail, int32_t ms, int32_t mt, int32_t mu,
+                           const double *dcf, double df, double eps, int32_t iflag, void *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBNUFFT_H */

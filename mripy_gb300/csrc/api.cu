@@ -1,0 +1,927 @@
+// C ABI of the gbnufft library: plans, bin sort, transform pipelines, CUDA graphs and
+// the host-buffer entry points that mirror mripy's NUFFT functions.
+//
+// Pipelines (all on the caller's stream, no host synchronisation after set_points):
+//   type-2   pad_deapod -> FFT -> interp                       (nufft_func.py:741-777)
+//   type-1   spread -> FFT -> crop_deapod                       (nufft_func.py:702-738)
+//   type-21  pad_deapod -> FFT -> interp(*dcf) -> spread -> FFT -> crop_deapod
+//                                                               (nufft_func.py:1261-1330)
+// The reference fuses interp and spread per sample (build_grid_3d21); with
+// output-stationary spreading a tile needs the interpolated values of every sample
+// whose stencil reaches it, so the two run as separate kernels with the sample values
+// (n_coil complex per sample) kept in a plan-owned buffer between them.
+#include <cub/cub.cuh>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+using namespace gbn;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define GBN_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(e_ == cudaErrorMemoryAllocation ? GBN_ERR_ALLOC : GBN_ERR_CUDA,          \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+    } while (0)
+
+#define GBN_FFT(call)                                                                           \
+    do {                                                                                        \
+        cufftResult r_ = (call);                                                                \
+        if (r_ != CUFFT_SUCCESS) return fail(GBN_ERR_CUFFT, std::string(#call) + " failed, cufftResult " + std::to_string((int)r_)); \
+    } while (0)
+
+#define GBN_TRY(call)                  \
+    do {                               \
+        int s_ = (call);               \
+        if (s_ != GBN_OK) return s_;   \
+    } while (0)
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    template <typename T>
+    T *as() const { return (T *)p; }
+};
+
+}  // namespace
+
+struct gbn_plan {
+    gbn_plan_desc desc{};
+    int dim = 2;
+    int m[3] = {1, 1, 1};
+    int ns = 0;
+    int nf[3] = {1, 1, 1};
+    double tau = 0;
+    Geom gs{}, gi{};
+    int coil_group = 1, threads = 256, max_sub = 1024;
+    int64_t G = 1, n_inst = 1;
+    size_t device_bytes = 0;
+    int smem_optin = 0;
+
+    // fixed buffers
+    float2 *grid = nullptr;
+    float *tab[3] = {nullptr, nullptr, nullptr};
+    cufftHandle fft = 0;
+    bool fft_ok = false;
+
+    // point-dependent buffers (grow-only)
+    bool points_set = false;
+    int64_t M = 0;
+    std::vector<int64_t> traj_off;
+    DevBuf traj_off_d, grp_scale, pts, home_key, home_keys_sorted, touch_count, touch_off, home_count,
+        iota, home_idx, home_pts, dup_keys, dup_vals, dup_keys_sorted, dup_idx, dup_pts, spread_count,
+        spread_tile_off, home_tile_off, nsub, sub_off, spread_subs, interp_subs, cub_tmp, scratch,
+        stage_in, stage_out, stage_w;
+    int64_t n_dup = 0, n_spread_sub = 0, n_interp_sub = 0;
+};
+
+struct gbn_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int ensure(gbn_plan *p, DevBuf &b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.cap >= bytes) return GBN_OK;
+    if (b.p) {
+        cudaFree(b.p);
+        p->device_bytes -= b.cap;
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        cudaGetLastError();
+        return fail(GBN_ERR_ALLOC, "cudaMalloc(" + std::to_string(bytes) + ") failed: " + cudaGetErrorString(e));
+    }
+    b.cap = bytes;
+    p->device_bytes += bytes;
+    return GBN_OK;
+}
+
+void release(DevBuf &b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+int compute_params(int dim, int ms, int mt, int mu, double eps, int max_nspread, int *nspread, int64_t nf[3],
+                   double *tau) {
+    if (dim < 1 || dim > 3) return fail(GBN_ERR_ARG, "dim must be 1, 2 or 3");
+    if (!(eps > 1e-33 && eps < 1e-1)) return fail(GBN_ERR_ARG, "eps must satisfy 1e-33 < eps < 1e-1");
+    const int sizes[3] = {ms, dim > 1 ? mt : 1, dim > 2 ? mu : 1};
+    for (int d = 0; d < dim; ++d)
+        if (sizes[d] < 1) return fail(GBN_ERR_ARG, "image sizes must be >= 1");
+    // _compute_{1,2,3}d_grid_params, fft/nufft_func.py:198-249
+    const double pi = 3.14159265358979323846;
+    const int rat = eps > 1e-11 ? 2 : 3;
+    int ns = (int)(-std::log(eps) / (pi * (rat - 1) / (rat - 0.5)) + 0.5);
+    if (max_nspread > 0) {
+        ns = std::min(ns, max_nspread);
+        ns = std::max(ns, 3);
+    }
+    if (ns < 1) ns = 1;
+    if (2 * ns > kMaxW) return fail(GBN_ERR_CAPACITY, "nspread above 20 is not supported");
+    for (int d = 0; d < 3; ++d) nf[d] = d < dim ? std::max<int64_t>((int64_t)rat * sizes[d], 2 * ns) : 1;
+    const double lambda = ns / (rat * (rat - 0.5));
+    *tau = pi * lambda / ((double)ms * ms);
+    *nspread = ns;
+    return GBN_OK;
+}
+
+void make_geom(const gbn_plan *p, const int tile[3], Geom &g) {
+    g.dim = p->dim;
+    g.ns = p->ns;
+    g.W = 2 * p->ns;
+    g.ntiles = 1;
+    for (int d = 0; d < 3; ++d) {
+        g.nf[d] = p->nf[d];
+        g.tile[d] = d < p->dim ? std::max(1, std::min(tile[d], p->nf[d])) : 1;
+        g.ntile[d] = (g.nf[d] + g.tile[d] - 1) / g.tile[d];
+        g.ntiles *= g.ntile[d];
+        const double h = 2.0 * 3.14159265358979323846 / p->nf[d];
+        g.beta2[d] = d < p->dim ? (float)(h * h / (4.0 * p->tau) * 1.4426950408889634) : 0.f;
+    }
+    g.G = p->G;
+    g.n_coil = (int)p->desc.n_coil;
+    g.n_traj = (int)p->desc.n_traj;
+}
+
+int pow2_floor(int v) {
+    int r = 1;
+    while (r * 2 <= v) r *= 2;
+    return r;
+}
+
+int check_plan(const gbn_plan *p, bool need_points) {
+    if (!p) return fail(GBN_ERR_ARG, "null plan");
+    if (need_points && !p->points_set) return fail(GBN_ERR_STATE, "gbn_set_points has not been called");
+    return GBN_OK;
+}
+
+DeapodArgs deapod_args(const gbn_plan *p, bool with_group_scale) {
+    DeapodArgs a;
+    a.g = p->gs;
+    for (int d = 0; d < 3; ++d) {
+        a.m[d] = p->m[d];
+        a.tab[d] = p->tab[d];
+    }
+    a.grp_scale = with_group_scale ? p->grp_scale.as<float>() : nullptr;
+    return a;
+}
+
+int fft_exec(gbn_plan *p, float2 *grid, int direction, cudaStream_t s) {
+    if (!p->fft_ok) return fail(GBN_ERR_STATE, "no FFT plan");
+    GBN_FFT(cufftSetStream(p->fft, s));
+    GBN_FFT(cufftExecC2C(p->fft, (cufftComplex *)grid, (cufftComplex *)grid,
+                         direction < 0 ? CUFFT_FORWARD : CUFFT_INVERSE));
+    return GBN_OK;
+}
+
+int dir_type1(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_FORWARD : GBN_FFT_INVERSE; }
+int dir_type2(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_INVERSE : GBN_FFT_FORWARD; }
+
+int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, float2 *grid, cudaStream_t s) {
+    GBN_CUDA(launch_zero_split(p->gs, p->spread_subs.as<int4>(), p->n_spread_sub, grid, s));
+    SpreadArgs a;
+    a.g = p->gs;
+    a.subs = p->spread_subs.as<int4>();
+    a.pts = p->dup_pts.as<float4>();
+    a.idx = p->dup_idx.as<uint32_t>();
+    a.c = (const float2 *)c;
+    a.c_elem = L.elem_stride;
+    a.c_coil = L.coil_stride;
+    a.weight = weight;
+    a.grid = grid;
+    int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
+    while (cg > 1 && spread_smem_bytes(p->gs, cg) > (size_t)p->smem_optin) cg /= 2;
+    if (spread_smem_bytes(p->gs, cg) > (size_t)p->smem_optin)
+        return fail(GBN_ERR_CAPACITY, "spread tile does not fit in shared memory");
+    GBN_CUDA(launch_spread(a, p->n_spread_sub, cg, p->threads, s));
+    return GBN_OK;
+}
+
+int interp_cg(const gbn_plan *p) {
+    int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
+    while (cg > 1 && interp_smem_bytes(p->gi, cg) > (size_t)p->smem_optin) cg /= 2;
+    return cg;
+}
+
+int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const float *weight, cudaStream_t s) {
+    InterpArgs a;
+    a.g = p->gi;
+    a.subs = p->interp_subs.as<int4>();
+    a.pts = p->home_pts.as<float4>();
+    a.idx = p->home_idx.as<uint32_t>();
+    a.grid = grid;
+    a.c = (float2 *)c;
+    a.c_elem = L.elem_stride;
+    a.c_coil = L.coil_stride;
+    a.weight = weight;
+    const int cg = interp_cg(p);
+    if (interp_smem_bytes(p->gi, cg) > (size_t)p->smem_optin)
+        return fail(GBN_ERR_CAPACITY, "interp window does not fit in shared memory");
+    GBN_CUDA(launch_interp(a, p->n_interp_sub, cg, p->threads, s));
+    return GBN_OK;
+}
+
+template <typename F>
+int cub_call(gbn_plan *p, F f) {
+    size_t bytes = 0;
+    GBN_CUDA(f(nullptr, bytes));
+    GBN_TRY(ensure(p, p->cub_tmp, bytes));
+    bytes = p->cub_tmp.cap;
+    GBN_CUDA(f(p->cub_tmp.p, bytes));
+    return GBN_OK;
+}
+
+int key_bits(uint64_t max_key) {
+    int b = 1;
+    while (b < 32 && (1ull << b) <= max_key) ++b;
+    return b;
+}
+
+// count -> tile offsets (exclusive), subproblem table
+int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, DevBuf &subs, int every_tile,
+               int64_t *n_sub_out, cudaStream_t s) {
+    const int64_t T = (int64_t)g.ntiles * g.n_traj;
+    GBN_TRY(ensure(p, tile_off, sizeof(uint32_t) * T));
+    GBN_TRY(ensure(p, p->nsub, sizeof(uint32_t) * T));
+    GBN_TRY(ensure(p, p->sub_off, sizeof(uint32_t) * (T + 1)));
+    uint32_t *toff = tile_off.as<uint32_t>();
+    GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, count, toff, (int)T, s);
+    }));
+    GBN_CUDA(launch_count_subs(count, T, p->max_sub, every_tile, p->nsub.as<uint32_t>(), s));
+    uint32_t *soff = p->sub_off.as<uint32_t>();
+    uint32_t *ns_ = p->nsub.as<uint32_t>();
+    GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, ns_, soff, (int)T, s);
+    }));
+    uint32_t last[2] = {0, 0};
+    GBN_CUDA(cudaMemcpyAsync(&last[0], soff + (T - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GBN_CUDA(cudaMemcpyAsync(&last[1], ns_ + (T - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GBN_CUDA(cudaStreamSynchronize(s));
+    const int64_t n_sub = (int64_t)last[0] + last[1];
+    if (n_sub > 0x7FFFFFFF) return fail(GBN_ERR_CAPACITY, "too many subproblems");
+    GBN_TRY(ensure(p, subs, sizeof(int4) * (size_t)std::max<int64_t>(n_sub, 1)));
+    GBN_CUDA(launch_build_subs(count, toff, soff, T, p->max_sub, every_tile, subs.as<int4>(), s));
+    *n_sub_out = n_sub;
+    return GBN_OK;
+}
+
+__global__ void k_iota(uint32_t *v, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (uint32_t)i;
+}
+
+int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const void *z, const int64_t *off,
+                    cudaStream_t s) {
+    GBN_TRY(check_plan(p, false));
+    const int nt = p->desc.n_traj;
+    if (!off) return fail(GBN_ERR_ARG, "traj_offsets is null");
+    if (dtype != GBN_COORD_F32 && dtype != GBN_COORD_F64) return fail(GBN_ERR_ARG, "bad coordinate dtype");
+    if (off[0] != 0) return fail(GBN_ERR_ARG, "traj_offsets[0] must be 0");
+    for (int g = 0; g < nt; ++g)
+        if (off[g + 1] < off[g]) return fail(GBN_ERR_ARG, "traj_offsets must be non-decreasing");
+    const int64_t M = off[nt];
+    if (M >= (int64_t)1 << 31) return fail(GBN_ERR_CAPACITY, "more than 2^31-1 samples");
+    const void *src[3] = {x, y, z};
+    for (int d = 0; d < p->dim; ++d)
+        if (M > 0 && !src[d]) return fail(GBN_ERR_ARG, "coordinate pointer is null");
+    p->points_set = false;
+    p->M = M;
+    p->traj_off.assign(off, off + nt + 1);
+
+    const size_t Mb = (size_t)std::max<int64_t>(M, 1);
+    const int64_t Ti = (int64_t)p->gi.ntiles * nt, Ts = (int64_t)p->gs.ntiles * nt;
+    GBN_TRY(ensure(p, p->traj_off_d, sizeof(int64_t) * (nt + 1)));
+    GBN_TRY(ensure(p, p->grp_scale, sizeof(float) * nt));
+    GBN_TRY(ensure(p, p->pts, sizeof(float4) * Mb));
+    GBN_TRY(ensure(p, p->home_key, sizeof(uint32_t) * Mb));
+    GBN_TRY(ensure(p, p->home_keys_sorted, sizeof(uint32_t) * Mb));
+    GBN_TRY(ensure(p, p->touch_count, sizeof(uint32_t) * Mb));
+    GBN_TRY(ensure(p, p->touch_off, sizeof(uint64_t) * Mb));
+    GBN_TRY(ensure(p, p->home_count, sizeof(uint32_t) * (Ti + 1)));  // + status word
+    GBN_TRY(ensure(p, p->iota, sizeof(uint32_t) * Mb));
+    GBN_TRY(ensure(p, p->home_idx, sizeof(uint32_t) * Mb));
+    GBN_TRY(ensure(p, p->home_pts, sizeof(float4) * Mb));
+    GBN_TRY(ensure(p, p->spread_count, sizeof(uint32_t) * Ts));
+    GBN_TRY(ensure(p, p->scratch, sizeof(float2) * Mb * (size_t)p->desc.n_coil));
+
+    std::vector<float> gscale(nt);
+    for (int g = 0; g < nt; ++g) {
+        const int64_t Mg = off[g + 1] - off[g];
+        gscale[g] = Mg > 0 ? (float)(1.0 / (double)Mg) : 0.f;
+    }
+    GBN_CUDA(cudaMemcpyAsync(p->traj_off_d.p, off, sizeof(int64_t) * (nt + 1), cudaMemcpyHostToDevice, s));
+    GBN_CUDA(cudaMemcpyAsync(p->grp_scale.p, gscale.data(), sizeof(float) * nt, cudaMemcpyHostToDevice, s));
+    GBN_CUDA(cudaMemsetAsync(p->home_count.p, 0, sizeof(uint32_t) * (Ti + 1), s));
+    GBN_CUDA(cudaMemsetAsync(p->spread_count.p, 0, sizeof(uint32_t) * Ts, s));
+
+    uint32_t *home_count = p->home_count.as<uint32_t>();
+    GBN_CUDA(launch_prep(dtype, x, y, z, M, p->traj_off_d.as<int64_t>(), p->gs, p->gi, p->desc.df,
+                         p->pts.as<float4>(), p->home_key.as<uint32_t>(), p->touch_count.as<uint32_t>(),
+                         home_count, s));
+    uint32_t *tc = p->touch_count.as<uint32_t>();
+    uint64_t *to = p->touch_off.as<uint64_t>();
+    if (M > 0) {
+        GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceScan::ExclusiveSum(tmp, bytes, tc, to, (int)M, s);
+        }));
+    }
+    uint64_t last_off = 0;
+    uint32_t last_cnt = 0, status = 0;
+    if (M > 0) {
+        GBN_CUDA(cudaMemcpyAsync(&last_off, to + (M - 1), sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        GBN_CUDA(cudaMemcpyAsync(&last_cnt, tc + (M - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    }
+    GBN_CUDA(cudaMemcpyAsync(&status, home_count + Ti, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GBN_CUDA(cudaStreamSynchronize(s));
+    if (status & 1u) return fail(GBN_ERR_ARG, "non-finite trajectory coordinate");
+    const uint64_t E = M > 0 ? last_off + last_cnt : 0;
+    if (E >= ((uint64_t)1 << 31)) return fail(GBN_ERR_CAPACITY, "spread list above 2^31 entries");
+    p->n_dup = (int64_t)E;
+    const size_t Eb = (size_t)std::max<uint64_t>(E, 1);
+    GBN_TRY(ensure(p, p->dup_keys, sizeof(uint32_t) * Eb));
+    GBN_TRY(ensure(p, p->dup_vals, sizeof(uint32_t) * Eb));
+    GBN_TRY(ensure(p, p->dup_keys_sorted, sizeof(uint32_t) * Eb));
+    GBN_TRY(ensure(p, p->dup_idx, sizeof(uint32_t) * Eb));
+    GBN_TRY(ensure(p, p->dup_pts, sizeof(float4) * Eb));
+    uint32_t *scount = p->spread_count.as<uint32_t>();
+    GBN_CUDA(launch_dup_keys(p->pts.as<float4>(), M, p->traj_off_d.as<int64_t>(), nt, p->gs, to,
+                             p->dup_keys.as<uint32_t>(), p->dup_vals.as<uint32_t>(), scount, s));
+    if (E > 0) {
+        uint32_t *kin = p->dup_keys.as<uint32_t>(), *vin = p->dup_vals.as<uint32_t>();
+        uint32_t *kout = p->dup_keys_sorted.as<uint32_t>(), *vout = p->dup_idx.as<uint32_t>();
+        const int bits = key_bits((uint64_t)Ts);
+        GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRadixSort::SortPairs(tmp, bytes, kin, kout, vin, vout, (int)E, 0, bits, s);
+        }));
+        GBN_CUDA(launch_gather_pts(p->pts.as<float4>(), vout, (int64_t)E, p->dup_pts.as<float4>(), s));
+    }
+    if (M > 0) {
+        k_iota<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(p->iota.as<uint32_t>(), M);
+        GBN_CUDA(cudaGetLastError());
+        uint32_t *kin = p->home_key.as<uint32_t>(), *vin = p->iota.as<uint32_t>();
+        uint32_t *kout = p->home_keys_sorted.as<uint32_t>(), *vout = p->home_idx.as<uint32_t>();
+        const int bits = key_bits((uint64_t)Ti);
+        GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRadixSort::SortPairs(tmp, bytes, kin, kout, vin, vout, (int)M, 0, bits, s);
+        }));
+        GBN_CUDA(launch_gather_pts(p->pts.as<float4>(), vout, M, p->home_pts.as<float4>(), s));
+    }
+    GBN_TRY(build_subs(p, p->gs, scount, p->spread_tile_off, p->spread_subs, 1, &p->n_spread_sub, s));
+    GBN_TRY(build_subs(p, p->gi, home_count, p->home_tile_off, p->interp_subs, 0, &p->n_interp_sub, s));
+    GBN_CUDA(cudaStreamSynchronize(s));
+    p->points_set = true;
+    return GBN_OK;
+}
+
+int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
+    if (!desc || !out) return fail(GBN_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (desc->n_coil < 1 || desc->n_traj < 1) return fail(GBN_ERR_ARG, "n_coil and n_traj must be >= 1");
+    if (!std::isfinite(desc->df)) return fail(GBN_ERR_ARG, "df must be finite");
+    gbn_plan *p = new (std::nothrow) gbn_plan();
+    if (!p) return fail(GBN_ERR_ALLOC, "host allocation failed");
+    p->desc = *desc;
+    p->dim = desc->dim;
+    int64_t nf64[3];
+    int st = compute_params(desc->dim, desc->ms, desc->mt, desc->mu, desc->eps, desc->max_nspread, &p->ns, nf64,
+                            &p->tau);
+    if (st != GBN_OK) {
+        delete p;
+        return st;
+    }
+    p->m[0] = desc->ms;
+    p->m[1] = desc->dim > 1 ? desc->mt : 1;
+    p->m[2] = desc->dim > 2 ? desc->mu : 1;
+    p->G = 1;
+    for (int d = 0; d < 3; ++d) {
+        p->nf[d] = (int)nf64[d];
+        p->G *= nf64[d];
+    }
+    if (!cells_fit(p->dim, p->nf)) {
+        delete p;
+        return fail(GBN_ERR_CAPACITY, "oversampled grid too large for the packed cell index");
+    }
+    p->n_inst = (int64_t)desc->n_coil * desc->n_traj;
+
+    // defaults (the autotuner overrides through desc)
+    int dspread[3], dinterp[3];
+    if (p->dim == 1) {
+        dspread[0] = 1024; dinterp[0] = 1024;
+    } else if (p->dim == 2) {
+        dspread[0] = 32; dspread[1] = 32;
+        dinterp[0] = 32; dinterp[1] = 32;
+    } else {
+        dspread[0] = 16; dspread[1] = 16; dspread[2] = 16;
+        dinterp[0] = 8; dinterp[1] = 8; dinterp[2] = 8;
+    }
+    int ts[3] = {1, 1, 1}, ti[3] = {1, 1, 1};
+    for (int d = 0; d < p->dim; ++d) {
+        ts[d] = desc->spread_tile[d] > 0 ? desc->spread_tile[d] : dspread[d];
+        ti[d] = desc->interp_tile[d] > 0 ? desc->interp_tile[d] : dinterp[d];
+    }
+    p->coil_group = desc->coil_group > 0 ? desc->coil_group : 8;
+    if (p->coil_group != 1 && p->coil_group != 2 && p->coil_group != 4 && p->coil_group != 8) {
+        delete p;
+        return fail(GBN_ERR_ARG, "coil_group must be 1, 2, 4 or 8");
+    }
+    p->threads = desc->threads > 0 ? desc->threads : 256;
+    if (p->threads != 128 && p->threads != 256 && p->threads != 512) {
+        delete p;
+        return fail(GBN_ERR_ARG, "threads must be 128, 256 or 512");
+    }
+    p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem : (p->dim == 3 ? 256 : 1024);
+    make_geom(p, ts, p->gs);
+    make_geom(p, ti, p->gi);
+
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) {
+        delete p;
+        return fail(GBN_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+
+    auto bail = [&](int code) {
+        gbn_plan_destroy(p);
+        return code;
+    };
+    const size_t grid_bytes = sizeof(float2) * (size_t)p->G * (size_t)p->n_inst;
+    e = cudaMalloc((void **)&p->grid, grid_bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        p->grid = nullptr;
+        return bail(fail(GBN_ERR_ALLOC, "grid allocation of " + std::to_string(grid_bytes) + " bytes failed"));
+    }
+    p->device_bytes += grid_bytes;
+    for (int d = 0; d < 3; ++d) {
+        e = cudaMalloc((void **)&p->tab[d], sizeof(float) * p->m[d]);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            p->tab[d] = nullptr;
+            return bail(fail(GBN_ERR_ALLOC, "table allocation failed"));
+        }
+        p->device_bytes += sizeof(float) * p->m[d];
+    }
+    e = launch_build_tables(p->dim, p->m, p->nf, p->tau, p->tab[0], p->tab[1], p->tab[2], 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return bail(fail(GBN_ERR_CUDA, std::string("table build: ") + cudaGetErrorString(e)));
+
+    int n[3] = {p->nf[0], p->nf[1], p->nf[2]};
+    if (p->G * p->n_inst >= ((int64_t)1 << 62) || p->n_inst > 0x7FFFFFFF)
+        return bail(fail(GBN_ERR_CAPACITY, "batch too large for cuFFT"));
+    cufftResult r = cufftPlanMany(&p->fft, p->dim, n, nullptr, 1, (int)p->G, nullptr, 1, (int)p->G, CUFFT_C2C,
+                                  (int)p->n_inst);
+    if (r != CUFFT_SUCCESS)
+        return bail(fail(GBN_ERR_CUFFT, "cufftPlanMany failed, cufftResult " + std::to_string((int)r)));
+    p->fft_ok = true;
+    size_t ws = 0;
+    if (cufftGetSize(p->fft, &ws) == CUFFT_SUCCESS) p->device_bytes += ws;
+    *out = p;
+    return GBN_OK;
+}
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+int gbn_version(void) { return 100; }
+
+const char *gbn_status_string(int status) {
+    switch (status) {
+        case GBN_OK: return "ok";
+        case GBN_ERR_ARG: return "invalid argument";
+        case GBN_ERR_ALLOC: return "allocation failed";
+        case GBN_ERR_CUDA: return "CUDA error";
+        case GBN_ERR_CUFFT: return "cuFFT error";
+        case GBN_ERR_STATE: return "invalid call order";
+        case GBN_ERR_CAPACITY: return "size beyond a supported limit";
+        case GBN_ERR_INTERNAL: return "internal error";
+        default: return "unknown status";
+    }
+}
+
+int gbn_last_error(char *buf, int len) {
+    if (!buf || len <= 0) return GBN_ERR_ARG;
+    std::snprintf(buf, (size_t)len, "%s", g_last_error.c_str());
+    return GBN_OK;
+}
+
+int gbn_grid_params(int dim, int ms, int mt, int mu, double eps, int max_nspread, int *nspread, int64_t nf[3],
+                    double *tau) {
+    if (!nspread || !nf || !tau) return fail(GBN_ERR_ARG, "null output pointer");
+    return compute_params(dim, ms, mt, mu, eps, max_nspread, nspread, nf, tau);
+}
+
+int gbn_plan_create(const gbn_plan_desc *desc, gbn_plan **out) {
+    try {
+        return plan_create_impl(desc, out);
+    } catch (...) {
+        return fail(GBN_ERR_INTERNAL, "exception in gbn_plan_create");
+    }
+}
+
+int gbn_plan_destroy(gbn_plan *p) {
+    if (!p) return GBN_OK;
+    if (p->fft_ok) cufftDestroy(p->fft);
+    if (p->grid) cudaFree(p->grid);
+    for (int d = 0; d < 3; ++d)
+        if (p->tab[d]) cudaFree(p->tab[d]);
+    DevBuf *bufs[] = {&p->traj_off_d, &p->grp_scale, &p->pts, &p->home_key, &p->home_keys_sorted,
+                      &p->touch_count, &p->touch_off, &p->home_count, &p->iota, &p->home_idx, &p->home_pts,
+                      &p->dup_keys, &p->dup_vals, &p->dup_keys_sorted, &p->dup_idx, &p->dup_pts,
+                      &p->spread_count, &p->spread_tile_off, &p->home_tile_off, &p->nsub, &p->sub_off,
+                      &p->spread_subs, &p->interp_subs, &p->cub_tmp, &p->scratch, &p->stage_in,
+                      &p->stage_out, &p->stage_w};
+    for (DevBuf *b : bufs) release(*b);
+    delete p;
+    return GBN_OK;
+}
+
+int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
+    if (!p || !o) return fail(GBN_ERR_ARG, "null argument");
+    std::memset(o, 0, sizeof(*o));
+    o->nspread = p->ns;
+    for (int d = 0; d < 3; ++d) {
+        o->nf[d] = p->nf[d];
+        o->spread_tile[d] = p->gs.tile[d];
+        o->interp_tile[d] = p->gi.tile[d];
+    }
+    o->tau = p->tau;
+    o->n_samples = p->M;
+    o->grid_cells = p->G;
+    o->n_inst = p->n_inst;
+    o->spread_subproblems = p->n_spread_sub;
+    o->interp_subproblems = p->n_interp_sub;
+    o->spread_entries = p->n_dup;
+    o->coil_group = p->coil_group;
+    o->threads = p->threads;
+    o->device_bytes = (int64_t)p->device_bytes;
+    return GBN_OK;
+}
+
+int gbn_set_points(gbn_plan *p, int coord_dtype, const void *x, const void *y, const void *z,
+                   const int64_t *traj_offsets, gbn_stream_t stream) {
+    try {
+        return set_points_impl(p, coord_dtype, x, y, z, traj_offsets, (cudaStream_t)stream);
+    } catch (...) {
+        return fail(GBN_ERR_INTERNAL, "exception in gbn_set_points");
+    }
+}
+
+void *gbn_plan_grid(gbn_plan *p) { return p ? (void *)p->grid : nullptr; }
+
+int gbn_spread(gbn_plan *p, const void *c, gbn_layout L, void *grid, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!c || !grid) return fail(GBN_ERR_ARG, "null buffer");
+    return run_spread(p, c, L, nullptr, (float2 *)grid, (cudaStream_t)stream);
+}
+
+int gbn_interp(gbn_plan *p, const void *grid, void *c, gbn_layout L, const float *weight, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!c || !grid) return fail(GBN_ERR_ARG, "null buffer");
+    return run_interp(p, (const float2 *)grid, c, L, weight, (cudaStream_t)stream);
+}
+
+int gbn_fft(gbn_plan *p, void *grid, int direction, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, false));
+    if (!grid) return fail(GBN_ERR_ARG, "null buffer");
+    return fft_exec(p, (float2 *)grid, direction, (cudaStream_t)stream);
+}
+
+int gbn_pad_deapod(gbn_plan *p, const void *img, gbn_layout L, void *grid, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, false));
+    if (!img || !grid) return fail(GBN_ERR_ARG, "null buffer");
+    GBN_CUDA(launch_pad(deapod_args(p, false), (const float2 *)img, L, (float2 *)grid, (cudaStream_t)stream));
+    return GBN_OK;
+}
+
+int gbn_crop_deapod(gbn_plan *p, const void *grid, void *img, gbn_layout L, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!img || !grid) return fail(GBN_ERR_ARG, "null buffer");
+    GBN_CUDA(launch_crop(deapod_args(p, true), (const float2 *)grid, (float2 *)img, L, (cudaStream_t)stream));
+    return GBN_OK;
+}
+
+int gbn_type1(gbn_plan *p, const void *c, gbn_layout cl, const float *weight, void *img, gbn_layout il,
+              gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!c || !img) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    GBN_TRY(run_spread(p, c, cl, weight, p->grid, s));
+    GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
+    GBN_CUDA(launch_crop(deapod_args(p, true), p->grid, (float2 *)img, il, s));
+    return GBN_OK;
+}
+
+int gbn_type2(gbn_plan *p, const void *img, gbn_layout il, void *c, gbn_layout cl, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!c || !img) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    GBN_CUDA(launch_pad(deapod_args(p, false), (const float2 *)img, il, p->grid, s));
+    GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
+    GBN_TRY(run_interp(p, p->grid, c, cl, nullptr, s));
+    return GBN_OK;
+}
+
+int gbn_type21(gbn_plan *p, const void *img, gbn_layout il, void *out, gbn_layout ol, const float *dcf,
+               gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!img || !out) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const gbn_layout sl = {0, 1, p->desc.n_coil};
+    GBN_CUDA(launch_pad(deapod_args(p, false), (const float2 *)img, il, p->grid, s));
+    GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
+    GBN_TRY(run_interp(p, p->grid, p->scratch.p, sl, dcf, s));
+    GBN_TRY(run_spread(p, p->scratch.p, sl, nullptr, p->grid, s));
+    GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
+    GBN_CUDA(launch_crop(deapod_args(p, true), p->grid, (float2 *)out, ol, s));
+    return GBN_OK;
+}
+
+int gbn_sense_forward(gbn_plan *p, const void *x, gbn_layout xl, const void *sens, gbn_layout sl, void *kdata,
+                      gbn_layout kl, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!x || !sens || !kdata) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    GBN_CUDA(launch_pad_sense(deapod_args(p, false), (const float2 *)x, xl, (const float2 *)sens, sl, p->grid, s));
+    GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
+    GBN_TRY(run_interp(p, p->grid, kdata, kl, nullptr, s));
+    return GBN_OK;
+}
+
+int gbn_sense_adjoint(gbn_plan *p, const void *kdata, gbn_layout kl, const float *dcf, const void *sens,
+                      gbn_layout sl, void *x, gbn_layout xl, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!x || !sens || !kdata) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    GBN_TRY(run_spread(p, kdata, kl, dcf, p->grid, s));
+    GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
+    GBN_CUDA(launch_crop_sense(deapod_args(p, true), p->grid, (const float2 *)sens, sl, (float2 *)x, xl, s));
+    return GBN_OK;
+}
+
+int gbn_sense_normal(gbn_plan *p, const void *x, gbn_layout xl, const void *sens, gbn_layout sl,
+                     const float *dcf, void *x_out, gbn_layout ol, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!x || !sens || !x_out) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const gbn_layout scl = {0, 1, p->desc.n_coil};
+    GBN_CUDA(launch_pad_sense(deapod_args(p, false), (const float2 *)x, xl, (const float2 *)sens, sl, p->grid, s));
+    GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
+    GBN_TRY(run_interp(p, p->grid, p->scratch.p, scl, dcf, s));
+    GBN_TRY(run_spread(p, p->scratch.p, scl, nullptr, p->grid, s));
+    GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
+    GBN_CUDA(launch_crop_sense(deapod_args(p, true), p->grid, (const float2 *)sens, sl, (float2 *)x_out, ol, s));
+    return GBN_OK;
+}
+
+int gbn_interp_grad_coords(gbn_plan *p, const void *grid, const void *grad_c, gbn_layout cl, float *grad_xyz,
+                           gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!grid || !grad_c || !grad_xyz) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    GBN_CUDA(cudaMemsetAsync(grad_xyz, 0, sizeof(float) * (size_t)p->M * p->dim, s));
+    GradArgs a;
+    a.g = p->gi;
+    a.subs = p->interp_subs.as<int4>();
+    a.pts = p->home_pts.as<float4>();
+    a.idx = p->home_idx.as<uint32_t>();
+    a.grid = (const float2 *)grid;
+    a.gc = (const float2 *)grad_c;
+    a.c_elem = cl.elem_stride;
+    a.c_coil = cl.coil_stride;
+    a.out = grad_xyz;
+    a.scale = (float)p->desc.df;
+    const int cg = interp_cg(p);
+    GBN_CUDA(launch_interp_grad(a, p->n_interp_sub, cg, p->threads, s));
+    return GBN_OK;
+}
+
+int gbn_graph_capture_normal(gbn_plan *p, const void *x, gbn_layout xl, const void *sens, gbn_layout sl,
+                             const float *dcf, void *x_out, gbn_layout ol, gbn_graph **out) {
+    GBN_TRY(check_plan(p, true));
+    if (!out) return fail(GBN_ERR_ARG, "null output");
+    *out = nullptr;
+    cudaStream_t s;
+    GBN_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    gbn_graph *g = new (std::nothrow) gbn_graph();
+    if (!g) {
+        cudaStreamDestroy(s);
+        return fail(GBN_ERR_ALLOC, "host allocation failed");
+    }
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    int st = GBN_OK;
+    if (e == cudaSuccess) {
+        st = sens ? gbn_sense_normal(p, x, xl, sens, sl, dcf, x_out, ol, (gbn_stream_t)s)
+                  : gbn_type21(p, x, xl, x_out, ol, dcf, (gbn_stream_t)s);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+        if (e2 == cudaSuccess && st == GBN_OK) {
+            g->graph = graph;
+            e = cudaGraphInstantiate(&g->exec, graph, 0);
+        } else {
+            if (graph) cudaGraphDestroy(graph);
+            if (st == GBN_OK) e = e2;
+        }
+    }
+    cudaStreamDestroy(s);
+    if (st != GBN_OK || e != cudaSuccess) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        if (g->graph) cudaGraphDestroy(g->graph);
+        delete g;
+        cudaGetLastError();
+        return st != GBN_OK ? st : fail(GBN_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
+    *out = g;
+    return GBN_OK;
+}
+
+int gbn_graph_launch(gbn_graph *g, gbn_stream_t stream) {
+    if (!g || !g->exec) return fail(GBN_ERR_ARG, "null graph");
+    GBN_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    return GBN_OK;
+}
+
+int gbn_graph_destroy(gbn_graph *g) {
+    if (!g) return GBN_OK;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return GBN_OK;
+}
+
+// ---- host-buffer entry points -----------------------------------------------------------
+static int64_t image_elems(const gbn_plan *p) {
+    return (int64_t)p->m[0] * p->m[1] * p->m[2] * p->desc.n_coil * p->desc.n_traj;
+}
+static gbn_layout host_img_layout(const gbn_plan *p) {
+    const int64_t P = (int64_t)p->m[0] * p->m[1] * p->m[2];
+    return gbn_layout{P * p->desc.n_coil, 1, p->desc.n_coil};
+}
+static gbn_layout host_sample_layout(const gbn_plan *p) { return gbn_layout{0, 1, p->desc.n_coil}; }
+
+int gbn_type1_host(gbn_plan *p, const void *h_c, void *h_img, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!h_c || !h_img) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t cb = sizeof(float2) * (size_t)p->M * p->desc.n_coil, ib = sizeof(float2) * image_elems(p);
+    GBN_TRY(ensure(p, p->stage_in, cb));
+    GBN_TRY(ensure(p, p->stage_out, ib));
+    GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_c, cb, cudaMemcpyHostToDevice, s));
+    GBN_TRY(gbn_type1(p, p->stage_in.p, host_sample_layout(p), nullptr, p->stage_out.p, host_img_layout(p),
+                      stream));
+    GBN_CUDA(cudaMemcpyAsync(h_img, p->stage_out.p, ib, cudaMemcpyDeviceToHost, s));
+    GBN_CUDA(cudaStreamSynchronize(s));
+    return GBN_OK;
+}
+
+int gbn_type2_host(gbn_plan *p, const void *h_img, void *h_c, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!h_c || !h_img) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t cb = sizeof(float2) * (size_t)p->M * p->desc.n_coil, ib = sizeof(float2) * image_elems(p);
+    GBN_TRY(ensure(p, p->stage_in, ib));
+    GBN_TRY(ensure(p, p->stage_out, cb));
+    GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_img, ib, cudaMemcpyHostToDevice, s));
+    GBN_TRY(gbn_type2(p, p->stage_in.p, host_img_layout(p), p->stage_out.p, host_sample_layout(p), stream));
+    GBN_CUDA(cudaMemcpyAsync(h_c, p->stage_out.p, cb, cudaMemcpyDeviceToHost, s));
+    GBN_CUDA(cudaStreamSynchronize(s));
+    return GBN_OK;
+}
+
+int gbn_type21_host(gbn_plan *p, const void *h_img, void *h_out, const float *h_dcf, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (!h_out || !h_img) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t ib = sizeof(float2) * image_elems(p);
+    GBN_TRY(ensure(p, p->stage_in, ib));
+    GBN_TRY(ensure(p, p->stage_out, ib));
+    const float *dcf = nullptr;
+    if (h_dcf) {
+        GBN_TRY(ensure(p, p->stage_w, sizeof(float) * (size_t)p->M));
+        GBN_CUDA(cudaMemcpyAsync(p->stage_w.p, h_dcf, sizeof(float) * (size_t)p->M, cudaMemcpyHostToDevice, s));
+        dcf = p->stage_w.as<float>();
+    }
+    GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_img, ib, cudaMemcpyHostToDevice, s));
+    GBN_TRY(gbn_type21(p, p->stage_in.p, host_img_layout(p), p->stage_out.p, host_img_layout(p), dcf, stream));
+    GBN_CUDA(cudaMemcpyAsync(h_out, p->stage_out.p, ib, cudaMemcpyDeviceToHost, s));
+    GBN_CUDA(cudaStreamSynchronize(s));
+    return GBN_OK;
+}
+
+// ---- one-shot reference-signature calls ---------------------------------------------------
+static int one_shot(int dim, int kind, const double *x, const double *y, const double *z, const void *in,
+                    int64_t M, int32_t ntrail, int32_t ms, int32_t mt, int32_t mu, const double *dcf, double df,
+                    double eps, int32_t iflag, void *out) {
+    if (M < 0 || ntrail < 1 || !x || !in || !out) return fail(GBN_ERR_ARG, "bad argument");
+    if ((dim > 1 && !y) || (dim > 2 && !z)) return fail(GBN_ERR_ARG, "null coordinate");
+    gbn_plan_desc d;
+    std::memset(&d, 0, sizeof(d));
+    d.dim = dim;
+    d.ms = ms;
+    d.mt = dim > 1 ? mt : 1;
+    d.mu = dim > 2 ? mu : 1;
+    d.eps = eps;
+    d.max_nspread = dim == 3 ? 6 : 0;
+    d.iflag = iflag;
+    d.df = df;
+    d.n_coil = ntrail;
+    d.n_traj = 1;
+    gbn_plan *p = nullptr;
+    GBN_TRY(gbn_plan_create(&d, &p));
+    cudaStream_t s = nullptr;
+    double *dc[3] = {nullptr, nullptr, nullptr};
+    float *dw = nullptr;
+    int st = GBN_OK;
+    const double *hc[3] = {x, y, z};
+    auto cleanup = [&]() {
+        for (int k = 0; k < 3; ++k)
+            if (dc[k]) cudaFree(dc[k]);
+        if (dw) cudaFree(dw);
+        if (s) cudaStreamDestroy(s);
+        gbn_plan_destroy(p);
+    };
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+        s = nullptr;
+        cleanup();
+        return fail(GBN_ERR_CUDA, "stream creation failed");
+    }
+    for (int k = 0; k < dim; ++k) {
+        if (cudaMalloc(&dc[k], sizeof(double) * (size_t)std::max<int64_t>(M, 1)) != cudaSuccess ||
+            cudaMemcpyAsync(dc[k], hc[k], sizeof(double) * (size_t)M, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            cudaGetLastError();
+            cleanup();
+            return fail(GBN_ERR_ALLOC, "coordinate upload failed");
+        }
+    }
+    const int64_t off[2] = {0, M};
+    st = gbn_set_points(p, GBN_COORD_F64, dc[0], dc[1], dc[2], off, (gbn_stream_t)s);
+    if (st == GBN_OK && kind == 21 && dcf) {
+        std::vector<float> w((size_t)M);
+        for (int64_t i = 0; i < M; ++i) w[(size_t)i] = (float)dcf[i];
+        st = gbn_type21_host(p, in, out, w.data(), (gbn_stream_t)s);
+    } else if (st == GBN_OK) {
+        if (kind == 1) st = gbn_type1_host(p, in, out, (gbn_stream_t)s);
+        else if (kind == 2) st = gbn_type2_host(p, in, out, (gbn_stream_t)s);
+        else st = gbn_type21_host(p, in, out, nullptr, (gbn_stream_t)s);
+    }
+    cleanup();
+    return st;
+}
+
+int gbn_nufft2d1_gaussker(const double *x, const double *y, const void *c, int64_t M, int32_t ntrail, int32_t ms,
+                          int32_t mt, double df, double eps, int32_t iflag, void *out) {
+    return one_shot(2, 1, x, y, nullptr, c, M, ntrail, ms, mt, 1, nullptr, df, eps, iflag, out);
+}
+int gbn_nufft2d2_gaussker(const double *x, const double *y, const void *Fk, int64_t M, int32_t ntrail, int32_t ms,
+                          int32_t mt, double df, double eps, int32_t iflag, void *out) {
+    return one_shot(2, 2, x, y, nullptr, Fk, M, ntrail, ms, mt, 1, nullptr, df, eps, iflag, out);
+}
+int gbn_nufft2d21_gaussker(const double *x, const double *y, const void *Fk, int64_t M, int32_t ntrail,
+                           int32_t ms, int32_t mt, double df, double eps, int32_t iflag, void *out) {
+    return one_shot(2, 21, x, y, nullptr, Fk, M, ntrail, ms, mt, 1, nullptr, df, eps, iflag, out);
+}
+int gbn_nufft3d1_gaussker(const double *x, const double *y, const double *z, const void *c, int64_t M,
+                          int32_t ntrail, int32_t ms, int32_t mt, int32_t mu, double df, double eps, int32_t iflag,
+                          void *out) {
+    return one_shot(3, 1, x, y, z, c, M, ntrail, ms, mt, mu, nullptr, df, eps, iflag, out);
+}
+int gbn_nufft3d2_gaussker(const double *x, const double *y, const double *z, const void *Fk, int64_t M,
+                          int32_t ntrail, int32_t ms, int32_t mt, int32_t mu, double df, double eps, int32_t iflag,
+                          void *out) {
+    return one_shot(3, 2, x, y, z, Fk, M, ntrail, ms, mt, mu, nullptr, df, eps, iflag, out);
+}
+int gbn_nufft3d21_gaussker(const double *x, const double *y, const double *z, const void *Fk, int64_t M,
+                           int32_t ntrail, int32_t ms, int32_t mt, int32_t mu, const double *dcf, double df,
+                           double eps, int32_t iflag, void *out) {
+    return one_shot(3, 21, x, y, z, Fk, M, ntrail, ms, mt, mu, dcf, df, eps, iflag, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,156 @@
+// Internal definitions shared by the gbnufft CUDA translation units.
+//
+// Data layout in HBM (one plan):
+//   grid      (n_traj * n_coil, nf1, nf2, nf3) complex64, instance-major, cuFFT-contiguous
+//   pts       (M_total) float4 {f0, f1, f2, packed first-tap cells} per sample; f_d in [0, 1)
+//             is the sample's position inside its grid cell, computed in FP64 from x*df mod 2pi
+//   home list (M_total) samples sorted by (group, interp home bin): pts + sample index
+//   dup list  (E) (sample, spread tile) pairs sorted by (group, tile): every tile a sample's
+//             stencil touches, so each spread block owns a disjoint output tile
+//   subs      int4 {tile id, start, length, flags} work items of <= max_subproblem samples
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbnufft.h"
+
+namespace gbn {
+
+constexpr int kMaxW = 40;          // 2*nspread; nspread <= 20 (eps down to 1e-33 in 2-D gives 17)
+constexpr int kSplitFlag = 1;      // tile is covered by more than one subproblem
+constexpr int kFirstFlag = 2;      // first subproblem of its tile
+
+struct Geom {
+    int dim;
+    int ns;          // nspread
+    int W;           // taps per dim = 2*ns
+    int nf[3];       // oversampled grid (1 beyond dim)
+    int tile[3];     // tile size (cells) of the kernel this geometry serves
+    int ntile[3];    // tiles per dim
+    int ntiles;      // tiles per trajectory group
+    float beta2[3];  // weight(d) = exp2(-beta2 * d^2), d in cells; beta = h^2/(4 tau), * log2(e)
+    int64_t G;       // cells per instance
+    int n_coil;
+    int n_traj;
+};
+
+// ---- packed first-tap cell indices ------------------------------------------------------
+// dim 1: c0 < 2^31; dim 2: c0, c1 < 2^16; dim 3: c0, c1 < 2^11, c2 < 2^10
+__host__ __device__ inline uint32_t pack_cells(int dim, int c0, int c1, int c2) {
+    if (dim == 1) return (uint32_t)c0;
+    if (dim == 2) return (uint32_t)c0 | ((uint32_t)c1 << 16);
+    return (uint32_t)c0 | ((uint32_t)c1 << 11) | ((uint32_t)c2 << 22);
+}
+__host__ __device__ inline void unpack_cells(int dim, uint32_t p, int &c0, int &c1, int &c2) {
+    if (dim == 1) { c0 = (int)p; c1 = 0; c2 = 0; return; }
+    if (dim == 2) { c0 = (int)(p & 0xFFFFu); c1 = (int)(p >> 16); c2 = 0; return; }
+    c0 = (int)(p & 0x7FFu); c1 = (int)((p >> 11) & 0x7FFu); c2 = (int)(p >> 22);
+}
+inline bool cells_fit(int dim, const int nf[3]) {
+    if (dim == 1) return nf[0] < (1 << 30);
+    if (dim == 2) return nf[0] <= 65536 && nf[1] <= 65536;
+    return nf[0] <= 2048 && nf[1] <= 2048 && nf[2] <= 1024;
+}
+
+// tiles a stencil of W cells starting at cell0 touches, walking forward with wrap
+__host__ __device__ inline int touched_tiles(int cell0, int W, int nf, int T, int ntile) {
+    int t = cell0 / T, pos = cell0, remaining = W, count = 0;
+    while (remaining > 0 && count < ntile) {
+        int tile_end = min((t + 1) * T, nf);
+        int take = min(remaining, tile_end - pos);
+        remaining -= take;
+        ++count;
+        pos = tile_end;
+        ++t;
+        if (pos >= nf) { pos = 0; t = 0; }
+    }
+    return count;
+}
+
+__device__ __forceinline__ int wrap_pos(int v, int n) {  // v in (-n, 2n)
+    v = v < 0 ? v + n : v;
+    return v >= n ? v - n : v;
+}
+
+// ---- internal launchers (defined in the .cu files) -------------------------------------
+struct SortBuffers;
+
+// prep.cu
+cudaError_t launch_prep(int coord_dtype, const void *x, const void *y, const void *z, int64_t M,
+                        const int64_t *d_traj_off, const Geom &gs, const Geom &gi, double df,
+                        float4 *pts, uint32_t *home_key, uint32_t *touch_count, uint32_t *home_count,
+                        cudaStream_t s);
+cudaError_t launch_dup_keys(const float4 *pts, int64_t M, const int64_t *d_traj_off, int n_traj,
+                            const Geom &gs, const uint64_t *touch_off, uint32_t *keys, uint32_t *vals,
+                            uint32_t *tile_count, cudaStream_t s);
+cudaError_t launch_gather_pts(const float4 *pts, const uint32_t *idx, int64_t n, float4 *out,
+                              cudaStream_t s);
+cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
+                              int64_t ntiles_total, int max_sub, int every_tile, int4 *subs,
+                              cudaStream_t s);
+cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int every_tile,
+                              uint32_t *n_sub, cudaStream_t s);
+
+// grid.cu
+struct SpreadArgs {
+    Geom g;
+    const int4 *subs;
+    const float4 *pts;        // dup-list order
+    const uint32_t *idx;      // dup-list sample index
+    const float2 *c;          // samples
+    int64_t c_elem, c_coil;   // strides (complex elements)
+    const float *weight;      // per sample (original index) or null: density compensation
+    float2 *grid;
+};
+struct InterpArgs {
+    Geom g;
+    const int4 *subs;
+    const float4 *pts;        // home order
+    const uint32_t *idx;      // home order sample index
+    const float2 *grid;
+    float2 *c;
+    int64_t c_elem, c_coil;
+    const float *weight;      // per sample (original index) or null
+};
+struct GradArgs {
+    Geom g;
+    const int4 *subs;
+    const float4 *pts;
+    const uint32_t *idx;
+    const float2 *grid;
+    const float2 *gc;         // upstream gradient of the samples
+    int64_t c_elem, c_coil;
+    float *out;               // (M, dim)
+    float scale;              // df
+};
+cudaError_t launch_zero_split(const Geom &g, const int4 *subs, int64_t n_sub, float2 *grid,
+                              cudaStream_t s);
+cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads,
+                          cudaStream_t s);
+cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, int threads,
+                          cudaStream_t s);
+cudaError_t launch_interp_grad(const GradArgs &a, int64_t n_sub, int coil_group, int threads,
+                               cudaStream_t s);
+size_t spread_smem_bytes(const Geom &g, int coil_group);
+size_t interp_smem_bytes(const Geom &g, int coil_group);
+
+// deapod.cu
+struct DeapodArgs {
+    Geom g;                    // nf, dim, n_coil, n_traj
+    int m[3];                  // image size (1 beyond dim)
+    const float *tab[3];       // per-dim factor sqrt(pi/tau) exp(tau k^2) / nf_d, index i = k + m/2
+    const float *grp_scale;    // per trajectory group (crop: 1/M_g) or null (= 1)
+};
+cudaError_t launch_build_tables(int dim, const int m[3], const int nf[3], double tau, float *tab0,
+                                float *tab1, float *tab2, cudaStream_t s);
+cudaError_t launch_pad(const DeapodArgs &a, const float2 *img, gbn_layout L, float2 *grid,
+                       cudaStream_t s);
+cudaError_t launch_crop(const DeapodArgs &a, const float2 *grid, float2 *img, gbn_layout L,
+                        cudaStream_t s);
+cudaError_t launch_pad_sense(const DeapodArgs &a, const float2 *x, gbn_layout XL, const float2 *sens,
+                             gbn_layout SL, float2 *grid, cudaStream_t s);
+cudaError_t launch_crop_sense(const DeapodArgs &a, const float2 *grid, const float2 *sens,
+                              gbn_layout SL, float2 *x, gbn_layout XL, cudaStream_t s);
+
+}  // namespace gbn

@@ -1,0 +1,51 @@
+// Interp (type-2 gridding) and trajectory-gradient launchers.
+#include "dispatch.cuh"
+
+namespace gbn {
+
+size_t interp_smem_bytes(const Geom &g, int coil_group) {
+    size_t cells = 1;
+    for (int d = 0; d < g.dim; ++d) cells *= (size_t)(g.tile[d] + g.W - 1);
+    return cells * (size_t)coil_group * sizeof(float2);
+}
+
+cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, int threads, cudaStream_t s) {
+    if (n_sub == 0) return cudaSuccess;
+    const size_t smem = interp_smem_bytes(a.g, coil_group);
+    const dim3 grid((unsigned)n_sub, (unsigned)((a.g.n_coil + coil_group - 1) / coil_group));
+    cudaError_t err = cudaSuccess;
+    GBN_DISPATCH_D(a.g.dim, GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
+        auto kern = k_interp<D, WT, CG>;
+        err = set_smem(kern, smem);
+        if (err == cudaSuccess) {
+            kern<<<grid, threads, smem, s>>>(a);
+            err = cudaGetLastError();
+        }
+    })));
+    return err;
+}
+
+cudaError_t launch_interp_grad(const GradArgs &a, int64_t n_sub, int coil_group, int threads, cudaStream_t s) {
+    if (n_sub == 0) return cudaSuccess;
+    const size_t smem = interp_smem_bytes(a.g, coil_group);
+    const dim3 grid((unsigned)n_sub, (unsigned)((a.g.n_coil + coil_group - 1) / coil_group));
+    // dw/dx = w * (-2 beta d / h) with beta = beta2 / log2(e), h = 2 pi / nf
+    float dsc[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < a.g.dim; ++d) {
+        const double beta = (double)a.g.beta2[d] / 1.4426950408889634;
+        const double h = 6.283185307179586 / a.g.nf[d];
+        dsc[d] = (float)(-2.0 * beta / h);
+    }
+    cudaError_t err = cudaSuccess;
+    GBN_DISPATCH_D(a.g.dim, GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
+        auto kern = k_interp_grad<D, WT, CG>;
+        err = set_smem(kern, smem);
+        if (err == cudaSuccess) {
+            kern<<<grid, threads > 256 ? 256 : threads, smem, s>>>(a, dsc[0], dsc[1], dsc[2]);
+            err = cudaGetLastError();
+        }
+    })));
+    return err;
+}
+
+}  // namespace gbn

@@ -1,0 +1,34 @@
+// Spread (type-1 gridding) launchers.
+#include "dispatch.cuh"
+
+namespace gbn {
+
+size_t spread_smem_bytes(const Geom &g, int coil_group) {
+    size_t cells = 1;
+    for (int d = 0; d < g.dim; ++d) cells *= (size_t)g.tile[d];
+    return cells * (size_t)coil_group * sizeof(float2);
+}
+
+cudaError_t launch_zero_split(const Geom &g, const int4 *subs, int64_t n_sub, float2 *grid, cudaStream_t s) {
+    if (n_sub == 0) return cudaSuccess;
+    GBN_DISPATCH_D(g.dim, (k_zero_split<D><<<(unsigned)n_sub, 256, 0, s>>>(g, subs, grid)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads, cudaStream_t s) {
+    if (n_sub == 0) return cudaSuccess;
+    const size_t smem = spread_smem_bytes(a.g, coil_group);
+    const dim3 grid((unsigned)n_sub, (unsigned)((a.g.n_coil + coil_group - 1) / coil_group));
+    cudaError_t err = cudaSuccess;
+    GBN_DISPATCH_D(a.g.dim, GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
+        auto kern = k_spread<D, WT, CG>;
+        err = set_smem(kern, smem);
+        if (err == cudaSuccess) {
+            kern<<<grid, threads, smem, s>>>(a);
+            err = cudaGetLastError();
+        }
+    })));
+    return err;
+}
+
+}  // namespace gbn

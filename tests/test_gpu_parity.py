@@ -1,0 +1,356 @@
+"""GPU parity: the sm_103a NUFFT against mripy's own outputs (golden vectors), the FP64
+oracle restatement, and the exact NUDFT.
+
+Tolerances (relative L2):
+  TOL_REF = 2e-5  GPU (complex64 data, FP32 stencil) vs the reference / oracle at the
+                  same eps (FP64): the difference is FP32 rounding only
+  TOL_EXACT = 1e-4  vs the FP64 NUDFT at nspread 6 (the accuracy target)
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from mripy_gb300 import nufft_func as nf
+from mripy_gb300 import operators as ops
+from mripy_gb300 import synth
+from mripy_gb300._native import GbnError
+from mripy_gb300.plan import NufftPlan
+
+pytestmark = pytest.mark.gpu
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+TOL_REF = 2e-5
+TOL_EXACT = 1e-4
+
+
+def rel(a, b):
+    a = a.cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = b.cpu().numpy() if isinstance(b, torch.Tensor) else np.asarray(b)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def cvec(rng, shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+
+def cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda")
+
+
+# ------------------------------------------------------------------ golden vectors
+@pytest.fixture(scope="module")
+def g1():
+    return np.load(os.path.join(G, "golden_1d.npz"))
+
+
+@pytest.fixture(scope="module")
+def g2():
+    return np.load(os.path.join(G, "golden_2d.npz"))
+
+
+@pytest.fixture(scope="module")
+def g3():
+    return np.load(os.path.join(G, "golden_3d.npz"))
+
+
+@pytest.mark.parametrize("eps,tag", [(5e-6, "e5em6"), (1e-3, "e1em3")])
+@pytest.mark.parametrize("df", [1.0, 2.0])
+@pytest.mark.parametrize("iflag", [1, -1])
+def test_golden_1d(g1, eps, tag, df, iflag):
+    key = "%s_df%d_if%+d" % (tag, int(df), iflag)
+    x, c, Fk = g1["x"], g1["c"], g1["Fk"]
+    assert rel(nf.nufft1d1_gaussker(x, c, 20, df=df, eps=eps, iflag=iflag), g1["t1_" + key]) < TOL_REF
+    assert rel(nf.nufft1d2_gaussker(x, Fk, 20, df=df, eps=eps, iflag=iflag), g1["t2_" + key]) < TOL_REF
+    assert rel(nf.nufft1d21_gaussker(x, Fk, 20, df=df, eps=eps, iflag=iflag), g1["t21_" + key]) < TOL_REF
+
+
+@pytest.mark.parametrize("eps,tag", [(5e-6, "e5em6"), (1e-5, "e1em5")])
+@pytest.mark.parametrize("df", [1.0, 2.0])
+@pytest.mark.parametrize("iflag", [1, -1])
+def test_golden_2d(g2, eps, tag, df, iflag):
+    key = "a_%s_df%d_if%+d" % (tag, int(df), iflag)
+    x, y, c, Fk = g2["a_x"], g2["a_y"], g2["a_c"], g2["a_Fk"]
+    out1 = nf.nufft2d1_gaussker(x, y, c, 16, 16, df=df, eps=eps, iflag=iflag)
+    assert out1.dtype == np.complex128 and out1.shape == (16, 16)
+    assert rel(out1, g2["t1_" + key]) < TOL_REF
+    assert rel(nf.nufft2d2_gaussker(x, y, Fk, 16, 16, df=df, eps=eps, iflag=iflag), g2["t2_" + key]) < TOL_REF
+    assert rel(nf.nufft2d21_gaussker(x, y, Fk, 16, 16, df=df, eps=eps, iflag=iflag), g2["t21_" + key]) < TOL_REF
+
+
+@pytest.mark.parametrize("eps,tag", [(1e-5, "e1em5"), (1e-3, "e1em3")])
+def test_golden_2d_coils_odd_sizes(g2, eps, tag):
+    key = "b_" + tag
+    x, y, c, Fk = g2["b_x"], g2["b_y"], g2["b_c"], g2["b_Fk"]
+    assert rel(nf.nufft2d1_gaussker_cuda(x, y, c, 15, 12, eps=eps), g2["t1_" + key]) < TOL_REF
+    assert rel(nf.nufft2d2_gaussker_cuda(x, y, Fk, 15, 12, eps=eps), g2["t2_" + key]) < TOL_REF
+    assert rel(nf.nufft2d21_gaussker_cuda(x, y, Fk, 15, 12, eps=eps), g2["t21_" + key]) < TOL_REF
+
+
+@pytest.mark.parametrize("eps,tag", [(5e-6, "e5em6"), (1e-5, "e1em5")])
+@pytest.mark.parametrize("iflag", [1, -1])
+def test_golden_3d(g3, eps, tag, iflag):
+    key = "a_%s_if%+d" % (tag, iflag)
+    x, y, z, c, Fk, dcf = (g3[k] for k in ("a_x", "a_y", "a_z", "a_c", "a_Fk", "a_dcf"))
+    assert rel(nf.nufft3d1_gaussker(x, y, z, c, 8, 8, 6, eps=eps, iflag=iflag), g3["t1_" + key]) < TOL_REF
+    assert rel(nf.nufft3d2_gaussker(x, y, z, Fk, 8, 8, 6, eps=eps, iflag=iflag), g3["t2_" + key]) < TOL_REF
+    assert rel(nf.nufft3d21_gaussker(x, y, z, Fk, 8, 8, 6, dcf=dcf, eps=eps, iflag=iflag),
+               g3["t21_" + key]) < TOL_REF
+
+
+def test_golden_3d_clamp_and_cuda_names(g3):
+    x, y, z, c = (g3[k] for k in ("a_x", "a_y", "a_z", "a_c"))
+    assert rel(nf.nufft3d1_gaussker_cuda(x, y, z, c, 8, 8, 6, eps=1e-12), g3["t1_a_e1em12_if+1"]) < TOL_REF
+
+
+def test_golden_operator_nufft3d(g3):
+    for cls in (ops.NUFFT3d, ops.NUFFT3d_cuda):
+        op = cls(tuple(int(v) for v in g3["b_shape"]), g3["b_dcf"])
+        op.normalize_set_ktraj(g3["b_ktraj"].copy())
+        assert rel(op.forward(g3["b_im"]), g3["b_forward"]) < TOL_REF
+        assert rel(op.backward(g3["b_kdata"]), g3["b_backward"]) < TOL_REF
+        assert rel(op.forward_backward(g3["b_im"]), g3["b_forward_backward"]) < TOL_REF
+
+
+# ------------------------------------------------------------------ configuration 1 at full size
+def test_config1_against_oracle_and_nudft():
+    cfg = synth.config1()
+    kx, ky = cfg["k"]
+    x, y = 2 * np.pi * kx, 2 * np.pi * ky
+    img = cfg["image"]
+    # forward (type-2) and adjoint (type-1), drop-in functions, nspread 6
+    c_gpu = nf.nufft2d2_gaussker(x, y, img, 128, 128, eps=5e-6)
+    c_orc = O.nufft_type2((x, y), img.astype(np.complex128), (128, 128), eps=5e-6)
+    assert rel(c_gpu, c_orc) < TOL_REF
+    rng = np.random.default_rng(7)
+    sub = rng.choice(len(x), 4096, replace=False)
+    c_exact = O.nudft_type2((x[sub], y[sub]), img.astype(np.complex128), (128, 128))
+    assert rel(c_gpu[sub], c_exact) < TOL_EXACT
+
+    cdat = cvec(rng, len(x)).astype(np.complex128)
+    F_gpu = nf.nufft2d1_gaussker(x, y, cdat, 128, 128, eps=5e-6)
+    F_orc = O.nufft_type1((x, y), cdat, (128, 128), eps=5e-6)
+    assert rel(F_gpu, F_orc) < TOL_REF
+    pix = rng.choice(128 * 128, 1024, replace=False)
+    F_exact = O.nudft_type1((x, y), cdat, (128, 128)).reshape(-1)[pix]
+    assert rel(F_gpu.reshape(-1)[pix], F_exact) < TOL_EXACT
+
+
+def test_adjoint_identity_plan():
+    rng = np.random.default_rng(11)
+    M = 20000
+    x = cuda(rng.uniform(-np.pi, np.pi, M))
+    y = cuda(rng.uniform(-np.pi, np.pi, M))
+    p = NufftPlan(2, (96, 80), n_coil=2, eps=5e-6).set_points([x, y])
+    F = cuda(cvec(rng, (1, 96, 80, 2)))
+    c = cuda(cvec(rng, (M, 2)))
+    AF = p.type2(F)
+    ATc = p.type1(c) * M            # type-1 carries 1/M
+    lhs = torch.vdot(c.reshape(-1), AF.reshape(-1)).item()
+    rhs = torch.vdot(ATc.reshape(-1), F.reshape(-1)).item()
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+
+
+# ------------------------------------------------------------------ layouts, coils, ragged groups
+def test_coil_layouts_and_oracle():
+    rng = np.random.default_rng(12)
+    M, nc = 5000, 3
+    xs = rng.uniform(-3 * np.pi, 3 * np.pi, (2, M))           # wraps mod 2 pi
+    p = NufftPlan(2, (40, 36), n_coil=nc, eps=1e-5).set_points([cuda(xs[0]), cuda(xs[1])])
+    c_np = cvec(rng, (M, nc))
+    c_last = cuda(c_np)                                       # (M, nc) coil-last
+    c_major = cuda(np.ascontiguousarray(c_np.T)).t()          # (M, nc) view of (nc, M)
+    F1 = p.type1(c_last)
+    F2 = p.type1(c_major)
+    assert rel(F1, F2) < 1e-6
+    F_orc = O.nufft_type1((xs[0], xs[1]), c_np.astype(np.complex128), (40, 36), eps=1e-5)
+    assert rel(F1[0], F_orc) < TOL_REF
+    img = cvec(rng, (40, 36, nc))
+    k1 = p.type2(cuda(img)[None])
+    img_major = cuda(np.ascontiguousarray(np.moveaxis(img, -1, 0)))   # (nc, 40, 36)
+    k2 = p.type2(img_major.permute(1, 2, 0)[None])
+    assert rel(k1, k2) < 1e-6
+    assert rel(k1, O.nufft_type2((xs[0], xs[1]), img.astype(np.complex128), (40, 36), eps=1e-5)) < TOL_REF
+
+
+def test_ragged_groups_match_per_group_oracle():
+    rng = np.random.default_rng(13)
+    counts = [3000, 0, 1234, 7000]
+    off = np.concatenate([[0], np.cumsum(counts)])
+    M, nc = int(off[-1]), 2
+    xs = rng.uniform(-np.pi, np.pi, (2, M))
+    p = NufftPlan(2, (48, 48), n_coil=nc, n_traj=len(counts), eps=5e-6)
+    p.set_points([cuda(xs[0]), cuda(xs[1])], traj_offsets=off.tolist())
+    c = cvec(rng, (M, nc))
+    F = p.type1(cuda(c)).cpu().numpy()                       # (4, 48, 48, nc)
+    img = cvec(rng, (len(counts), 48, 48, nc))
+    k = p.type2(cuda(img)).cpu().numpy()
+    for g, (a, b) in enumerate(zip(off[:-1], off[1:])):
+        if b == a:
+            assert np.abs(F[g]).max() == 0.0
+            continue
+        Fo = O.nufft_type1((xs[0][a:b], xs[1][a:b]), c[a:b].astype(np.complex128), (48, 48), eps=5e-6)
+        assert rel(F[g], Fo) < TOL_REF
+        ko = O.nufft_type2((xs[0][a:b], xs[1][a:b]), img[g].astype(np.complex128), (48, 48), eps=5e-6)
+        assert rel(k[a:b], ko) < TOL_REF
+
+
+def test_float32_coordinates():
+    rng = np.random.default_rng(14)
+    xs = rng.uniform(-np.pi, np.pi, (2, 4000)).astype(np.float32)
+    img = cvec(rng, (32, 32))
+    out = nf.nufft2d2_gaussker(cuda(xs[0]), cuda(xs[1]), cuda(img), 32, 32, eps=1e-5)
+    assert out.dtype == torch.complex64 and out.is_cuda
+    ref = O.nufft_type2((xs[0].astype(np.float64), xs[1].astype(np.float64)), img.astype(np.complex128),
+                        (32, 32), eps=1e-5)
+    assert rel(out, ref) < TOL_REF
+
+
+def test_large_nspread_generic_kernel():
+    # function default eps 1e-15: ratio 3, nspread 14 (28 taps per dim, generic kernel)
+    rng = np.random.default_rng(15)
+    x, y = rng.uniform(-np.pi, np.pi, (2, 600))
+    c = cvec(rng, 600).astype(np.complex128)
+    F = cvec(rng, (20, 18)).astype(np.complex128)
+    assert rel(nf.nufft2d1_gaussker(x, y, c, 20, 18), O.nufft_type1((x, y), c, (20, 18))) < TOL_REF
+    assert rel(nf.nufft2d2_gaussker(x, y, F, 20, 18), O.nufft_type2((x, y), F, (20, 18))) < TOL_REF
+    assert rel(nf.nufft2d1_gaussker(x, y, c, 20, 18), O.nudft_type1((x, y), c, (20, 18))) < 1e-5
+
+
+def test_3d_multicoil_against_oracle():
+    rng = np.random.default_rng(16)
+    M, nc = 3000, 3
+    xs = rng.uniform(-np.pi, np.pi, (3, M))
+    c = cvec(rng, (M, nc)).astype(np.complex128)
+    F = cvec(rng, (20, 18, 16, nc)).astype(np.complex128)
+    dcf = rng.uniform(0.5, 1.5, M)
+    for eps in (5e-6, 1e-5):
+        assert rel(nf.nufft3d1_gaussker(*xs, c, 20, 18, 16, eps=eps),
+                   O.nufft_type1(tuple(xs), c, (20, 18, 16), eps=eps)) < TOL_REF
+        assert rel(nf.nufft3d2_gaussker(*xs, F, 20, 18, 16, eps=eps),
+                   O.nufft_type2(tuple(xs), F, (20, 18, 16), eps=eps)) < TOL_REF
+        assert rel(nf.nufft3d21_gaussker(*xs, F, 20, 18, 16, dcf=dcf, eps=eps),
+                   O.nufft_type21(tuple(xs), F, (20, 18, 16), dcf=dcf, eps=eps)) < TOL_REF
+
+
+# ------------------------------------------------------------------ SENSE fusion and graphs
+def test_sense_fused_kernels_match_composition():
+    rng = np.random.default_rng(17)
+    shape, nc, M = (64, 48), 4, 12000
+    xs = rng.uniform(-np.pi, np.pi, (2, M))
+    p = NufftPlan(2, shape, n_coil=nc, eps=5e-6).set_points([cuda(xs[0]), cuda(xs[1])])
+    S = cuda(synth.coil_maps(shape, nc, rng))
+    x = cuda(cvec(rng, (1,) + shape))
+    dcf = cuda(rng.uniform(0.2, 1.0, M).astype(np.float32))
+    k = p.sense_forward(x, S)
+    k_ref = p.type2((x[..., None] * S[None]).contiguous())
+    assert rel(k, k_ref) < 1e-6
+    xa = p.sense_adjoint(k, S, dcf=dcf)
+    xa_ref = (p.type1((k * dcf[:, None]).contiguous()) * S.conj()[None]).sum(-1)
+    assert rel(xa, xa_ref) < 1e-6
+    xn = p.sense_normal(x, S, dcf=dcf)
+    xn_ref = (p.type21((x[..., None] * S[None]).contiguous(), dcf=dcf) * S.conj()[None]).sum(-1)
+    assert rel(xn, xn_ref) < 1e-6
+
+
+def test_graph_replay_matches_eager():
+    rng = np.random.default_rng(18)
+    shape, nc, M = (64, 64), 8, 20000
+    xs = rng.uniform(-np.pi, np.pi, (2, M))
+    p = NufftPlan(2, shape, n_coil=nc, eps=5e-6).set_points([cuda(xs[0]), cuda(xs[1])])
+    S = cuda(synth.coil_maps(shape, nc, rng))
+    xb = cuda(cvec(rng, (1,) + shape))
+    ob = torch.empty_like(xb)
+    eager = p.sense_normal(xb, S).clone()
+    g = p.capture_normal(xb, ob, sens=S)
+    g.launch()
+    torch.cuda.synchronize()
+    assert rel(ob, eager) < 1e-6
+    xb.copy_(cuda(cvec(rng, (1,) + shape)))                  # new input, same buffer
+    g.launch()
+    torch.cuda.synchronize()
+    assert rel(ob, p.sense_normal(xb, S)) < 1e-6
+    g.close()
+
+
+def test_joint_operator_fused_path_matches_generic():
+    rng = np.random.default_rng(19)
+    shape, nc = (48, 40), 3
+    kx, ky = synth.golden_radial_2d(60, 96)
+    S = synth.coil_maps(shape, nc, rng)
+    nft = ops.NUFFT2d(shape)
+    nft.set_ktraj(2 * np.pi * kx, 2 * np.pi * ky)
+    A = ops.joint2operators(ops.espirit(S), nft)
+    x = cvec(rng, shape + (1,))
+    kd = A.forward(x)
+    kd_ref = nft.forward(S * x)
+    assert rel(kd, kd_ref) < 1e-5
+    xb = A.backward(kd)
+    xb_ref = np.sum(np.conj(S) * nft.backward(kd), axis=-1, keepdims=True)
+    assert rel(xb, xb_ref) < 1e-5
+    xn = A.forward_backward(x)
+    xn_ref = np.sum(np.conj(S) * nft.forward_backward(S * x), axis=-1, keepdims=True)
+    assert rel(xn, xn_ref) < 1e-5
+
+
+# ------------------------------------------------------------------ trajectory gradient
+def test_interp_grad_coords_against_fp64_gradients():
+    rng = np.random.default_rng(20)
+    shape, M = (24, 20), 300
+    xs = rng.uniform(-np.pi, np.pi, (2, M))
+    F = cvec(rng, shape).astype(np.complex128)
+    gc = cvec(rng, M).astype(np.complex128)
+    p = NufftPlan(2, shape, n_coil=1, eps=5e-6).set_points([cuda(xs[0]), cuda(xs[1])])
+    grid = p.pad_deapod(cuda(F.astype(np.complex64))[None, ..., None])
+    p.fft(grid, -1)
+    gk = p.interp_grad_coords(grid, cuda(gc.astype(np.complex64))[:, None]).cpu().numpy()
+    exact = O.nudft_type2_coord_grad((xs[0], xs[1]), F, shape, gc)
+    assert rel(gk, exact) < 1e-3
+    # FP64 central differences of the FP64 gridding oracle, step 1e-6
+    h = 1e-6
+    for j in (0, 17, 150, 299):
+        for d in range(2):
+            xp, xm = xs.copy(), xs.copy()
+            xp[d, j] += h
+            xm[d, j] -= h
+            cp = O.nufft_type2((xp[0], xp[1]), F, shape, eps=5e-6)
+            cm = O.nufft_type2((xm[0], xm[1]), F, shape, eps=5e-6)
+            fd = np.real(np.vdot(gc, (cp - cm) / (2 * h)))
+            assert abs(gk[j, d] - fd) <= 1e-3 * np.abs(exact).max()
+
+
+# ------------------------------------------------------------------ failure paths
+def test_non_finite_coordinate_is_rejected():
+    x = torch.zeros(100, dtype=torch.float64, device="cuda")
+    y = torch.zeros(100, dtype=torch.float64, device="cuda")
+    x[37] = float("nan")
+    p = NufftPlan(2, (16, 16), eps=1e-5)
+    with pytest.raises(GbnError) as ei:
+        p.set_points([x, y])
+    assert ei.value.status == 1 and "non-finite" in str(ei.value)
+    with pytest.raises(GbnError):
+        p.type2(torch.zeros((1, 16, 16, 1), dtype=torch.complex64, device="cuda"))
+
+
+def test_shape_and_dtype_errors():
+    p = NufftPlan(2, (16, 16), n_coil=2, eps=1e-5)
+    x = torch.zeros(10, dtype=torch.float64, device="cuda")
+    p.set_points([x, x])
+    with pytest.raises(ValueError):
+        p.type2(torch.zeros((1, 16, 15, 2), dtype=torch.complex64, device="cuda"))
+    with pytest.raises(TypeError):
+        p.type2(torch.zeros((1, 16, 16, 2), dtype=torch.complex128, device="cuda"))
+    with pytest.raises(ValueError):
+        p.set_points([x, x], traj_offsets=[0, 5])
+
+
+def test_empty_trajectory():
+    p = NufftPlan(2, (16, 16), eps=1e-5)
+    e = torch.zeros(0, dtype=torch.float64, device="cuda")
+    p.set_points([e, e])
+    out = p.type1(torch.zeros((0, 1), dtype=torch.complex64, device="cuda"))
+    assert out.shape == (1, 16, 16, 1) and torch.count_nonzero(out) == 0
+    k = p.type2(torch.ones((1, 16, 16, 1), dtype=torch.complex64, device="cuda"))
+    assert k.shape == (0, 1)
