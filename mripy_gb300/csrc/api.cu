@@ -599,13 +599,13 @@ void *gbn_plan_grid(gbn_plan *p) { return p ? (void *)p->grid : nullptr; }
 
 int gbn_spread(gbn_plan *p, const void *c, gbn_layout L, void *grid, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!c || !grid) return fail(GBN_ERR_ARG, "null buffer");
+    if ((!c && p->M > 0) || !grid) return fail(GBN_ERR_ARG, "null buffer");
     return run_spread(p, c, L, nullptr, (float2 *)grid, (cudaStream_t)stream);
 }
 
 int gbn_interp(gbn_plan *p, const void *grid, void *c, gbn_layout L, const float *weight, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!c || !grid) return fail(GBN_ERR_ARG, "null buffer");
+    if ((!c && p->M > 0) || !grid) return fail(GBN_ERR_ARG, "null buffer");
     return run_interp(p, (const float2 *)grid, c, L, weight, (cudaStream_t)stream);
 }
 
@@ -632,7 +632,7 @@ int gbn_crop_deapod(gbn_plan *p, const void *grid, void *img, gbn_layout L, gbn_
 int gbn_type1(gbn_plan *p, const void *c, gbn_layout cl, const float *weight, void *img, gbn_layout il,
               gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!c || !img) return fail(GBN_ERR_ARG, "null buffer");
+    if ((!c && p->M > 0) || !img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     GBN_TRY(run_spread(p, c, cl, weight, p->grid, s));
     GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
@@ -642,7 +642,7 @@ int gbn_type1(gbn_plan *p, const void *c, gbn_layout cl, const float *weight, vo
 
 int gbn_type2(gbn_plan *p, const void *img, gbn_layout il, void *c, gbn_layout cl, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!c || !img) return fail(GBN_ERR_ARG, "null buffer");
+    if ((!c && p->M > 0) || !img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     GBN_CUDA(launch_pad(deapod_args(p, false), (const float2 *)img, il, p->grid, s));
     GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
@@ -668,7 +668,7 @@ int gbn_type21(gbn_plan *p, const void *img, gbn_layout il, void *out, gbn_layou
 int gbn_sense_forward(gbn_plan *p, const void *x, gbn_layout xl, const void *sens, gbn_layout sl, void *kdata,
                       gbn_layout kl, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!x || !sens || !kdata) return fail(GBN_ERR_ARG, "null buffer");
+    if (!x || !sens || (!kdata && p->M > 0)) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     GBN_CUDA(launch_pad_sense(deapod_args(p, false), (const float2 *)x, xl, (const float2 *)sens, sl, p->grid, s));
     GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
@@ -679,7 +679,7 @@ int gbn_sense_forward(gbn_plan *p, const void *x, gbn_layout xl, const void *sen
 int gbn_sense_adjoint(gbn_plan *p, const void *kdata, gbn_layout kl, const float *dcf, const void *sens,
                       gbn_layout sl, void *x, gbn_layout xl, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!x || !sens || !kdata) return fail(GBN_ERR_ARG, "null buffer");
+    if (!x || !sens || (!kdata && p->M > 0)) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     GBN_TRY(run_spread(p, kdata, kl, dcf, p->grid, s));
     GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
@@ -705,7 +705,8 @@ int gbn_sense_normal(gbn_plan *p, const void *x, gbn_layout xl, const void *sens
 int gbn_interp_grad_coords(gbn_plan *p, const void *grid, const void *grad_c, gbn_layout cl, float *grad_xyz,
                            gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!grid || !grad_c || !grad_xyz) return fail(GBN_ERR_ARG, "null buffer");
+    if (!grid || ((!grad_c || !grad_xyz) && p->M > 0)) return fail(GBN_ERR_ARG, "null buffer");
+    if (p->M == 0) return GBN_OK;
     cudaStream_t s = (cudaStream_t)stream;
     GBN_CUDA(cudaMemsetAsync(grad_xyz, 0, sizeof(float) * (size_t)p->M * p->dim, s));
     GradArgs a;
@@ -789,7 +790,7 @@ static gbn_layout host_sample_layout(const gbn_plan *p) { return gbn_layout{0, 1
 
 int gbn_type1_host(gbn_plan *p, const void *h_c, void *h_img, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!h_c || !h_img) return fail(GBN_ERR_ARG, "null buffer");
+    if ((!h_c && p->M > 0) || !h_img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     const size_t cb = sizeof(float2) * (size_t)p->M * p->desc.n_coil, ib = sizeof(float2) * image_elems(p);
     GBN_TRY(ensure(p, p->stage_in, cb));
@@ -804,7 +805,7 @@ int gbn_type1_host(gbn_plan *p, const void *h_c, void *h_img, gbn_stream_t strea
 
 int gbn_type2_host(gbn_plan *p, const void *h_img, void *h_c, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
-    if (!h_c || !h_img) return fail(GBN_ERR_ARG, "null buffer");
+    if ((!h_c && p->M > 0) || !h_img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     const size_t cb = sizeof(float2) * (size_t)p->M * p->desc.n_coil, ib = sizeof(float2) * image_elems(p);
     GBN_TRY(ensure(p, p->stage_in, ib));
