@@ -300,29 +300,44 @@ def _kgrid(shape):
     return np.meshgrid(*[freqs(m) for m in shape], indexing="ij")
 
 
-def nudft_type1(coords, c, shape, df=1.0, iflag=1):
-    """(1/M) sum_j c_j exp(s i k.x_j), s = sign(iflag) (nudft{1,2,3}d1)."""
+_CHUNK_ELEMS = 1 << 23  # complex128 phase entries per chunk (128 MiB)
+
+
+def nudft_type1(coords, c, shape, df=1.0, iflag=1, pixels=None):
+    """(1/M) sum_j c_j exp(s i k.x_j), s = sign(iflag) (nudft{1,2,3}d1).
+    pixels: optional flat indices into the image; then returns (len(pixels), *trail).
+    Memory is bounded by chunking over samples."""
     s = -1.0 if iflag < 0 else 1.0
-    ks = _kgrid(shape)
-    xs = [np.asarray(v, dtype=np.float64) * df for v in coords]
+    ks = [k.reshape(-1) for k in _kgrid(shape)]
+    if pixels is not None:
+        ks = [k[np.asarray(pixels)] for k in ks]
+    xs = [np.asarray(v, dtype=np.float64).reshape(-1) * df for v in coords]
     c2, trail = _split(np.asarray(c), 1)
-    phase = sum(k.reshape(-1, 1) * x.reshape(1, -1) for k, x in zip(ks, xs))   # (K, M)
-    E = np.exp(s * 1j * phase)
-    out = (E @ c2) / len(xs[0])                                               # (K, nt)
-    return out.reshape(tuple(shape) + trail)
+    M, K = len(xs[0]), len(ks[0])
+    out = np.zeros((K, c2.shape[1]), dtype=np.complex128)
+    step = max(1, _CHUNK_ELEMS // max(K, 1))
+    for a in range(0, M, step):
+        phase = sum(k[:, None] * x[None, a:a + step] for k, x in zip(ks, xs))   # (K, m)
+        out += np.exp(s * 1j * phase) @ c2[a:a + step]
+    out /= M
+    return out.reshape((K,) + trail) if pixels is not None else out.reshape(tuple(shape) + trail)
 
 
 def nudft_type2(coords, Fk, shape, df=1.0, iflag=1):
     """sum_k F_k exp(-s i k.x_j): the exact operator that type-2 approximates."""
     s = -1.0 if iflag < 0 else 1.0
     dim = len(shape)
-    ks = _kgrid(shape)
-    xs = [np.asarray(v, dtype=np.float64) * df for v in coords]
+    ks = [k.reshape(-1) for k in _kgrid(shape)]
+    xs = [np.asarray(v, dtype=np.float64).reshape(-1) * df for v in coords]
     F2, trail = _split(np.asarray(Fk), dim)
-    phase = sum(x.reshape(-1, 1) * k.reshape(1, -1) for k, x in zip(ks, xs))   # (M, K)
-    E = np.exp(-s * 1j * phase)
-    out = E @ F2.reshape(-1, F2.shape[-1])
-    return out.reshape((len(xs[0]),) + trail)
+    F2 = F2.reshape(-1, F2.shape[-1])
+    M, K = len(xs[0]), len(ks[0])
+    out = np.empty((M, F2.shape[1]), dtype=np.complex128)
+    step = max(1, _CHUNK_ELEMS // max(K, 1))
+    for a in range(0, M, step):
+        phase = sum(x[a:a + step, None] * k[None, :] for k, x in zip(ks, xs))   # (m, K)
+        out[a:a + step] = np.exp(-s * 1j * phase) @ F2
+    return out.reshape((M,) + trail)
 
 
 def nudft_type2_coord_grad(coords, Fk, shape, grad_c, df=1.0, iflag=1):
@@ -330,15 +345,17 @@ def nudft_type2_coord_grad(coords, Fk, shape, grad_c, df=1.0, iflag=1):
     coils, for the exact type-2 sum.  Returns (M, dim) float64."""
     s = -1.0 if iflag < 0 else 1.0
     dim = len(shape)
-    ks = _kgrid(shape)
-    xs = [np.asarray(v, dtype=np.float64) * df for v in coords]
+    ks = [k.reshape(-1) for k in _kgrid(shape)]
+    xs = [np.asarray(v, dtype=np.float64).reshape(-1) * df for v in coords]
     F2, _ = _split(np.asarray(Fk), dim)
     F2 = F2.reshape(-1, F2.shape[-1])
-    g2 = np.asarray(grad_c).reshape(len(xs[0]), -1)
-    phase = sum(x.reshape(-1, 1) * k.reshape(1, -1) for k, x in zip(ks, xs))
-    E = np.exp(-s * 1j * phase)
-    out = np.empty((len(xs[0]), dim))
-    for d in range(dim):
-        dc = (E * (-s * 1j * ks[d].reshape(1, -1))) @ F2                       # (M, nt)
-        out[:, d] = np.real(np.conj(g2) * dc).sum(axis=1) * df
+    M, K = len(xs[0]), len(ks[0])
+    g2 = np.asarray(grad_c).reshape(M, -1)
+    out = np.empty((M, dim))
+    step = max(1, _CHUNK_ELEMS // max(K, 1))
+    for a in range(0, M, step):
+        E = np.exp(-s * 1j * sum(x[a:a + step, None] * k[None, :] for k, x in zip(ks, xs)))
+        for d in range(dim):
+            dc = (E * (-s * 1j * ks[d][None, :])) @ F2                         # (m, nt)
+            out[a:a + step, d] = np.real(np.conj(g2[a:a + step]) * dc).sum(axis=1) * df
     return out
