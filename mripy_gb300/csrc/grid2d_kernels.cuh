@@ -1,0 +1,269 @@
+// 2-D gridding kernels with warp-level accumulation (the multi-coil hot path).
+//
+// Lane mapping: lane = c + CG*q, coil c in [0, CG), tap slot q in [0, NQ), NQ = 32/CG.
+// Slot q handles the y-taps ky = q, q+NQ, q+2NQ, ... (KT of them), so for one grid row a
+// warp touches NQ*KT consecutive y cells of CG consecutive coils: with the shared-memory
+// layout [x][y][coil] that is one contiguous run of 8-byte words, free of bank conflicts.
+//
+// Interp: one warp per sample.  Lanes 0..W-1 evaluate wx, lanes 16..16+W-1 evaluate wy
+// (one exp2 per lane), shuffles broadcast them, each lane accumulates its KT*W taps for
+// its coil, and a shuffle reduction over the NQ slots yields the coil value.
+//
+// Spread: output-stationary tile [TX][TY][CG] in shared memory; warp w owns tile rows
+// [w*R, (w+1)*R).  A batch of samples is staged (weights, coil values, local offsets),
+// then every warp walks the batch and applies the taps that fall in its own rows.  No
+// two warps ever write the same cell and the lanes of a warp write distinct cells, so the
+// accumulation is plain load-add-store: no atomics, and a fixed summation order.
+#pragma once
+
+#include "common.cuh"
+
+namespace gbn {
+
+template <int WT, int CG>
+struct Lanes2D {
+    static constexpr int NQ = 32 / CG;
+    static constexpr int WMAX = WT ? WT : 16;
+    static constexpr int KT = (WMAX + NQ - 1) / NQ;
+};
+
+__device__ __forceinline__ int wrap_mod(int v, int n) {
+    v %= n;
+    return v < 0 ? v + n : v;
+}
+
+// --------------------------------------------------------------------------------- interp
+template <int WT, int CG>
+__global__ void __launch_bounds__(512) k_interp2d(InterpArgs a) {
+    using L = Lanes2D<WT, CG>;
+    extern __shared__ float4 smem_i2[];
+    float2 *win = reinterpret_cast<float2 *>(smem_i2);  // [WX][WY][CG]
+    const Geom &g = a.g;
+    const int4 sub = a.subs[blockIdx.x];
+    const int cg0 = blockIdx.y * CG;
+    const int grp = sub.x / g.ntiles;
+    const int tile = sub.x % g.ntiles;
+    const int o0 = (tile / g.ntile[1]) * g.tile[0];
+    const int o1 = (tile % g.ntile[1]) * g.tile[1];
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+    const int WX = g.tile[0] + W - 1, WY = g.tile[1] + W - 1;
+    const int nf0 = g.nf[0], nf1 = g.nf[1];
+
+    // stage the window (periodic wrap), all CG coils of a cell contiguous
+    {
+        const int ws0 = o0 - (ns - 1), ws1 = o1 - (ns - 1);
+        const float2 *base = a.grid + ((int64_t)grp * g.n_coil + cg0) * g.G;
+        const int ncell = WX * WY;
+        for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+            const int wx = i / WY, wy = i - wx * WY;
+            const int gx = wrap_mod(ws0 + wx, nf0), gy = wrap_mod(ws1 + wy, nf1);
+            const float2 *src = base + (int64_t)gx * nf1 + gy;
+            float2 *dst = win + (size_t)i * CG;
+#pragma unroll
+            for (int c = 0; c < CG; ++c)
+                dst[c] = (cg0 + c < g.n_coil) ? src[(int64_t)c * g.G] : make_float2(0.f, 0.f);
+        }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const int kk = lane & 15;
+    const float beta = lane < 16 ? g.beta2[0] : g.beta2[1];
+    for (int s = warp; s < sub.z; s += nw) {
+        const int64_t li = (int64_t)sub.y + s;
+        const float4 p = a.pts[li];
+        const uint32_t j = a.idx[li];
+        int c0x, c0y, c0z;
+        unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
+        int ccx = c0x + ns - 1, ccy = c0y + ns - 1;
+        ccx -= ccx >= nf0 ? nf0 : 0;
+        ccy -= ccy >= nf1 ? nf1 : 0;
+        const int rel0 = ccx - o0, rel1 = ccy - o1;
+        float myw = 0.f;
+        if (kk < W) {
+            const float d = (lane < 16 ? p.x : p.y) + (float)(ns - 1 - kk);
+            myw = exp2f(-beta * d * d);
+        }
+        float wy[L::KT];
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) {
+            const int ky = q + t * L::NQ;
+            const float v = __shfl_sync(0xffffffffu, myw, 16 + (ky < 16 ? ky : 15));
+            wy[t] = ky < W ? v : 0.f;
+        }
+        float ax = 0.f, ay = 0.f;
+        const float2 *rowbase = win + ((size_t)rel0 * WY + rel1) * CG + c;
+#pragma unroll
+        for (int kx = 0; kx < L::WMAX; ++kx) {
+            if (WT == 0 && kx >= W) break;
+            const float wx = __shfl_sync(0xffffffffu, myw, kx);
+            const float2 *row = rowbase + (size_t)kx * WY * CG;
+#pragma unroll
+            for (int t = 0; t < L::KT; ++t) {
+                const int ky = q + t * L::NQ;
+                if (ky < W) {
+                    const float2 v = row[ky * CG];
+                    const float w = wx * wy[t];
+                    ax = fmaf(w, v.x, ax);
+                    ay = fmaf(w, v.y, ay);
+                }
+            }
+        }
+#pragma unroll
+        for (int off = CG; off < 32; off <<= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, off);
+            ay += __shfl_xor_sync(0xffffffffu, ay, off);
+        }
+        if (q == 0 && cg0 + c < g.n_coil) {
+            const float sc = a.weight ? a.weight[j] : 1.f;
+            a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + c) * a.c_coil] = make_float2(ax * sc, ay * sc);
+        }
+    }
+}
+
+// --------------------------------------------------------------------------------- spread
+constexpr int kSpreadBatch = 64;  // samples staged per batch
+
+template <int WT, int CG>
+__global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
+    using L = Lanes2D<WT, CG>;
+    extern __shared__ float4 smem_s2[];
+    const Geom &g = a.g;
+    const int TX = g.tile[0], TY = g.tile[1];
+    float2 *acc = reinterpret_cast<float2 *>(smem_s2);              // [TX][TY][CG]
+    float *st_w = reinterpret_cast<float *>(acc + (size_t)TX * TY * CG);  // [batch][32]: wx[16], wy[16]
+    float2 *st_v = reinterpret_cast<float2 *>(st_w + kSpreadBatch * 32);  // [batch][CG]
+    int2 *st_r = reinterpret_cast<int2 *>(st_v + kSpreadBatch * CG);      // [batch]: local first-tap cell
+
+    const int4 sub = a.subs[blockIdx.x];
+    const int cg0 = blockIdx.y * CG;
+    const int grp = sub.x / g.ntiles;
+    const int tile = sub.x % g.ntiles;
+    const int o0 = (tile / g.ntile[1]) * TX;
+    const int o1 = (tile % g.ntile[1]) * TY;
+    const int nf0 = g.nf[0], nf1 = g.nf[1];
+    const int e0 = min(TX, nf0 - o0), e1 = min(TY, nf1 - o1);
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+
+    for (int i = threadIdx.x; i < TX * TY * CG; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const int R = (TX + nw - 1) / nw;
+    const int row0 = warp * R, row1 = min(row0 + R, e0);
+
+    for (int base = 0; base < sub.z; base += kSpreadBatch) {
+        const int n = min(kSpreadBatch, sub.z - base);
+        __syncthreads();  // previous batch consumed (and the zeroing above done)
+        for (int i = threadIdx.x; i < n * 32; i += blockDim.x) {
+            const int s = i >> 5, k = i & 31, kq = k & 15;
+            const float4 p = a.pts[(int64_t)sub.y + base + s];
+            float val = 0.f;
+            if (kq < W) {
+                const float d = (k < 16 ? p.x : p.y) + (float)(ns - 1 - kq);
+                val = exp2f(-(k < 16 ? g.beta2[0] : g.beta2[1]) * d * d);
+            }
+            st_w[i] = val;
+            if (k == 0) {
+                int c0x, c0y, c0z;
+                unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
+                int rx = c0x - o0, ry = c0y - o1;
+                rx += rx < 0 ? nf0 : 0;
+                ry += ry < 0 ? nf1 : 0;
+                st_r[s] = make_int2(rx, ry);
+            }
+        }
+        for (int i = threadIdx.x; i < n * CG; i += blockDim.x) {
+            const int s = i / CG, cc = i - s * CG;
+            const int64_t li = (int64_t)sub.y + base + s;
+            const uint32_t j = a.idx[li];
+            float2 v = make_float2(0.f, 0.f);
+            if (cg0 + cc < g.n_coil) {
+                v = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
+                if (a.weight) {
+                    const float sw = a.weight[j];
+                    v.x *= sw;
+                    v.y *= sw;
+                }
+            }
+            st_v[i] = v;
+        }
+        __syncthreads();
+
+        for (int s = 0; s < n; ++s) {
+            const int2 r = st_r[s];
+            // rows of this warp that the stencil reaches (tap kx = row - rx mod nf0 < W)
+            bool any = false;
+            for (int row = row0; row < row1; ++row) {
+                int kx = row - r.x;
+                kx += kx < 0 ? nf0 : 0;
+                any |= kx < W;
+            }
+            if (!any) continue;
+            const float2 v = st_v[s * CG + c];
+            const float *w = st_w + s * 32;
+            float wy[L::KT];
+            int ly[L::KT];
+#pragma unroll
+            for (int t = 0; t < L::KT; ++t) {
+                const int ky = q + t * L::NQ;
+                int y = r.y + ky;
+                y -= y >= nf1 ? nf1 : 0;
+                const bool ok = ky < W && y < e1;
+                wy[t] = ok ? w[16 + ky] : 0.f;
+                ly[t] = ok ? y : -1;
+            }
+            for (int row = row0; row < row1; ++row) {
+                int kx = row - r.x;
+                kx += kx < 0 ? nf0 : 0;
+                if (kx >= W) continue;
+                const float wx = w[kx];
+                float2 *dst = acc + (size_t)row * TY * CG + c;
+#pragma unroll
+                for (int t = 0; t < L::KT; ++t) {
+                    if (ly[t] >= 0) {
+                        float2 *cell = dst + (size_t)ly[t] * CG;
+                        const float ww = wx * wy[t];
+                        float2 o = *cell;
+                        o.x = fmaf(ww, v.x, o.x);
+                        o.y = fmaf(ww, v.y, o.y);
+                        *cell = o;
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // flush: consecutive threads take consecutive coils of a cell (shared reads contiguous,
+    // each coil plane receives 32-byte runs)
+    const bool split = (sub.w & kSplitFlag) != 0;
+    const int ecell = e0 * e1;
+    for (int i = threadIdx.x; i < ecell * CG; i += blockDim.x) {
+        const int cc = i % CG, cell = i / CG;
+        if (cg0 + cc >= g.n_coil) continue;
+        const int lx = cell / e1, ly = cell - lx * e1;
+        const float2 val = acc[((size_t)lx * TY + ly) * CG + cc];
+        float2 *dst = a.grid + ((int64_t)grp * g.n_coil + cg0 + cc) * g.G + (int64_t)(o0 + lx) * nf1 + (o1 + ly);
+        if (split) {
+            atomicAdd(&dst->x, val.x);
+            atomicAdd(&dst->y, val.y);
+        } else {
+            *dst = val;
+        }
+    }
+}
+
+inline size_t spread2d_smem_bytes(const Geom &g, int cg) {
+    return (size_t)g.tile[0] * g.tile[1] * cg * sizeof(float2) + kSpreadBatch * 32 * sizeof(float) +
+           (size_t)kSpreadBatch * cg * sizeof(float2) + kSpreadBatch * sizeof(int2);
+}
+
+inline size_t interp2d_smem_bytes(const Geom &g, int cg) {
+    return (size_t)(g.tile[0] + g.W - 1) * (g.tile[1] + g.W - 1) * cg * sizeof(float2);
+}
+
+}  // namespace gbn

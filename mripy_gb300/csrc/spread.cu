@@ -1,9 +1,16 @@
 // Spread (type-1 gridding) launchers.
+//
+// 2-D with at most 16 taps per dimension: k_spread2d (warp-owned rows, no atomics).
+// Otherwise (1-D, 3-D, wide stencils): k_spread (shared-memory atomics).
 #include "dispatch.cuh"
+#include "grid2d_kernels.cuh"
 
 namespace gbn {
 
+static bool use_2d_path(const Geom &g) { return g.dim == 2 && g.W <= 16; }
+
 size_t spread_smem_bytes(const Geom &g, int coil_group) {
+    if (use_2d_path(g)) return spread2d_smem_bytes(g, coil_group);
     size_t cells = 1;
     for (int d = 0; d < g.dim; ++d) cells *= (size_t)g.tile[d];
     return cells * (size_t)coil_group * sizeof(float2);
@@ -20,6 +27,17 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
     const size_t smem = spread_smem_bytes(a.g, coil_group);
     const dim3 grid((unsigned)n_sub, (unsigned)((a.g.n_coil + coil_group - 1) / coil_group));
     cudaError_t err = cudaSuccess;
+    if (use_2d_path(a.g)) {
+        GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
+            auto kern = k_spread2d<WT, CG>;
+            err = set_smem(kern, smem);
+            if (err == cudaSuccess) {
+                kern<<<grid, threads, smem, s>>>(a);
+                err = cudaGetLastError();
+            }
+        }));
+        return err;
+    }
     GBN_DISPATCH_D(a.g.dim, GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
         auto kern = k_spread<D, WT, CG>;
         err = set_smem(kern, smem);
