@@ -72,9 +72,10 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 20 ms; only samples whose
+    nvidia-smi timestamp falls inside the marked timed window are summarised."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -82,14 +83,16 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            time.sleep(0.5)  # let the sampler come up before the timed window opens
         except Exception:
             self.proc = None
 
@@ -97,31 +100,49 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def mark_start(self):
+        import datetime
+        self.t0 = datetime.datetime.now()
+
+    def mark_end(self):
+        import datetime
+        self.t1 = datetime.datetime.now()
+
     def stop(self):
+        import datetime
         if self.proc is None:
             return None
+        time.sleep(0.1)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], 0.0, set()
+        sm, smax, reasons, all_sm = [], 0.0, set(), []
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        pad = datetime.timedelta(milliseconds=25)
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax = max(smax, float(parts[2]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                mhz = float(parts[2])
+                smax = max(smax, float(parts[3]))
             except ValueError:
                 continue
-            for n, v in zip(names, parts[5:9]):
+            all_sm.append(mhz)
+            if self.t0 is not None and not (self.t0 - pad <= ts <= self.t1 + pad):
+                continue
+            sm.append(mhz)
+            for n, v in zip(names, parts[6:10]):
                 if v.lower() == "active":
                     reasons.add(n)
         if not sm:
-            return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+            return {"sm_mhz": None, "sm_max_mhz": smax or None, "reasons": [],
+                    "samples": 0, "note": "timed window shorter than the 20 ms sampling period"}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
 
 
 # ------------------------------------------------------------------------------ workload
@@ -148,17 +169,18 @@ def flops(M, n_coil, W, dim):
 
 
 def event_time(torch, fn, reps, stream, flush=None):
-    ts = []
-    for _ in range(reps):
+    """CUDA-event time of each call of fn on ``stream``; the L2 flush between calls is
+    outside the event pairs.  One host synchronisation at the end."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    for i in range(reps):
         if flush is not None:
             flush()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
+        starts[i].record(stream)
         fn()
-        b.record(stream)
-        b.synchronize()
-        ts.append(a.elapsed_time(b))
+        ends[i].record(stream)
+    ends[-1].synchronize()
+    ts = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     return float(np.median(ts)), ts
 
 
@@ -216,10 +238,14 @@ def run_gpu(args):
     if sampler:
         sampler.start()
     torch.cuda.synchronize()
+    if sampler:
+        sampler.mark_start()
     t_wall = time.perf_counter()
     step_ms_med, step_ms = event_time(torch, g.replay, args.steps, stream, flush)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
+    if sampler:
+        sampler.mark_end()
     clocks = sampler.stop() if sampler else None
     mean_ms = max_over_ranks(float(np.mean(step_ms)))
     value = replica_units(M * n_coil, world) / (mean_ms * 1e-3) / 1e6
@@ -285,7 +311,7 @@ def run_gpu(args):
 
     for _ in range(3):
         plain_step()
-    t_plain, _ = event_time(torch, plain_step, max(5, args.steps // 2), stream, flush)
+    t_plain, _ = event_time(torch, plain_step, min(100, max(5, args.steps // 2)), stream, flush)
     result["plain"] = {"value": round(M * n_coil / (t_plain * 1e-3) / 1e6, 2), "unit": UNIT,
                        "ms_per_step": round(t_plain, 4), "speedup_batched_vs_plain": round(t_plain / mean_ms, 2)}
 
@@ -321,7 +347,7 @@ def run_gpu(args):
     for _ in range(3):
         e2e_step()
     ts = []
-    for _ in range(max(5, args.steps)):
+    for _ in range(min(50, max(5, args.steps))):
         flush()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -399,8 +425,8 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup

@@ -71,10 +71,20 @@ __global__ void __launch_bounds__(512) k_interp2d(InterpArgs a) {
     const int c = lane % CG, q = lane / CG;
     const int kk = lane & 15;
     const float beta = lane < 16 ? g.beta2[0] : g.beta2[1];
+    // software pipeline: the next sample's record is in flight while this one is gathered
+    float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t j_next = 0;
+    if (warp < sub.z) {
+        p_next = a.pts[(int64_t)sub.y + warp];
+        j_next = a.idx[(int64_t)sub.y + warp];
+    }
     for (int s = warp; s < sub.z; s += nw) {
-        const int64_t li = (int64_t)sub.y + s;
-        const float4 p = a.pts[li];
-        const uint32_t j = a.idx[li];
+        const float4 p = p_next;
+        const uint32_t j = j_next;
+        if (s + nw < sub.z) {
+            p_next = a.pts[(int64_t)sub.y + s + nw];
+            j_next = a.idx[(int64_t)sub.y + s + nw];
+        }
         int c0x, c0y, c0z;
         unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
         int ccx = c0x + ns - 1, ccy = c0y + ns - 1;
@@ -168,11 +178,16 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
             }
             st_w[i] = val;
             if (k == 0) {
+                // signed local position of the first tap: in (-W, nf - W].  The stencil
+                // [r, r + W) never wraps onto the tile twice because nf >= tile + W on this
+                // path (the generic kernel serves smaller grids).
                 int c0x, c0y, c0z;
                 unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
                 int rx = c0x - o0, ry = c0y - o1;
                 rx += rx < 0 ? nf0 : 0;
                 ry += ry < 0 ? nf1 : 0;
+                rx -= rx > nf0 - W ? nf0 : 0;
+                ry -= ry > nf1 - W ? nf1 : 0;
                 st_r[s] = make_int2(rx, ry);
             }
         }
@@ -195,14 +210,9 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
 
         for (int s = 0; s < n; ++s) {
             const int2 r = st_r[s];
-            // rows of this warp that the stencil reaches (tap kx = row - rx mod nf0 < W)
-            bool any = false;
-            for (int row = row0; row < row1; ++row) {
-                int kx = row - r.x;
-                kx += kx < 0 ? nf0 : 0;
-                any |= kx < W;
-            }
-            if (!any) continue;
+            // rows of this warp that the stencil [r.x, r.x + W) reaches
+            const int lo = max(row0, r.x), hi = min(row1, r.x + W);
+            if (lo >= hi) continue;
             const float2 v = st_v[s * CG + c];
             const float *w = st_w + s * 32;
             float wy[L::KT];
@@ -210,18 +220,16 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
 #pragma unroll
             for (int t = 0; t < L::KT; ++t) {
                 const int ky = q + t * L::NQ;
-                int y = r.y + ky;
-                y -= y >= nf1 ? nf1 : 0;
-                const bool ok = ky < W && y < e1;
+                const int y = r.y + ky;
+                const bool ok = ky < W && (unsigned)y < (unsigned)e1;
                 wy[t] = ok ? w[16 + ky] : 0.f;
                 ly[t] = ok ? y : -1;
             }
-            for (int row = row0; row < row1; ++row) {
-                int kx = row - r.x;
-                kx += kx < 0 ? nf0 : 0;
-                if (kx >= W) continue;
-                const float wx = w[kx];
-                float2 *dst = acc + (size_t)row * TY * CG + c;
+            const float *wx_row = w - r.x;
+            float2 *dst = acc + (size_t)lo * TY * CG + c;
+#pragma unroll 4
+            for (int row = lo; row < hi; ++row, dst += TY * CG) {
+                const float wx = wx_row[row];
 #pragma unroll
                 for (int t = 0; t < L::KT; ++t) {
                     if (ly[t] >= 0) {

@@ -7,7 +7,10 @@
 
 namespace gbn {
 
-static bool use_2d_path(const Geom &g) { return g.dim == 2 && g.W <= 16; }
+// the warp-row kernel uses signed tile-local coordinates, exact when nf >= tile + W
+static bool use_2d_path(const Geom &g) {
+    return g.dim == 2 && g.W <= 16 && g.nf[0] >= g.tile[0] + g.W && g.nf[1] >= g.tile[1] + g.W;
+}
 
 size_t spread_smem_bytes(const Geom &g, int coil_group) {
     if (use_2d_path(g)) return spread2d_smem_bytes(g, coil_group);
