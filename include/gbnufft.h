@@ -68,7 +68,8 @@ typedef struct {
     int32_t interp_tile[3]; /* home bin of the interp kernel, cells per dim */
     int32_t max_subproblem; /* samples per thread block before a bin is split */
     int32_t coil_group;     /* coils per thread block: 1, 2, 4 or 8 */
-    int32_t threads;        /* threads per block for spread/interp: 128, 256 or 512 */
+    int32_t threads;        /* threads per spread block: 128, 256 or 512 */
+    int32_t interp_threads; /* threads per interp block: 128, 256 or 512 */
 } gbn_plan_desc;
 
 typedef struct {
@@ -85,6 +86,8 @@ typedef struct {
     int32_t interp_tile[3];
     int32_t coil_group;
     int32_t threads;
+    int32_t interp_threads;
+    int32_t max_subproblem;
     int64_t device_bytes;   /* device memory held by the plan */
 } gbn_plan_info;
 

@@ -71,7 +71,7 @@ struct gbn_plan {
     int nf[3] = {1, 1, 1};
     double tau = 0;
     Geom gs{}, gi{};
-    int coil_group = 1, threads = 256, max_sub = 1024;
+    int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256;
     int64_t G = 1, n_inst = 1;
     size_t device_bytes = 0;
     int smem_optin = 0;
@@ -242,7 +242,7 @@ int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const flo
     const int cg = interp_cg(p);
     if (interp_smem_bytes(p->gi, cg) > (size_t)p->smem_optin)
         return fail(GBN_ERR_CAPACITY, "interp window does not fit in shared memory");
-    GBN_CUDA(launch_interp(a, p->n_interp_sub, cg, p->threads, s));
+    GBN_CUDA(launch_interp(a, p->n_interp_sub, cg, p->interp_threads, s));
     return GBN_OK;
 }
 
@@ -434,8 +434,10 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     if (p->dim == 1) {
         dspread[0] = 1024; dinterp[0] = 1024;
     } else if (p->dim == 2) {
-        dspread[0] = 32; dspread[1] = 32;
-        dinterp[0] = 32; dinterp[1] = 32;
+        // measured on GB300 for the 8-coil 512^2 radial workload: 16x32 output tiles keep
+        // four spread blocks resident per SM; 16x16 interp bins keep the staged window small
+        dspread[0] = 16; dspread[1] = 32;
+        dinterp[0] = 16; dinterp[1] = 16;
     } else {
         dspread[0] = 16; dspread[1] = 16; dspread[2] = 16;
         dinterp[0] = 8; dinterp[1] = 8; dinterp[2] = 8;
@@ -451,11 +453,14 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         return fail(GBN_ERR_ARG, "coil_group must be 1, 2, 4 or 8");
     }
     p->threads = desc->threads > 0 ? desc->threads : 256;
-    if (p->threads != 128 && p->threads != 256 && p->threads != 512) {
-        delete p;
-        return fail(GBN_ERR_ARG, "threads must be 128, 256 or 512");
+    p->interp_threads = desc->interp_threads > 0 ? desc->interp_threads : (p->dim == 2 ? 512 : 256);
+    for (int t : {p->threads, p->interp_threads}) {
+        if (t != 128 && t != 256 && t != 512) {
+            delete p;
+            return fail(GBN_ERR_ARG, "threads must be 128, 256 or 512");
+        }
     }
-    p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem : (p->dim == 3 ? 256 : 1024);
+    p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem : 256;
     make_geom(p, ts, p->gs);
     make_geom(p, ti, p->gi);
 
@@ -582,6 +587,8 @@ int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     o->spread_entries = p->n_dup;
     o->coil_group = p->coil_group;
     o->threads = p->threads;
+    o->interp_threads = p->interp_threads;
+    o->max_subproblem = p->max_sub;
     o->device_bytes = (int64_t)p->device_bytes;
     return GBN_OK;
 }
