@@ -191,6 +191,24 @@ int gbn_graph_capture_normal(gbn_plan *plan, const void *x, gbn_layout x_layout,
 int gbn_graph_launch(gbn_graph *graph, gbn_stream_t stream);
 int gbn_graph_destroy(gbn_graph *graph);
 
+/* ---- allocation-free spread ------------------------------------------------------------ */
+/* No counterpart in the reference.  The 2-D spread of gbn_spread (samples -> oversampled
+ * grid, (n_coil, nf1, nf2) complex64, nf from eps as gbn_grid_params) for callers that
+ * cannot allocate device memory: code inside a framework that owns the GPU memory pool,
+ * real-time loops that must not block in cudaMalloc, plugin hosts that pass only pre-sized
+ * buffers.  The caller passes device inputs and the output grid; the binning scratch is a
+ * fixed file-scope device array (about 8.7 MiB, held by every GPU that loads the library),
+ * so nothing is allocated.  Limits: M <= GBN_NOALLOC_MAX_SAMPLES, nspread <= 8, ms % 8 == 0,
+ * mt % 16 == 0, grid of at most GBN_NOALLOC_MAX_TILES 16x32 tiles (else GBN_ERR_CAPACITY).
+ * All calls share the array: calls that overlap on the GPU race, so order them on one
+ * stream.  The first call on a device resolves the array's address; make it before any
+ * stream capture. */
+#define GBN_NOALLOC_MAX_SAMPLES 262144
+#define GBN_NOALLOC_MAX_TILES 16384
+int gbn_spread2d_noalloc(int coord_dtype, const void *x, const void *y, int64_t M, const void *c,
+                         gbn_layout c_layout, int32_t n_coil, int32_t ms, int32_t mt, double eps, double df,
+                         void *grid, gbn_stream_t stream);
+
 /* ---- host-buffer entry points (the reference's numpy-in / numpy-out calls) ---- */
 /* One call = H2D of the inputs, the transform, D2H of the result, on the plan's
  * staging buffers (pinned host memory recommended for the caller's arrays).

@@ -25,6 +25,7 @@ EXPORTED = (
     "gbn_sense_forward", "gbn_sense_adjoint", "gbn_sense_normal",
     "gbn_interp_grad_coords",
     "gbn_graph_capture_normal", "gbn_graph_launch", "gbn_graph_destroy",
+    "gbn_spread2d_noalloc",
     "gbn_type1_host", "gbn_type2_host", "gbn_type21_host",
     "gbn_nufft2d1_gaussker", "gbn_nufft2d2_gaussker", "gbn_nufft2d21_gaussker",
     "gbn_nufft3d1_gaussker", "gbn_nufft3d2_gaussker", "gbn_nufft3d21_gaussker",
@@ -100,6 +101,7 @@ def _declare(lib):
         "gbn_graph_capture_normal": ([_vp, _vp, Layout, _vp, Layout, _vp, _vp, Layout, P(_vp)], _i32),
         "gbn_graph_launch": ([_vp, _vp], _i32),
         "gbn_graph_destroy": ([_vp], _i32),
+        "gbn_spread2d_noalloc": ([_i32, _vp, _vp, _i64, _vp, Layout, _i32, _i32, _i32, _f64, _f64, _vp, _vp], _i32),
         "gbn_type1_host": ([_vp, _vp, _vp, _vp], _i32),
         "gbn_type2_host": ([_vp, _vp, _vp, _vp], _i32),
         "gbn_type21_host": ([_vp, _vp, _vp, _vp, _vp], _i32),

@@ -34,6 +34,13 @@ int fail(int code, const std::string &msg) {
     return code;
 }
 
+}  // namespace
+
+// lets other translation units report through gbn_last_error
+int gbn::record_error(int code, const char *msg) { return fail(code, msg); }
+
+namespace {
+
 #define GBN_CUDA(call)                                                                          \
     do {                                                                                        \
         cudaError_t e_ = (call);                                                                \

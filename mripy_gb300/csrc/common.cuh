@@ -76,6 +76,9 @@ __device__ __forceinline__ int wrap_pos(int v, int n) {  // v in (-n, 2n)
 // ---- internal launchers (defined in the .cu files) -------------------------------------
 struct SortBuffers;
 
+// api.cu: sets the calling thread's gbn_last_error message and returns code
+int record_error(int code, const char *msg);
+
 // prep.cu
 cudaError_t launch_prep(int coord_dtype, const void *x, const void *y, const void *z, int64_t M,
                         const int64_t *d_traj_off, const Geom &gs, const Geom &gi, double df,
