@@ -206,6 +206,12 @@ int fft_exec(gbn_plan *p, float2 *grid, int direction, cudaStream_t s) {
     return GBN_OK;
 }
 
+// shared memory a block may take when choosing coils per block: in 3-D two blocks per SM
+// (latency hiding) beat more coils per block
+size_t smem_budget(const gbn_plan *p) {
+    return p->dim == 3 ? std::min<size_t>((size_t)p->smem_optin, 116 * 1024) : (size_t)p->smem_optin;
+}
+
 int dir_type1(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_FORWARD : GBN_FFT_INVERSE; }
 int dir_type2(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_INVERSE : GBN_FFT_FORWARD; }
 
@@ -222,7 +228,7 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
     a.weight = weight;
     a.grid = grid;
     int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
-    while (cg > 1 && spread_smem_bytes(p->gs, cg) > (size_t)p->smem_optin) cg /= 2;
+    while (cg > 1 && spread_smem_bytes(p->gs, cg) > smem_budget(p)) cg /= 2;
     if (spread_smem_bytes(p->gs, cg) > (size_t)p->smem_optin)
         return fail(GBN_ERR_CAPACITY, "spread tile does not fit in shared memory");
     GBN_CUDA(launch_spread(a, p->n_spread_sub, cg, p->threads, s));
@@ -231,7 +237,7 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
 
 int interp_cg(const gbn_plan *p) {
     int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
-    while (cg > 1 && interp_smem_bytes(p->gi, cg) > (size_t)p->smem_optin) cg /= 2;
+    while (cg > 1 && interp_smem_bytes(p->gi, cg) > smem_budget(p)) cg /= 2;
     return cg;
 }
 
@@ -446,7 +452,8 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         dspread[0] = 16; dspread[1] = 32;
         dinterp[0] = 16; dinterp[1] = 16;
     } else {
-        dspread[0] = 16; dspread[1] = 16; dspread[2] = 16;
+        // warp lanes run along z: 32-cell z rows for the spread tile, 8^3 interp bins
+        dspread[0] = 8; dspread[1] = 8; dspread[2] = 32;
         dinterp[0] = 8; dinterp[1] = 8; dinterp[2] = 8;
     }
     int ts[3] = {1, 1, 1}, ti[3] = {1, 1, 1};

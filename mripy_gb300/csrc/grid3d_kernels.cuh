@@ -1,0 +1,273 @@
+// 3-D gridding kernels with warp-level accumulation (the same design as the 2-D kernels,
+// with z as the lane direction).
+//
+// Lane mapping: lane = c + CG*q, coil c in [0, CG), z-tap slot q in [0, NQ); slot q handles
+// kz = q, q+NQ, ... (KT taps).  Shared-memory layout [x][y][z][coil]: for one (x, y) row a
+// warp touches NQ*KT consecutive z cells of CG consecutive coils, one contiguous run.
+//
+// Interp: one warp per sample over the staged window of its home bin (tile + W - 1 cells per
+// dimension, periodic wrap).  Lanes 0..15 evaluate wx, lanes 16..31 wy (one exp2 each), every
+// lane evaluates the wz of its own taps; each lane then sums its W*W*KT taps for its coil
+// and a shuffle reduction over the slots yields the coil value.
+//
+// Spread: output-stationary tile [TX][TY][TZ][CG]; warp w owns the x-planes
+// [w*P, (w+1)*P).  Samples are staged in batches (weights, weighted coil values, signed local
+// first-tap cells); every warp walks the batch and applies the taps in its own planes with
+// plain load-add-store (no atomics, fixed order).  Signed local coordinates are exact when
+// nf >= tile + W in every dimension; smaller grids use the generic kernels.
+#pragma once
+
+#include "grid2d_kernels.cuh"
+#include "grid_kernels.cuh"
+
+namespace gbn {
+
+inline bool grid3d_applies(const Geom &g) {
+    return g.dim == 3 && g.W <= 16 && g.nf[0] >= g.tile[0] + g.W && g.nf[1] >= g.tile[1] + g.W &&
+           g.nf[2] >= g.tile[2] + g.W;
+}
+
+// --------------------------------------------------------------------------------- interp
+template <int WT, int CG>
+__global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
+    using L = Lanes2D<WT, CG>;
+    extern __shared__ float4 smem_i3[];
+    float2 *win = reinterpret_cast<float2 *>(smem_i3);  // [WX][WY][WZ][CG]
+    const Geom &g = a.g;
+    const int4 sub = a.subs[blockIdx.x];
+    const int cg0 = blockIdx.y * CG;
+    const int grp = sub.x / g.ntiles;
+    int o[3], e[3];
+    tile_coords<3>(g, sub.x % g.ntiles, o, e);
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+    const int WX = g.tile[0] + W - 1, WY = g.tile[1] + W - 1, WZ = g.tile[2] + W - 1;
+    const int nf0 = g.nf[0], nf1 = g.nf[1], nf2 = g.nf[2];
+
+    {
+        const int ws0 = o[0] - (ns - 1), ws1 = o[1] - (ns - 1), ws2 = o[2] - (ns - 1);
+        const float2 *base = a.grid + ((int64_t)grp * g.n_coil + cg0) * g.G;
+        const int ncell = WX * WY * WZ;
+        for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+            const int wz = i % WZ, wy = (i / WZ) % WY, wx = i / (WZ * WY);
+            const int gx = wrap_mod(ws0 + wx, nf0), gy = wrap_mod(ws1 + wy, nf1), gz = wrap_mod(ws2 + wz, nf2);
+            const float2 *src = base + ((int64_t)gx * nf1 + gy) * nf2 + gz;
+            float2 *dst = win + (size_t)i * CG;
+#pragma unroll
+            for (int c = 0; c < CG; ++c)
+                dst[c] = (cg0 + c < g.n_coil) ? src[(int64_t)c * g.G] : make_float2(0.f, 0.f);
+        }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const int kk = lane & 15;
+    const float beta = lane < 16 ? g.beta2[0] : g.beta2[1];
+    float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t j_next = 0;
+    if (warp < sub.z) {
+        p_next = a.pts[(int64_t)sub.y + warp];
+        j_next = a.idx[(int64_t)sub.y + warp];
+    }
+    for (int s = warp; s < sub.z; s += nw) {
+        const float4 p = p_next;
+        const uint32_t j = j_next;
+        if (s + nw < sub.z) {
+            p_next = a.pts[(int64_t)sub.y + s + nw];
+            j_next = a.idx[(int64_t)sub.y + s + nw];
+        }
+        int c0[3];
+        unpack_cells(3, __float_as_uint(p.w), c0[0], c0[1], c0[2]);
+        int rel[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            int cc = c0[d] + ns - 1;
+            cc -= cc >= g.nf[d] ? g.nf[d] : 0;
+            rel[d] = cc - o[d];
+        }
+        float myw = 0.f;
+        if (kk < W) {
+            const float d = (lane < 16 ? p.x : p.y) + (float)(ns - 1 - kk);
+            myw = exp2f(-beta * d * d);
+        }
+        float wy[L::WMAX];
+#pragma unroll
+        for (int k = 0; k < L::WMAX; ++k) wy[k] = __shfl_sync(0xffffffffu, myw, 16 + k);
+        float wz[L::KT];
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) {
+            const int kz = q + t * L::NQ;
+            const float d = p.z + (float)(ns - 1 - kz);
+            wz[t] = kz < W ? exp2f(-g.beta2[2] * d * d) : 0.f;
+        }
+        float2 acc = make_float2(0.f, 0.f);
+        const float2 *base = win + (((size_t)rel[0] * WY + rel[1]) * WZ + rel[2]) * CG + c;
+#pragma unroll 1
+        for (int kx = 0; kx < W; ++kx) {
+            const float wx = __shfl_sync(0xffffffffu, myw, kx);
+            const float2 *plane = base + (size_t)kx * WY * WZ * CG;
+#pragma unroll
+            for (int ky = 0; ky < L::WMAX; ++ky) {
+                if (WT == 0 && ky >= W) break;
+                const float wxy = wx * wy[ky];
+                const float2 *row = plane + (size_t)ky * WZ * CG;
+#pragma unroll
+                for (int t = 0; t < L::KT; ++t) {
+                    const int kz = q + t * L::NQ;
+                    if (kz < W) {
+                        const float w = wxy * wz[t];
+                        acc = __ffma2_rn(make_float2(w, w), row[kz * CG], acc);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int off = CG; off < 32; off <<= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
+        }
+        if (q == 0 && cg0 + c < g.n_coil) {
+            const float sc = a.weight ? a.weight[j] : 1.f;
+            a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + c) * a.c_coil] = make_float2(acc.x * sc, acc.y * sc);
+        }
+    }
+}
+
+// --------------------------------------------------------------------------------- spread
+constexpr int kSpread3dBatch = 32;
+
+template <int WT, int CG>
+__global__ void __launch_bounds__(256) k_spread3d(SpreadArgs a) {
+    using L = Lanes2D<WT, CG>;
+    extern __shared__ float4 smem_s3[];
+    const Geom &g = a.g;
+    const int TX = g.tile[0], TY = g.tile[1], TZ = g.tile[2];
+    float2 *acc = reinterpret_cast<float2 *>(smem_s3);                        // [TX][TY][TZ][CG]
+    float *st_w = reinterpret_cast<float *>(acc + (size_t)TX * TY * TZ * CG);  // [batch][48]: wx, wy, wz
+    float2 *st_v = reinterpret_cast<float2 *>(st_w + kSpread3dBatch * 48);     // [batch][CG]
+    int4 *st_r = reinterpret_cast<int4 *>(st_v + kSpread3dBatch * CG);         // [batch]: signed first taps
+
+    const int4 sub = a.subs[blockIdx.x];
+    const int cg0 = blockIdx.y * CG;
+    const int grp = sub.x / g.ntiles;
+    int o[3], e[3];
+    tile_coords<3>(g, sub.x % g.ntiles, o, e);
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+
+    for (int i = threadIdx.x; i < TX * TY * TZ * CG; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const int P = (TX + nw - 1) / nw;
+    const int x0 = warp * P, x1 = min(x0 + P, e[0]);
+
+    for (int base = 0; base < sub.z; base += kSpread3dBatch) {
+        const int n = min(kSpread3dBatch, sub.z - base);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n * 48; i += blockDim.x) {
+            const int s = i / 48, k = i - s * 48, d = k >> 4, kq = k & 15;
+            const float4 p = a.pts[(int64_t)sub.y + base + s];
+            float val = 0.f;
+            if (kq < W) {
+                const float f = d == 0 ? p.x : (d == 1 ? p.y : p.z);
+                const float dd = f + (float)(ns - 1 - kq);
+                val = exp2f(-g.beta2[d] * dd * dd);
+            }
+            st_w[i] = val;
+            if (k == 0) {
+                int c0[3];
+                unpack_cells(3, __float_as_uint(p.w), c0[0], c0[1], c0[2]);
+                int r[3];
+#pragma unroll
+                for (int dd = 0; dd < 3; ++dd) {
+                    int rr = c0[dd] - o[dd];
+                    rr += rr < 0 ? g.nf[dd] : 0;
+                    rr -= rr > g.nf[dd] - W ? g.nf[dd] : 0;
+                    r[dd] = rr;
+                }
+                st_r[s] = make_int4(r[0], r[1], r[2], 0);
+            }
+        }
+        for (int i = threadIdx.x; i < n * CG; i += blockDim.x) {
+            const int s = i / CG, cc = i - s * CG;
+            const uint32_t j = a.idx[(int64_t)sub.y + base + s];
+            float2 v = make_float2(0.f, 0.f);
+            if (cg0 + cc < g.n_coil) {
+                v = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
+                if (a.weight) {
+                    const float sw = a.weight[j];
+                    v.x *= sw;
+                    v.y *= sw;
+                }
+            }
+            st_v[i] = v;
+        }
+        __syncthreads();
+
+        for (int s = 0; s < n; ++s) {
+            const int4 r = st_r[s];
+            const int xl = max(x0, r.x), xh = min(x1, r.x + W);
+            if (xl >= xh) continue;
+            const int yl = max(0, r.y), yh = min(e[1], r.y + W);
+            if (yl >= yh) continue;
+            const float2 v = st_v[s * CG + c];
+            const float *w = st_w + s * 48;
+            float wz[L::KT];
+            int lz[L::KT];
+#pragma unroll
+            for (int t = 0; t < L::KT; ++t) {
+                const int kz = q + t * L::NQ;
+                const int z = r.z + kz;
+                const bool ok = kz < W && (unsigned)z < (unsigned)e[2];
+                wz[t] = ok ? w[32 + kz] : 0.f;
+                lz[t] = ok ? z : -1;
+            }
+            for (int x = xl; x < xh; ++x) {
+                const float wx = w[x - r.x];
+                for (int y = yl; y < yh; ++y) {
+                    const float wxy = wx * w[16 + y - r.y];
+                    float2 *rowp = acc + ((size_t)x * TY + y) * TZ * CG + c;
+#pragma unroll
+                    for (int t = 0; t < L::KT; ++t) {
+                        if (lz[t] >= 0) {
+                            float2 *cell = rowp + (size_t)lz[t] * CG;
+                            const float ww = wxy * wz[t];
+                            *cell = __ffma2_rn(make_float2(ww, ww), v, *cell);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    const bool split = (sub.w & kSplitFlag) != 0;
+    const int ecell = e[0] * e[1] * e[2];
+    for (int i = threadIdx.x; i < ecell * CG; i += blockDim.x) {
+        const int cc = i % CG, cell = i / CG;
+        if (cg0 + cc >= g.n_coil) continue;
+        const int lz = cell % e[2], ly = (cell / e[2]) % e[1], lx = cell / (e[2] * e[1]);
+        const float2 val = acc[(((size_t)lx * TY + ly) * TZ + lz) * CG + cc];
+        float2 *dst = a.grid + ((int64_t)grp * g.n_coil + cg0 + cc) * g.G +
+                      ((int64_t)(o[0] + lx) * g.nf[1] + (o[1] + ly)) * g.nf[2] + (o[2] + lz);
+        if (split) {
+            atomicAdd(&dst->x, val.x);
+            atomicAdd(&dst->y, val.y);
+        } else {
+            *dst = val;
+        }
+    }
+}
+
+inline size_t spread3d_smem_bytes(const Geom &g, int cg) {
+    return (size_t)g.tile[0] * g.tile[1] * g.tile[2] * cg * sizeof(float2) + kSpread3dBatch * 48 * sizeof(float) +
+           (size_t)kSpread3dBatch * cg * sizeof(float2) + kSpread3dBatch * sizeof(int4);
+}
+
+inline size_t interp3d_smem_bytes(const Geom &g, int cg) {
+    return (size_t)(g.tile[0] + g.W - 1) * (g.tile[1] + g.W - 1) * (g.tile[2] + g.W - 1) * cg * sizeof(float2);
+}
+
+}  // namespace gbn

@@ -4,6 +4,7 @@
 // lanes).  Otherwise (1-D, 3-D, wide stencils): k_interp (one thread per sample).
 #include "dispatch.cuh"
 #include "grid2d_kernels.cuh"
+#include "grid3d_kernels.cuh"
 
 namespace gbn {
 
@@ -33,6 +34,17 @@ cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, in
             err = set_smem(kern, smem);
             if (err == cudaSuccess) {
                 kern<<<grid, threads, smem, s>>>(a);
+                err = cudaGetLastError();
+            }
+        }));
+        return err;
+    }
+    if (a.g.dim == 3 && a.g.W <= 16) {
+        GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
+            auto kern = k_interp3d<WT, CG>;
+            err = set_smem(kern, smem);
+            if (err == cudaSuccess) {
+                kern<<<grid, threads > 256 ? 256 : threads, smem, s>>>(a);
                 err = cudaGetLastError();
             }
         }));

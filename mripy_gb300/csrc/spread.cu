@@ -4,6 +4,7 @@
 // Otherwise (1-D, 3-D, wide stencils): k_spread (shared-memory atomics).
 #include "dispatch.cuh"
 #include "grid2d_kernels.cuh"
+#include "grid3d_kernels.cuh"
 
 namespace gbn {
 
@@ -14,6 +15,7 @@ static bool use_2d_path(const Geom &g) {
 
 size_t spread_smem_bytes(const Geom &g, int coil_group) {
     if (use_2d_path(g)) return spread2d_smem_bytes(g, coil_group);
+    if (grid3d_applies(g)) return spread3d_smem_bytes(g, coil_group);
     size_t cells = 1;
     for (int d = 0; d < g.dim; ++d) cells *= (size_t)g.tile[d];
     return cells * (size_t)coil_group * sizeof(float2);
@@ -36,6 +38,17 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
             err = set_smem(kern, smem);
             if (err == cudaSuccess) {
                 kern<<<grid, threads, smem, s>>>(a);
+                err = cudaGetLastError();
+            }
+        }));
+        return err;
+    }
+    if (grid3d_applies(a.g)) {
+        GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
+            auto kern = k_spread3d<WT, CG>;
+            err = set_smem(kern, smem);
+            if (err == cudaSuccess) {
+                kern<<<grid, threads > 256 ? 256 : threads, smem, s>>>(a);
                 err = cudaGetLastError();
             }
         }));

@@ -235,6 +235,23 @@ def test_3d_multicoil_against_oracle():
                    O.nufft_type21(tuple(xs), F, (20, 18, 16), dcf=dcf, eps=eps)) < TOL_REF
 
 
+@pytest.mark.parametrize("eps", [5e-6, 1e-5])
+def test_3d_warp_kernels_against_oracle(eps):
+    # grid 48x44x52 >= tile + stencil in every dimension: the warp-level 3-D spread runs;
+    # 5 coils exercise a partly filled coil group
+    rng = np.random.default_rng(21)
+    M, nc, shape = 4000, 5, (24, 22, 26)
+    xs = rng.uniform(-np.pi, np.pi, (3, M))
+    xs[:, :1500] *= 0.1                                          # dense centre: split bins
+    c = cvec(rng, (M, nc)).astype(np.complex128)
+    F = cvec(rng, shape + (nc,)).astype(np.complex128)
+    dcf = rng.uniform(0.5, 1.5, M)
+    assert rel(nf.nufft3d1_gaussker(*xs, c, *shape, eps=eps), O.nufft_type1(tuple(xs), c, shape, eps=eps)) < TOL_REF
+    assert rel(nf.nufft3d2_gaussker(*xs, F, *shape, eps=eps), O.nufft_type2(tuple(xs), F, shape, eps=eps)) < TOL_REF
+    assert rel(nf.nufft3d21_gaussker(*xs, F, *shape, dcf=dcf, eps=eps),
+               O.nufft_type21(tuple(xs), F, shape, dcf=dcf, eps=eps)) < TOL_REF
+
+
 # ------------------------------------------------------------------ SENSE fusion and graphs
 def test_sense_fused_kernels_match_composition():
     rng = np.random.default_rng(17)
