@@ -1,21 +1,28 @@
-"""Benchmark: batched NUFFT forward + adjoint Msamples/s on the batched 2-D multi-coil
-workload (256^2 image x 8 coils, golden-angle radial 402 spokes x 512 samples,
-oversampled grid 512^2, nspread 6).
+"""Benchmark: batched NUFFT forward + adjoint throughput (Msamples/s).
 
-One step = type-2 (forward) + type-1 (adjoint) over all 8 coils, replayed from one
-CUDA graph; value = (samples x coils) / step time.  Also reported:
-  plain       the per-instance path: one single-coil plan, eager launches, coil by coil
-  e2e         the same step through the C ABI with host (pinned) buffers, H2D and D2H
-              inside the timed region (gbn_type2_host + gbn_type1_host)
-  roofline    dominant gridding kernel: algorithmic bytes / its CUDA-event duration vs
-              the measured HBM copy bandwidth; fp32 fraction beside it
-  cpu_baseline  the FP64 C restatement of mripy's CPU NUFFT on the host cores
-  accuracy    relative L2 error vs the FP64 NUDFT on a sample subset
+Default workload (the headline): configuration 2, 2-D 256^2 image x 8 coils,
+golden-angle radial 402 spokes x 512 samples, oversampled grid 512^2, nspread 6.
+``--workload c1..c5`` measures the other configurations the same way:
+  c1  2-D 128^2, 1 coil, uniform radial 128 x 256
+  c3  64 frames x 12 coils of 192^2, ragged golden-angle spokes U{5..34} x 384
+  c4  3-D 128^3 x 8 coils, 20,000 centre-out spokes x 128 (256^3 grid)
+  c5  2-D 256^2 x 16 coils, variable-density spiral 24 x 2048, perturbed coordinates
+
+One step = type-2 (forward) + type-1 (adjoint) over every instance (group x coil),
+replayed from one CUDA graph; value = (samples x coils) / step time.  Also reported:
+  plain        the per-instance path: single-coil plans, eager launches, instance by instance
+  e2e          the same step through the C ABI with pinned host buffers, H2D and D2H inside
+               the timed region (gbn_type2_host + gbn_type1_host)
+  roofline     dominant gridding kernel: algorithmic bytes / its CUDA-event time vs the
+               measured HBM copy bandwidth, with the FP32 rate beside it
+  cpu_baseline the FP64 C restatement of mripy's CPU NUFFT on the host cores
+  accuracy     relative L2 error vs the FP64 NUDFT on a subset
+  solver       c2: 20 CG-SENSE iterations through the graph-captured normal operator
 
 --impl reference times mripy's CPU NUFFT algorithm (the oracle port; mripy itself is
-Python/numba and is not installed on the GPU host) on the same workload.
-Under torchrun (N > 1) every rank runs its own replica (weak scaling, no collective
-in the data path); rank 0 prints the line with the max step time over ranks.
+Python + numba and is not installed on the GPU host) on the same workload.
+Under torchrun (N > 1) every rank runs its own replica (weak scaling, no collective in
+the data path); rank 0 prints the line with the max step time over ranks.
 """
 import argparse
 import ctypes
@@ -32,7 +39,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "batched NUFFT fwd+adj Msamples/s vs per-instance plain at ≤1e-4 rel err"
-WORKLOAD = "2-D 8-coil golden-angle radial 402x512 samples, 256^2 image, 512^2 grid, nspread 6 (eps 5e-6)"
 UNIT = "Msamples/s"
 L2_BYTES = 129 * 2 ** 20
 
@@ -118,7 +124,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons, all_sm = [], 0.0, set(), []
+        sm, smax, reasons = [], 0.0, set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
         pad = datetime.timedelta(milliseconds=25)
         for ln in self.lines:
@@ -131,7 +137,6 @@ class ClockSampler:
                 smax = max(smax, float(parts[3]))
             except ValueError:
                 continue
-            all_sm.append(mhz)
             if self.t0 is not None and not (self.t0 - pad <= ts <= self.t1 + pad):
                 continue
             sm.append(mhz)
@@ -145,22 +150,58 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-# ------------------------------------------------------------------------------ workload
+# ------------------------------------------------------------------------------ workloads
 
-def make_workload(torch):
+class Workload:
+    def __init__(self, name, description, dim, shape, coords, imgs, n_coil, offsets=None, eps=5e-6,
+                 max_nspread=None, sens=None, base_image=None):
+        self.name, self.description, self.dim, self.shape = name, description, dim, tuple(shape)
+        self.coords = [np.ascontiguousarray(c, dtype=np.float64) for c in coords]   # radians
+        self.imgs = imgs                      # (n_traj, *shape, n_coil) complex64
+        self.n_coil = n_coil
+        self.M = len(self.coords[0])
+        self.offsets = list(offsets) if offsets is not None else [0, self.M]
+        self.n_traj = len(self.offsets) - 1
+        self.eps, self.max_nspread = eps, max_nspread
+        self.sens, self.base_image = sens, base_image
+
+
+def make_workload(name):
     from mripy_gb300 import synth
-    cfg = synth.config2()
-    kx, ky = cfg["k"]
-    x = 2 * np.pi * kx
-    y = 2 * np.pi * ky
-    imgs = (cfg["image"][..., None] * cfg["sens"]).astype(np.complex64)       # (256, 256, 8) coil images
-    return x, y, imgs
+    two_pi = 2 * np.pi
+    if name == "c1":
+        cfg = synth.config1()
+        return Workload("c1", "2-D 128^2, 1 coil, uniform radial 128x256, 256^2 grid, nspread 6", 2, (128, 128),
+                        [two_pi * k for k in cfg["k"]], cfg["image"][None, ..., None], 1)
+    if name == "c2":
+        cfg = synth.config2()
+        imgs = (cfg["image"][..., None] * cfg["sens"]).astype(np.complex64)[None]
+        return Workload("c2", "2-D 8-coil golden-angle radial 402x512 samples, 256^2 image, 512^2 grid, "
+                        "nspread 6 (eps 5e-6)", 2, (256, 256), [two_pi * k for k in cfg["k"]], imgs, 8,
+                        sens=cfg["sens"], base_image=cfg["image"])
+    if name == "c3":
+        cfg = synth.config3()
+        return Workload("c3", "64 frames x 12 coils of 192^2, ragged golden-angle spokes U{5..34} x 384, "
+                        "384^2 grid, nspread 6", 2, (192, 192), [two_pi * k for k in cfg["k"]], cfg["image"], 12,
+                        offsets=cfg["offsets"])
+    if name == "c4":
+        cfg = synth.config4()
+        imgs = (cfg["image"][..., None] * cfg["sens"]).astype(np.complex64)[None]
+        return Workload("c4", "3-D 128^3 x 8 coils, 20000 centre-out spokes x 128 (Fibonacci sphere), 256^3 grid, "
+                        "nspread 6", 3, (128, 128, 128), [two_pi * k for k in cfg["k"]], imgs, 8, max_nspread=6,
+                        sens=cfg["sens"], base_image=cfg["image"])
+    if name == "c5":
+        cfg = synth.config5()
+        return Workload("c5", "2-D 256^2 x 16 coils, variable-density spiral 24x2048, perturbed coordinates, "
+                        "512^2 grid, nspread 6", 2, (256, 256), [two_pi * k for k in cfg["k_perturbed"]],
+                        cfg["image"][None], 16)
+    raise ValueError("unknown workload " + name)
 
 
-def algorithmic_bytes(M, n_coil, dim, grid_cells):
-    """Per direction: samples (complex64) + packed coordinates read once per shared
-    trajectory (4 B per dim) + the oversampled grid of every coil (complex64)."""
-    return 8 * M * n_coil + 4 * dim * M + 8 * grid_cells * n_coil
+def algorithmic_bytes(M, n_coil, dim, grid_cells, n_inst):
+    """Per direction: samples (complex64, every coil) + packed coordinates read once per
+    shared trajectory (4 B per dim) + the oversampled grid of every instance (complex64)."""
+    return 8 * M * n_coil + 4 * dim * M + 8 * grid_cells * n_inst
 
 
 def flops(M, n_coil, W, dim):
@@ -184,7 +225,7 @@ def event_time(torch, fn, reps, stream, flush=None):
     return float(np.median(ts)), ts
 
 
-def run_gpu(args):
+def run_gpu(args, wl):
     import torch
     from mripy_gb300 import _native as N
     from mripy_gb300.plan import NufftPlan
@@ -195,14 +236,13 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    x, y, imgs = make_workload(torch)
-    M, n_coil, shape = len(x), imgs.shape[-1], imgs.shape[:2]
-    xd = torch.from_numpy(x).to(dev)
-    yd = torch.from_numpy(y).to(dev)
-    img = torch.from_numpy(imgs).to(dev)[None]                              # (1, 256, 256, 8)
+    coords = [torch.from_numpy(c).to(dev) for c in wl.coords]
+    img = torch.from_numpy(np.ascontiguousarray(wl.imgs)).to(dev)           # (n_traj, *shape, n_coil)
+    M, n_coil, n_inst = wl.M, wl.n_coil, wl.n_traj * wl.n_coil
     samples = torch.empty((M, n_coil), dtype=torch.complex64, device=dev)
     out_img = torch.empty_like(img)
-    plan = NufftPlan(2, shape, n_coil=n_coil, eps=5e-6).set_points([xd, yd])
+    plan = NufftPlan(wl.dim, wl.shape, n_coil=n_coil, n_traj=wl.n_traj, eps=wl.eps, max_nspread=wl.max_nspread)
+    plan.set_points(coords, traj_offsets=wl.offsets)
     info = plan.info()
     stream = torch.cuda.current_stream()
     flush_buf = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
@@ -241,7 +281,7 @@ def run_gpu(args):
     if sampler:
         sampler.mark_start()
     t_wall = time.perf_counter()
-    step_ms_med, step_ms = event_time(torch, g.replay, args.steps, stream, flush)
+    _, step_ms = event_time(torch, g.replay, args.steps, stream, flush)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
     if sampler:
@@ -253,10 +293,10 @@ def run_gpu(args):
     result = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": round(mean_ms, 4), "higher_is_better": True,
               "scaling": "weak", "vs_baseline": None, "dtype": "c64",
-              "data": "synthetic (seeded phantom x coil maps, golden-angle radial trajectory)",
-              "config": {"workload": WORKLOAD, "samples_per_coil": M, "coils": n_coil, "image": list(shape),
-                         "grid": list(info["nf"]), "nspread": info["nspread"],
-                         "step": "type-2 + type-1 over all coils, one CUDA graph",
+              "data": "synthetic (seeded phantoms/random images x coil maps, %s)" % wl.description,
+              "config": {"workload": wl.description, "samples": M, "coils": n_coil, "groups": wl.n_traj,
+                         "image": list(wl.shape), "grid": list(info["nf"]), "nspread": info["nspread"],
+                         "step": "type-2 + type-1 over all instances, one CUDA graph",
                          "l2": "flushed between timed steps (write of %d MiB)" % (2 * L2_BYTES // 2 ** 20),
                          "parallelism": "replicas" if world > 1 else "single GPU"},
               "wall_s_timed": round(t_wall, 3)}
@@ -265,76 +305,89 @@ def run_gpu(args):
             torch.distributed.barrier()
         return None
 
-    # --- per-kernel timing (gridding stages alone, same stream, L2 flushed)
+    # --- per-kernel timing (stages alone, same stream, L2 flushed)
     grid = plan.grid()
     plan.pad_deapod(img, grid)
     plan.fft(grid, N.GBN_FFT_FORWARD)
     grid_copy = grid.clone()
-    t_interp, _ = event_time(torch, lambda: plan.interp(grid_copy, out=samples), 20, stream, flush)
-    t_spread, _ = event_time(torch, lambda: plan.spread(samples, grid), 20, stream, flush)
-    t_pad, _ = event_time(torch, lambda: plan.pad_deapod(img, grid), 20, stream, flush)
-    t_fft, _ = event_time(torch, lambda: plan.fft(grid, N.GBN_FFT_FORWARD), 20, stream, flush)
-    t_crop, _ = event_time(torch, lambda: plan.crop_deapod(grid, out_img), 20, stream, flush)
+    reps = 20 if wl.dim == 2 else 5
+    t_interp, _ = event_time(torch, lambda: plan.interp(grid_copy, out=samples), reps, stream, flush)
+    t_spread, _ = event_time(torch, lambda: plan.spread(samples, grid), reps, stream, flush)
+    t_pad, _ = event_time(torch, lambda: plan.pad_deapod(img, grid), reps, stream, flush)
+    t_fft, _ = event_time(torch, lambda: plan.fft(grid, N.GBN_FFT_FORWARD), reps, stream, flush)
+    t_crop, _ = event_time(torch, lambda: plan.crop_deapod(grid, out_img), reps, stream, flush)
+    del grid_copy
     G = info["grid_cells"]
-    bytes_dir = algorithmic_bytes(M, n_coil, 2, G)
-    fl = flops(M, n_coil, 2 * info["nspread"], 2)
+    bytes_dir = algorithmic_bytes(M, n_coil, wl.dim, G, n_inst)
+    fl = flops(M, n_coil, 2 * info["nspread"], wl.dim)
     hbm, peak_kind = peaks()
     dominant = "spread" if t_spread >= t_interp else "interp"
     t_dom = max(t_spread, t_interp)
     achieved = bytes_dir / (t_dom * 1e-3) / 1e9
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "ncu_traffic_c2.txt")
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic_%s.txt" % wl.name)
     if os.path.exists(tpath):
         for ln in open(tpath):
             if ln.startswith(dominant + "_dram_bytes_per_launch:"):
                 traffic = int(ln.split(":")[1])
     result["roofline"] = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1),
                           "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic,
-                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                          else "fallback 6.8 TB/s",
+                          "peak_source": ("of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                                          else "of fallback 6.8 TB/s"),
                           "algorithmic_bytes_per_launch": bytes_dir,
                           "fp32_tflops_achieved": round(fl / (t_dom * 1e-3) / 1e12, 2)}
     result["kernels_ms"] = {"interp": round(t_interp, 4), "spread": round(t_spread, 4), "pad_deapod": round(t_pad, 4),
                             "fft": round(t_fft, 4), "crop_deapod": round(t_crop, 4)}
     result["gpu_launches"] = 5 * args.steps  # pad, interp, zero-split, spread, crop per step (cuFFT not counted)
 
-    # --- plain per-instance path: single-coil plan, eager, coil by coil
-    p1 = NufftPlan(2, shape, n_coil=1, eps=5e-6).set_points([xd, yd])
-    s1 = torch.empty((M, 1), dtype=torch.complex64, device=dev)
-    o1 = torch.empty((1,) + tuple(shape) + (1,), dtype=torch.complex64, device=dev)
-    coil_imgs = [img[..., c:c + 1].contiguous() for c in range(n_coil)]
+    # --- plain per-instance path: single-coil plan per group, eager, instance by instance
+    plans = []
+    for gi in range(wl.n_traj):
+        a, b = wl.offsets[gi], wl.offsets[gi + 1]
+        p1 = NufftPlan(wl.dim, wl.shape, n_coil=1, eps=wl.eps, max_nspread=wl.max_nspread)
+        p1.set_points([c[a:b] for c in coords])
+        plans.append((p1, torch.empty((b - a, 1), dtype=torch.complex64, device=dev),
+                      [img[gi, ..., c:c + 1].contiguous()[None] for c in range(n_coil)]))
+    o1 = torch.empty((1,) + wl.shape + (1,), dtype=torch.complex64, device=dev)
 
     def plain_step():
-        for c in range(n_coil):
-            p1.type2(coil_imgs[c], out=s1)
-            p1.type1(s1, out=o1)
+        for p1, s1, coil_imgs in plans:
+            for ci in coil_imgs:
+                p1.type2(ci, out=s1)
+                p1.type1(s1, out=o1)
 
-    for _ in range(3):
+    for _ in range(2):
         plain_step()
-    t_plain, _ = event_time(torch, plain_step, min(100, max(5, args.steps // 2)), stream, flush)
+    t_plain, _ = event_time(torch, plain_step, min(20, max(3, args.steps // 10)), stream, flush)
     result["plain"] = {"value": round(M * n_coil / (t_plain * 1e-3) / 1e6, 2), "unit": UNIT,
                        "ms_per_step": round(t_plain, 4), "speedup_batched_vs_plain": round(t_plain / mean_ms, 2)}
+    for p1, _, _ in plans:
+        p1.close()
+    del plans
 
-    # --- accuracy vs FP64 NUDFT on a subset
+    # --- accuracy vs the FP64 NUDFT on a subset (first group)
     import oracle as O
     plan.type2(img, out=samples)
     plan.type1(samples, out=out_img)
     torch.cuda.synchronize()
     rng = np.random.default_rng(1)
-    sub = rng.choice(M, 512, replace=False)
+    a, b = wl.offsets[0], wl.offsets[1]
+    nsub = 256 if wl.dim == 2 else 48
+    sub = a + rng.choice(b - a, min(nsub, b - a), replace=False)
     cf = samples.cpu().numpy()
-    ex = O.nudft_type2((x[sub], y[sub]), imgs[..., :2].astype(np.complex128), tuple(shape))
-    err_fwd = np.linalg.norm(cf[sub, :2] - ex) / np.linalg.norm(ex)
-    pix = rng.choice(shape[0] * shape[1], 256, replace=False)
-    cs = cf[:, :1].astype(np.complex128)
-    exa = O.nudft_type1((x, y), cs, tuple(shape), pixels=pix)[:, 0]
+    ex = O.nudft_type2(tuple(c[sub] for c in wl.coords), wl.imgs[0, ..., :1].astype(np.complex128), wl.shape)
+    err_fwd = np.linalg.norm(cf[sub, :1] - ex) / np.linalg.norm(ex)
+    npix = 256 if wl.dim == 2 else 32
+    pix = rng.choice(int(np.prod(wl.shape)), npix, replace=False)
+    cs = cf[a:b, :1].astype(np.complex128)
+    exa = O.nudft_type1(tuple(c[a:b] for c in wl.coords), cs, wl.shape, pixels=pix)[:, 0]
     ga = out_img[0, ..., 0].cpu().numpy().reshape(-1)[pix]
     err_adj = np.linalg.norm(ga - exa) / np.linalg.norm(exa)
     result["accuracy"] = {"fwd_rel_l2_vs_nudft": float("%.3e" % err_fwd), "adj_rel_l2_vs_nudft": float("%.3e" % err_adj),
-                          "target": 1e-4}
+                          "target": 1e-4, "subset": "%d samples / %d pixels of group 0, coil 0" % (len(sub), npix)}
 
     # --- end to end through the C ABI with pinned host buffers
-    h_img = torch.from_numpy(imgs.reshape(1, *imgs.shape)).pin_memory()
+    h_img = torch.from_numpy(np.ascontiguousarray(wl.imgs)).pin_memory()
     h_k = torch.empty((M, n_coil), dtype=torch.complex64).pin_memory()
     h_out = torch.empty_like(h_img).pin_memory()
     lib = N.lib()
@@ -344,25 +397,29 @@ def run_gpu(args):
         N.check(lib.gbn_type2_host(plan._h, ctypes.c_void_p(h_img.data_ptr()), ctypes.c_void_p(h_k.data_ptr()), sp))
         N.check(lib.gbn_type1_host(plan._h, ctypes.c_void_p(h_k.data_ptr()), ctypes.c_void_p(h_out.data_ptr()), sp))
 
-    for _ in range(3):
+    for _ in range(2):
         e2e_step()
     ts = []
-    for _ in range(min(50, max(5, args.steps))):
+    for _ in range(min(30 if wl.dim == 2 else 5, max(3, args.steps))):
         flush()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e2e_step()
         ts.append(time.perf_counter() - t0)
     t_e2e = float(np.mean(ts))
-    img_bytes = imgs.nbytes
+    img_bytes = wl.imgs.nbytes
     k_bytes = M * n_coil * 8
     result["e2e"] = {"value": round(M * n_coil / t_e2e / 1e6, 2), "unit": UNIT,
                      "h2d_bytes_per_step": img_bytes + k_bytes, "d2h_bytes_per_step": k_bytes + img_bytes,
                      "ms_per_step": round(t_e2e * 1e3, 3),
                      "path": "gbn_type2_host + gbn_type1_host (host pinned buffers, includes H2D and D2H)"}
 
+    # --- solver: 20 CG-SENSE iterations through the graph-captured normal operator
+    if wl.name == "c2":
+        result["solver"] = cg_sense_time(torch, wl, coords)
+
     # --- CPU baseline: FP64 port of mripy's CPU NUFFT on the host cores (bounded sample)
-    result["cpu_baseline"] = cpu_baseline(x, y, imgs, sample_coils=n_coil, reps=1)
+    result["cpu_baseline"] = cpu_baseline(wl, reps=1)
     if clocks:
         result["clocks"] = clocks
     if world > 1:
@@ -370,51 +427,81 @@ def run_gpu(args):
     return result
 
 
-def cpu_baseline(x, y, imgs, sample_coils, reps=1):
+def cg_sense_time(torch, wl, coords):
+    from mripy_gb300 import operators as ops
+    from mripy_gb300 import solvers
+    nft = ops.NUFFT2d(wl.shape)
+    nft.set_ktraj(coords[0], coords[1])
+    A = ops.joint2operators(ops.espirit(wl.sens), nft)
+    x = torch.from_numpy(wl.base_image).cuda()[..., None]
+    y = A.forward(x)
+    rng = np.random.default_rng(2)
+    sigma = float(torch.linalg.vector_norm(y)) / np.sqrt(y.numel()) * 10 ** (-30 / 20)
+    noise = torch.from_numpy((rng.standard_normal(tuple(y.shape)) + 1j * rng.standard_normal(tuple(y.shape)))
+                             .astype(np.complex64) * sigma / np.sqrt(2)).cuda()
+    y = y + noise
+    solvers.cg_sense(A, y, n_iter=20)             # warm-up (plans, graph)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xr, norms = solvers.cg_sense(A, y, n_iter=20)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    # relative error against the phantom after a least-squares scale
+    xt = x.reshape(-1)
+    xh = xr.reshape(-1)
+    a = torch.vdot(xh, xt) / torch.vdot(xh, xh)
+    err = float(torch.linalg.vector_norm(a * xh - xt) / torch.linalg.vector_norm(xt))
+    return {"cg_sense_iterations": 20, "ms_total": round(dt * 1e3, 2),
+            "ms_per_iteration": round(dt * 1e3 / 20, 3), "residual_reduction": float("%.3e" % float(norms[-1] / norms[0])),
+            "rel_error_vs_phantom": round(err, 4), "noise": "complex Gaussian, 30 dB SNR"}
+
+
+def cpu_baseline(wl, reps=1):
+    """The FP64 C restatement of mripy's CPU NUFFT (oracle/) on the host cores: fwd + adj
+    of group 0.  2-D: every coil, all samples; 3-D: 1 coil and the first 400,000 samples
+    (about 10-30 s of CPU work), scaled to samples per second."""
     import oracle as O
     cores = os.cpu_count() or 1
     workers = min(cores, 64)
-    shape = imgs.shape[:2]
-    sub = imgs[..., :sample_coils].astype(np.complex128)
-    O.nufft_type2((x[:1000], y[:1000]), sub[..., :1], shape, eps=5e-6)         # load the library
+    a, b = wl.offsets[0], wl.offsets[1]
+    if wl.dim == 3:
+        ncs, nsamp = 1, min(400000, b - a)
+    else:
+        ncs, nsamp = wl.n_coil, b - a
+    xs = tuple(c[a:a + nsamp] for c in wl.coords)
+    sub = wl.imgs[0, ..., :ncs].astype(np.complex128)
+    O.nufft_type2(tuple(c[:100] for c in xs), sub[..., :1], wl.shape, eps=wl.eps)   # load the library
     ts = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        c = O.nufft_type2((x, y), sub, shape, eps=5e-6, workers=workers)
-        O.nufft_type1((x, y), c, shape, eps=5e-6, workers=workers)
+        c = O.nufft_type2(xs, sub, wl.shape, eps=wl.eps, workers=workers)
+        O.nufft_type1(xs, c, wl.shape, eps=wl.eps, workers=workers)
         ts.append(time.perf_counter() - t0)
     t = float(np.median(ts))
-    return {"value": round(len(x) * sample_coils / t / 1e6, 3), "unit": UNIT, "kind": "port",
-            "cores": min(cores, sample_coils),
-            "sample": "full workload, %d coils, fwd+adj, FP64 C restatement of build_grid_2d{1,2}_fast "
+    return {"value": round(nsamp * ncs / t / 1e6, 3), "unit": UNIT, "kind": "port",
+            "cores": min(cores, ncs),
+            "sample": "%s: group 0, %d coil(s), %d samples, fwd+adj, FP64 C restatement of build_grid_*_fast "
                       "(OpenMP over coils as mripy's prange) + scipy.fft with %d workers; %d rep(s)" % (
-                          sample_coils, workers, reps),
+                          wl.name, ncs, nsamp, workers, reps),
             "seconds": round(t, 3)}
 
 
-def run_reference(args):
+def run_reference(args, wl):
     rank, world, _ = dist_env()
     if rank != 0:
         return None
-    from mripy_gb300 import synth
-    cfg = synth.config2()
-    kx, ky = cfg["k"]
-    x, y = 2 * np.pi * kx, 2 * np.pi * ky
-    imgs = (cfg["image"][..., None] * cfg["sens"]).astype(np.complex64)
-    n_coil = imgs.shape[-1]
     for _ in range(max(0, args.warmup)):
-        cpu_baseline(x, y, imgs, n_coil, reps=1)
+        cpu_baseline(wl, reps=1)
     t0 = time.perf_counter()
-    vals = [cpu_baseline(x, y, imgs, n_coil, reps=1) for _ in range(args.steps)]
+    vals = [cpu_baseline(wl, reps=1) for _ in range(args.steps)]
     wall = time.perf_counter() - t0
-    secs = float(np.mean([v["seconds"] for v in vals]))
-    value = len(x) * n_coil / secs / 1e6
+    value = float(np.mean([v["value"] for v in vals]))
     cb = dict(vals[0])
     cb["value"] = round(value, 3)
     return {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(secs * 1e3, 2), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": WORKLOAD}, "impl": "reference",
+            "warmup": args.warmup, "ms_per_step": round(float(np.mean([v["seconds"] for v in vals])) * 1e3, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": wl.description}, "impl": "reference",
             "reference_note": "mripy's NUFFT is Python+numba (not installable on the GPU host); timed as the FP64 "
                               "C restatement of its CPU loops (oracle/), on all host threads it can use",
             "cpu_baseline": cb,
@@ -428,16 +515,19 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "gb300":
+        args.warmup = max(args.warmup, 3)
     import oracle
     oracle.build()
+    wl = make_workload(args.workload)
     if args.impl == "reference":
-        res = run_reference(args)
+        res = run_reference(args, wl)
     else:
         from mripy_gb300 import build
         build.build()
-        res = run_gpu(args)
+        res = run_gpu(args, wl)
     if res is not None:
         print(json.dumps(res))
 

@@ -474,7 +474,22 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
             return fail(GBN_ERR_ARG, "threads must be 128, 256 or 512");
         }
     }
-    p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem : 256;
+    // 2-D with 4 or 8 coils per block: the register-tile spread kernel, whose tile is
+    // (4 rows x warps) x (4 columns x 32/coils) cells, unless the caller chose a tile.
+    // Measured on GB300 (8 coils, 512^2 radial): 128-thread blocks, 128-sample work items.
+    bool reg_spread = false;
+    if (p->dim == 2 && desc->spread_tile[0] <= 0 && desc->spread_tile[1] <= 0) {
+        const int cg_eff = std::min(p->coil_group, pow2_floor(std::max(1, (int)desc->n_coil)));
+        if (cg_eff >= 4) {
+            if (desc->threads <= 0) p->threads = 128;
+            if (p->threads <= 256) {
+                ts[0] = 4 * (p->threads / 32);
+                ts[1] = 4 * (32 / cg_eff);
+                reg_spread = true;
+            }
+        }
+    }
+    p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem : (reg_spread ? 128 : 256);
     make_geom(p, ts, p->gs);
     make_geom(p, ti, p->gi);
 

@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
     float *st_w = reinterpret_cast<float *>(acc + (size_t)TX * TY * CG);  // [batch][32]: wx[16], wy[16]
     float2 *st_v = reinterpret_cast<float2 *>(st_w + kSpreadBatch * 32);  // [batch][CG]
     int2 *st_r = reinterpret_cast<int2 *>(st_v + kSpreadBatch * CG);      // [batch]: local first-tap cell
+    int *st_y = reinterpret_cast<int *>(st_r + kSpreadBatch);             // [batch][16]: local y of tap ky, -1 off tile
 
     const int4 sub = a.subs[blockIdx.x];
     const int cg0 = blockIdx.y * CG;
@@ -177,18 +178,20 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
                 val = exp2f(-(k < 16 ? g.beta2[0] : g.beta2[1]) * d * d);
             }
             st_w[i] = val;
-            if (k == 0) {
-                // signed local position of the first tap: in (-W, nf - W].  The stencil
-                // [r, r + W) never wraps onto the tile twice because nf >= tile + W on this
-                // path (the generic kernel serves smaller grids).
-                int c0x, c0y, c0z;
-                unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
-                int rx = c0x - o0, ry = c0y - o1;
-                rx += rx < 0 ? nf0 : 0;
-                ry += ry < 0 ? nf1 : 0;
-                rx -= rx > nf0 - W ? nf0 : 0;
-                ry -= ry > nf1 - W ? nf1 : 0;
-                st_r[s] = make_int2(rx, ry);
+            // signed local position of the first tap: in (-W, nf - W].  The stencil
+            // [r, r + W) never wraps onto the tile twice because nf >= tile + W on this
+            // path (the generic kernel serves smaller grids).
+            int c0x, c0y, c0z;
+            unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
+            int rx = c0x - o0, ry = c0y - o1;
+            rx += rx < 0 ? nf0 : 0;
+            ry += ry < 0 ? nf1 : 0;
+            rx -= rx > nf0 - W ? nf0 : 0;
+            ry -= ry > nf1 - W ? nf1 : 0;
+            if (k == 0) st_r[s] = make_int2(rx, ry);
+            if (k >= 16) {
+                const int y = ry + kq;
+                st_y[s * 16 + kq] = (kq < W && (unsigned)y < (unsigned)e1) ? y : -1;
             }
         }
         for (int i = threadIdx.x; i < n * CG; i += blockDim.x) {
@@ -215,30 +218,28 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
             if (lo >= hi) continue;
             const float2 v = st_v[s * CG + c];
             const float *w = st_w + s * 32;
-            float wy[L::KT];
+            // per lane: the column weight folded into the coil value, and the tap's tile column
+            float2 wyv[L::KT];
             int ly[L::KT];
 #pragma unroll
             for (int t = 0; t < L::KT; ++t) {
                 const int ky = q + t * L::NQ;
-                const int y = r.y + ky;
-                const bool ok = ky < W && (unsigned)y < (unsigned)e1;
-                wy[t] = ok ? w[16 + ky] : 0.f;
-                ly[t] = ok ? y : -1;
+                const bool in = ky < 16;
+                const float wy = in ? w[16 + (in ? ky : 0)] : 0.f;
+                ly[t] = in ? st_y[s * 16 + (in ? ky : 0)] : -1;
+                wyv[t] = make_float2(wy * v.x, wy * v.y);
             }
             const float *wx_row = w - r.x;
             float2 *dst = acc + (size_t)lo * TY * CG + c;
 #pragma unroll 4
             for (int row = lo; row < hi; ++row, dst += TY * CG) {
                 const float wx = wx_row[row];
+                const float2 wx2 = make_float2(wx, wx);
 #pragma unroll
                 for (int t = 0; t < L::KT; ++t) {
                     if (ly[t] >= 0) {
                         float2 *cell = dst + (size_t)ly[t] * CG;
-                        const float ww = wx * wy[t];
-                        float2 o = *cell;
-                        o.x = fmaf(ww, v.x, o.x);
-                        o.y = fmaf(ww, v.y, o.y);
-                        *cell = o;
+                        *cell = __ffma2_rn(wx2, wyv[t], *cell);
                     }
                 }
             }
@@ -265,9 +266,143 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
     }
 }
 
+// ------------------------------------------------------------------ spread, register tile
+// For 4 or 8 coils per block the output tile lives in registers: warp w owns the rows
+// [4w, 4w + 4) and lane (c, q) holds columns q, q + NQ, q + 2NQ, q + 3NQ of coil c, so the
+// tile is (4 * warps) x (4 * NQ) cells.  Per staged sample a warp whose rows the stencil
+// reaches folds the column weights into the coil value once (4 complex values per lane)
+// and then needs one broadcast load and 4 packed FMAs per row; there is no shared-memory
+// read-modify-write at all.  Columns outside the stencil carry a zero weight.
+constexpr int kRegRows = 4;  // rows per warp
+constexpr int kRegCols = 4;  // columns per lane
+
+template <int WT, int CG>
+__global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
+    constexpr int NQ = 32 / CG;
+    extern __shared__ float4 smem_r2[];
+    const Geom &g = a.g;
+    float *st_w = reinterpret_cast<float *>(smem_r2);                     // [batch][32]: wx[16], wy[16]
+    float2 *st_v = reinterpret_cast<float2 *>(st_w + kSpreadBatch * 32);  // [batch][CG]
+    int2 *st_r = reinterpret_cast<int2 *>(st_v + kSpreadBatch * CG);      // [batch]: signed first taps
+
+    const int4 sub = a.subs[blockIdx.x];
+    const int cg0 = blockIdx.y * CG;
+    const int grp = sub.x / g.ntiles;
+    const int tile = sub.x % g.ntiles;
+    const int TX = g.tile[0], TY = g.tile[1];  // TX = 4 * warps, TY = 4 * NQ (set by the host)
+    const int o0 = (tile / g.ntile[1]) * TX;
+    const int o1 = (tile % g.ntile[1]) * TY;
+    const int nf0 = g.nf[0], nf1 = g.nf[1];
+    const int e0 = min(TX, nf0 - o0), e1 = min(TY, nf1 - o1);
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const int row0 = warp * kRegRows;
+    float2 acc[kRegRows][kRegCols];
+#pragma unroll
+    for (int r = 0; r < kRegRows; ++r)
+#pragma unroll
+        for (int k = 0; k < kRegCols; ++k) acc[r][k] = make_float2(0.f, 0.f);
+
+    for (int base = 0; base < sub.z; base += kSpreadBatch) {
+        const int n = min(kSpreadBatch, sub.z - base);
+        __syncthreads();  // previous batch consumed
+        for (int i = threadIdx.x; i < n * 32; i += blockDim.x) {
+            const int s = i >> 5, k = i & 31, kq = k & 15;
+            const float4 p = a.pts[(int64_t)sub.y + base + s];
+            float val = 0.f;
+            if (kq < W) {
+                const float d = (k < 16 ? p.x : p.y) + (float)(ns - 1 - kq);
+                val = exp2f(-(k < 16 ? g.beta2[0] : g.beta2[1]) * d * d);
+            }
+            st_w[i] = val;
+            if (k == 0) {
+                // signed local first-tap cell, in (-W, nf - W] (nf >= tile + W on this path)
+                int c0x, c0y, c0z;
+                unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
+                int rx = c0x - o0, ry = c0y - o1;
+                rx += rx < 0 ? nf0 : 0;
+                ry += ry < 0 ? nf1 : 0;
+                rx -= rx > nf0 - W ? nf0 : 0;
+                ry -= ry > nf1 - W ? nf1 : 0;
+                st_r[s] = make_int2(rx, ry);
+            }
+        }
+        for (int i = threadIdx.x; i < n * CG; i += blockDim.x) {
+            const int s = i / CG, cc = i - s * CG;
+            const uint32_t j = a.idx[(int64_t)sub.y + base + s];
+            float2 v = make_float2(0.f, 0.f);
+            if (cg0 + cc < g.n_coil) {
+                v = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
+                if (a.weight) {
+                    const float sw = a.weight[j];
+                    v.x *= sw;
+                    v.y *= sw;
+                }
+            }
+            st_v[i] = v;
+        }
+        __syncthreads();
+
+        for (int s = 0; s < n; ++s) {
+            const int2 r = st_r[s];
+            if (r.x + W <= row0 || r.x >= row0 + kRegRows) continue;  // warp-uniform
+            const float *w = st_w + s * 32;
+            const float2 v = st_v[s * CG + c];
+            float2 wyv[kRegCols];
+#pragma unroll
+            for (int k = 0; k < kRegCols; ++k) {
+                const int ky = q + k * NQ - r.y;
+                const float wy = (unsigned)ky < (unsigned)W ? w[16 + (ky & 15)] : 0.f;
+                wyv[k] = make_float2(wy * v.x, wy * v.y);
+            }
+#pragma unroll
+            for (int rr = 0; rr < kRegRows; ++rr) {
+                const int kx = row0 + rr - r.x;
+                if ((unsigned)kx < (unsigned)W) {
+                    const float wx = w[kx];
+                    const float2 wx2 = make_float2(wx, wx);
+#pragma unroll
+                    for (int k = 0; k < kRegCols; ++k) acc[rr][k] = __ffma2_rn(wx2, wyv[k], acc[rr][k]);
+                }
+            }
+        }
+    }
+
+    // flush the register tile: rows and columns beyond the grid edge are dropped
+    if (cg0 + c >= g.n_coil) return;
+    const bool split = (sub.w & kSplitFlag) != 0;
+    float2 *dstc = a.grid + ((int64_t)grp * g.n_coil + cg0 + c) * g.G;
+#pragma unroll
+    for (int rr = 0; rr < kRegRows; ++rr) {
+        const int lx = row0 + rr;
+        if (lx >= e0) break;
+#pragma unroll
+        for (int k = 0; k < kRegCols; ++k) {
+            const int ly = q + k * NQ;
+            if (ly >= e1) continue;
+            float2 *dst = dstc + (int64_t)(o0 + lx) * nf1 + (o1 + ly);
+            if (split) {
+                atomicAdd(&dst->x, acc[rr][k].x);
+                atomicAdd(&dst->y, acc[rr][k].y);
+            } else {
+                *dst = acc[rr][k];
+            }
+        }
+    }
+}
+
+inline size_t spread2d_reg_smem_bytes(int cg) {
+    return kSpreadBatch * 32 * sizeof(float) + (size_t)kSpreadBatch * cg * sizeof(float2) +
+           kSpreadBatch * sizeof(int2);
+}
+
 inline size_t spread2d_smem_bytes(const Geom &g, int cg) {
     return (size_t)g.tile[0] * g.tile[1] * cg * sizeof(float2) + kSpreadBatch * 32 * sizeof(float) +
-           (size_t)kSpreadBatch * cg * sizeof(float2) + kSpreadBatch * sizeof(int2);
+           (size_t)kSpreadBatch * cg * sizeof(float2) + kSpreadBatch * sizeof(int2) +
+           kSpreadBatch * 16 * sizeof(int);
 }
 
 inline size_t interp2d_smem_bytes(const Geom &g, int cg) {

@@ -32,6 +32,21 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
     const size_t smem = spread_smem_bytes(a.g, coil_group);
     const dim3 grid((unsigned)n_sub, (unsigned)((a.g.n_coil + coil_group - 1) / coil_group));
     cudaError_t err = cudaSuccess;
+    // register-tile kernel: 4 or 8 coils per block and the tile it is built for
+    if (use_2d_path(a.g) && (coil_group == 4 || coil_group == 8) && threads <= 256 &&
+        a.g.tile[0] == kRegRows * (threads / 32) &&
+        a.g.tile[1] == kRegCols * (32 / coil_group)) {
+        const size_t rsmem = spread2d_reg_smem_bytes(coil_group);
+        GBN_DISPATCH_W(a.g.W, {
+            if (coil_group == 8) {
+                k_spread2d_reg<WT, 8><<<grid, threads, rsmem, s>>>(a);
+            } else {
+                k_spread2d_reg<WT, 4><<<grid, threads, rsmem, s>>>(a);
+            }
+            err = cudaGetLastError();
+        });
+        return err;
+    }
     if (use_2d_path(a.g)) {
         GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
             auto kern = k_spread2d<WT, CG>;
