@@ -478,18 +478,25 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     // (4 rows x warps) x (4 columns x 32/coils) cells, unless the caller chose a tile.
     // Measured on GB300 (8 coils, 512^2 radial): 128-thread blocks, 128-sample work items.
     bool reg_spread = false;
-    if (p->dim == 2 && desc->spread_tile[0] <= 0 && desc->spread_tile[1] <= 0) {
-        const int cg_eff = std::min(p->coil_group, pow2_floor(std::max(1, (int)desc->n_coil)));
-        if (cg_eff >= 4) {
-            if (desc->threads <= 0) p->threads = 128;
-            if (p->threads <= 256) {
-                ts[0] = 4 * (p->threads / 32);
-                ts[1] = 4 * (32 / cg_eff);
-                reg_spread = true;
-            }
+    const int cg_eff = std::min(p->coil_group, pow2_floor(std::max(1, (int)desc->n_coil)));
+    if (p->dim == 2 && desc->spread_tile[0] <= 0 && desc->spread_tile[1] <= 0 && cg_eff >= 4) {
+        if (desc->threads <= 0) p->threads = 128;
+        if (p->threads <= 256) {
+            ts[0] = 4 * (p->threads / 32);
+            ts[1] = 4 * (32 / cg_eff);
+            reg_spread = true;
         }
     }
-    p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem : (reg_spread ? 128 : 256);
+    // 3-D likewise: (x, y) rows of 4 per warp, tile (TX, TY, 4 x 32/coils) with TX*TY = 4 x warps
+    if (p->dim == 3 && desc->spread_tile[0] <= 0 && desc->spread_tile[1] <= 0 && desc->spread_tile[2] <= 0 &&
+        cg_eff >= 4 && p->threads <= 256) {
+        const int rows = 4 * (p->threads / 32);
+        ts[1] = rows >= 32 ? 8 : 4;
+        ts[0] = rows / ts[1];
+        ts[2] = 4 * (32 / cg_eff);
+        reg_spread = true;
+    }
+    p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem : (reg_spread && p->dim == 2 ? 128 : 256);
     make_geom(p, ts, p->gs);
     make_geom(p, ti, p->gi);
 

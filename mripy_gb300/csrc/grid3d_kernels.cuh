@@ -261,6 +261,139 @@ __global__ void __launch_bounds__(256) k_spread3d(SpreadArgs a) {
     }
 }
 
+// ------------------------------------------------------------------ spread, register tile
+// For 4 or 8 coils per block: warp w owns the 4 (x, y) rows  rho = 4w .. 4w+3  of the tile
+// (TY a multiple of 4, so they share x and have consecutive y) and lane (c, q) holds z
+// cells q, q + NQ, q + 2NQ, q + 3NQ of coil c in registers: tile (4*warps/TY) x TY x 4*NQ.
+// Per staged sample a warp whose x the stencil reaches folds the z weights into the coil
+// value (4 complex values per lane), then needs one broadcast load and 4 packed FMAs per
+// row; no shared-memory read-modify-write.
+template <int WT, int CG>
+__global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
+    constexpr int NQ = 32 / CG;
+    extern __shared__ float4 smem_r3[];
+    const Geom &g = a.g;
+    float *st_w = reinterpret_cast<float *>(smem_r3);                        // [batch][48]: wx, wy, wz
+    float2 *st_v = reinterpret_cast<float2 *>(st_w + kSpread3dBatch * 48);   // [batch][CG]
+    int4 *st_r = reinterpret_cast<int4 *>(st_v + kSpread3dBatch * CG);       // [batch]: signed first taps
+
+    const int4 sub = a.subs[blockIdx.x];
+    const int cg0 = blockIdx.y * CG;
+    const int grp = sub.x / g.ntiles;
+    int o[3], e[3];
+    tile_coords<3>(g, sub.x % g.ntiles, o, e);
+    const int TY = g.tile[1];
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const int rho0 = warp * kRegRows;
+    const int xw = rho0 / TY, y0 = rho0 - xw * TY;
+    float2 acc[kRegRows][kRegCols];
+#pragma unroll
+    for (int r = 0; r < kRegRows; ++r)
+#pragma unroll
+        for (int k = 0; k < kRegCols; ++k) acc[r][k] = make_float2(0.f, 0.f);
+
+    for (int base = 0; base < sub.z; base += kSpread3dBatch) {
+        const int n = min(kSpread3dBatch, sub.z - base);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n * 48; i += blockDim.x) {
+            const int s = i / 48, k = i - s * 48, d = k >> 4, kq = k & 15;
+            const float4 p = a.pts[(int64_t)sub.y + base + s];
+            float val = 0.f;
+            if (kq < W) {
+                const float f = d == 0 ? p.x : (d == 1 ? p.y : p.z);
+                const float dd = f + (float)(ns - 1 - kq);
+                val = exp2f(-g.beta2[d] * dd * dd);
+            }
+            st_w[i] = val;
+            if (k == 0) {
+                int c0[3];
+                unpack_cells(3, __float_as_uint(p.w), c0[0], c0[1], c0[2]);
+                int r[3];
+#pragma unroll
+                for (int dd = 0; dd < 3; ++dd) {
+                    int rr = c0[dd] - o[dd];
+                    rr += rr < 0 ? g.nf[dd] : 0;
+                    rr -= rr > g.nf[dd] - W ? g.nf[dd] : 0;
+                    r[dd] = rr;
+                }
+                st_r[s] = make_int4(r[0], r[1], r[2], 0);
+            }
+        }
+        for (int i = threadIdx.x; i < n * CG; i += blockDim.x) {
+            const int s = i / CG, cc = i - s * CG;
+            const uint32_t j = a.idx[(int64_t)sub.y + base + s];
+            float2 v = make_float2(0.f, 0.f);
+            if (cg0 + cc < g.n_coil) {
+                v = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
+                if (a.weight) {
+                    const float sw = a.weight[j];
+                    v.x *= sw;
+                    v.y *= sw;
+                }
+            }
+            st_v[i] = v;
+        }
+        __syncthreads();
+
+        for (int s = 0; s < n; ++s) {
+            const int4 r = st_r[s];
+            const int kx = xw - r.x;
+            if ((unsigned)kx >= (unsigned)W) continue;                     // warp-uniform
+            if (y0 + kRegRows <= r.y || y0 >= r.y + W) continue;          // warp-uniform
+            const float *w = st_w + s * 48;
+            const float2 v = st_v[s * CG + c];
+            const float wx = w[kx];
+            float2 wzv[kRegCols];
+#pragma unroll
+            for (int k = 0; k < kRegCols; ++k) {
+                const int kz = q + k * NQ - r.z;
+                const float wz = (unsigned)kz < (unsigned)W ? wx * w[32 + (kz & 15)] : 0.f;
+                wzv[k] = make_float2(wz * v.x, wz * v.y);
+            }
+#pragma unroll
+            for (int rr = 0; rr < kRegRows; ++rr) {
+                const int ky = y0 + rr - r.y;
+                if ((unsigned)ky < (unsigned)W) {
+                    const float wy = w[16 + ky];
+                    const float2 wy2 = make_float2(wy, wy);
+#pragma unroll
+                    for (int k = 0; k < kRegCols; ++k) acc[rr][k] = __ffma2_rn(wy2, wzv[k], acc[rr][k]);
+                }
+            }
+        }
+    }
+
+    if (cg0 + c >= g.n_coil || xw >= e[0]) return;
+    const bool split = (sub.w & kSplitFlag) != 0;
+    float2 *dstc = a.grid + ((int64_t)grp * g.n_coil + cg0 + c) * g.G;
+#pragma unroll
+    for (int rr = 0; rr < kRegRows; ++rr) {
+        const int ly = y0 + rr;
+        if (ly >= e[1]) break;
+#pragma unroll
+        for (int k = 0; k < kRegCols; ++k) {
+            const int lz = q + k * NQ;
+            if (lz >= e[2]) continue;
+            float2 *dst = dstc + ((int64_t)(o[0] + xw) * g.nf[1] + (o[1] + ly)) * g.nf[2] + (o[2] + lz);
+            if (split) {
+                atomicAdd(&dst->x, acc[rr][k].x);
+                atomicAdd(&dst->y, acc[rr][k].y);
+            } else {
+                *dst = acc[rr][k];
+            }
+        }
+    }
+}
+
+inline size_t spread3d_reg_smem_bytes(int cg) {
+    return kSpread3dBatch * 48 * sizeof(float) + (size_t)kSpread3dBatch * cg * sizeof(float2) +
+           kSpread3dBatch * sizeof(int4);
+}
+
 inline size_t spread3d_smem_bytes(const Geom &g, int cg) {
     return (size_t)g.tile[0] * g.tile[1] * g.tile[2] * cg * sizeof(float2) + kSpread3dBatch * 48 * sizeof(float) +
            (size_t)kSpread3dBatch * cg * sizeof(float2) + kSpread3dBatch * sizeof(int4);

@@ -1,7 +1,9 @@
 // Spread (type-1 gridding) launchers.
 //
-// 2-D with at most 16 taps per dimension: k_spread2d (warp-owned rows, no atomics).
-// Otherwise (1-D, 3-D, wide stencils): k_spread (shared-memory atomics).
+// 2-D / 3-D with at most 16 taps per dimension and 4 or 8 coils per block, on the tile shape
+// they are built for: k_spread2d_reg / k_spread3d_reg (accumulators in registers).
+// Other 2-D / 3-D tiles: k_spread2d / k_spread3d (warp-owned shared-memory rows, no atomics).
+// Otherwise (1-D, wide stencils, small grids): k_spread (shared-memory atomics).
 #include "dispatch.cuh"
 #include "grid2d_kernels.cuh"
 #include "grid3d_kernels.cuh"
@@ -56,6 +58,21 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
                 err = cudaGetLastError();
             }
         }));
+        return err;
+    }
+    // 3-D register-tile kernel: (x, y) rows of 4 per warp, z run of 4 * 32/coils cells
+    if (grid3d_applies(a.g) && (coil_group == 4 || coil_group == 8) && threads <= 256 &&
+        a.g.tile[1] % kRegRows == 0 && a.g.tile[0] * a.g.tile[1] == kRegRows * (threads / 32) &&
+        a.g.tile[2] == kRegCols * (32 / coil_group)) {
+        const size_t rsmem = spread3d_reg_smem_bytes(coil_group);
+        GBN_DISPATCH_W(a.g.W, {
+            if (coil_group == 8) {
+                k_spread3d_reg<WT, 8><<<grid, threads, rsmem, s>>>(a);
+            } else {
+                k_spread3d_reg<WT, 4><<<grid, threads, rsmem, s>>>(a);
+            }
+            err = cudaGetLastError();
+        });
         return err;
     }
     if (grid3d_applies(a.g)) {

@@ -17,7 +17,7 @@ from mripy_gb300 import nufft_func as nf
 from mripy_gb300 import operators as ops
 from mripy_gb300 import synth
 from mripy_gb300._native import GbnError
-from mripy_gb300.plan import NufftPlan
+from mripy_gb300.plan import NufftPlan, Tuning
 
 pytestmark = pytest.mark.gpu
 
@@ -252,7 +252,68 @@ def test_3d_warp_kernels_against_oracle(eps):
                O.nufft_type21(tuple(xs), F, shape, dcf=dcf, eps=eps)) < TOL_REF
 
 
+@pytest.mark.parametrize("nc,tuning", [
+    (11, None),                                   # register tile 4x8x16, coil groups of 8 and 3
+    (8, Tuning(threads=128)),                     # register tile 4x4x16
+    (4, None),                                    # register tile 4x8x32, 4 coils per block
+    (8, Tuning(spread_tile=(8, 8, 32))),          # shared-memory tile kernel
+    (8, Tuning(max_subproblem=64)),               # many split tiles (global-atomic flush)
+])
+def test_3d_spread_tiles_weights_against_oracle(nc, tuning):
+    rng = np.random.default_rng(22)
+    M, shape = 6000, (26, 24, 28)
+    xs = rng.uniform(-np.pi, np.pi, (3, M))
+    xs[:, :2500] *= 0.08                                         # dense centre
+    xs[:, 2500:2600] = np.pi                                     # stencils across the periodic edge
+    p = NufftPlan(3, shape, n_coil=nc, eps=5e-6, tuning=tuning).set_points([cuda(v) for v in xs])
+    c = cvec(rng, (M, nc))
+    w = rng.uniform(0.5, 1.5, M)
+    F = p.type1(cuda(c), weight=cuda(w.astype(np.float32)))
+    Fo = O.nufft_type1(tuple(xs), (c * w[:, None]).astype(np.complex128), shape, eps=5e-6)
+    assert rel(F[0], Fo) < TOL_REF
+
+
 # ------------------------------------------------------------------ SENSE fusion and graphs
+@pytest.mark.parametrize("dim,shape,nc,eps", [
+    (1, (5001,), 3, 5e-6),        # rows longer than one staged segment, coil chunks of 1
+    (2, (15, 13), 3, 1e-12),      # ratio 3: odd oversampled grid 45 x 39
+    (2, (1100, 1030), 2, 1e-5),   # SENSE crop: two segments per row (tau follows ms only,
+                                  # so ms must be the largest size or exp(tau k^2) overflows)
+    (3, (9, 7, 11), 5, 1e-12),    # odd 3-D, ratio 3
+    (3, (12, 10, 8), 20, 1e-5),   # coil chunks in 3-D
+])
+def test_pad_crop_shapes_layouts_groups(dim, shape, nc, eps):
+    rng = np.random.default_rng(23)
+    counts = [700, 300]
+    off = np.concatenate([[0], np.cumsum(counts)])
+    M = int(off[-1])
+    xs = rng.uniform(-np.pi, np.pi, (dim, M))
+    # 3-D: nspread clamped to 6 as nufft3d*_gaussker does (the oracle's 3-D parameters)
+    p = NufftPlan(dim, shape, n_coil=nc, n_traj=2, eps=eps, max_nspread=6 if dim == 3 else None)
+    p.set_points([cuda(v) for v in xs], traj_offsets=off.tolist())
+    img = cvec(rng, (2,) + shape + (nc,))
+    c = cvec(rng, (M, nc))
+    k_last = p.type2(cuda(img))
+    img_major = cuda(np.ascontiguousarray(np.moveaxis(img, -1, 1)))          # (2, nc, *shape)
+    k_major = p.type2(img_major.movedim(1, -1))
+    assert rel(k_last, k_major) < 1e-6
+    F = p.type1(cuda(c))
+    F_major = torch.empty((2, nc) + shape, dtype=torch.complex64, device="cuda")
+    p.type1(cuda(c), out=F_major.movedim(1, -1))
+    assert rel(F, F_major.movedim(1, -1)) < 1e-6
+    for g_, (a, b) in enumerate(zip(off[:-1], off[1:])):
+        co = tuple(v[a:b] for v in xs)
+        assert rel(k_last[a:b], O.nufft_type2(co, img[g_].astype(np.complex128), shape, eps=eps)) < TOL_REF
+        assert rel(F[g_], O.nufft_type1(co, c[a:b].astype(np.complex128), shape, eps=eps)) < TOL_REF
+    # SENSE-fused pad / crop on the same shapes against the per-coil composition
+    S = cuda(cvec(rng, shape + (nc,)))
+    x = cuda(cvec(rng, (2,) + shape))
+    ks = p.sense_forward(x, S)
+    assert rel(ks, p.type2((x[..., None] * S[None]).contiguous())) < 1e-6
+    xa = p.sense_adjoint(ks, S)
+    assert rel(xa, (p.type1(ks) * S.conj()[None]).sum(-1)) < 1e-5
+
+
 def test_sense_fused_kernels_match_composition():
     rng = np.random.default_rng(17)
     shape, nc, M = (64, 48), 4, 12000
