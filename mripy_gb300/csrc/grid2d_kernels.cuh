@@ -269,27 +269,42 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
 // ------------------------------------------------------------------ spread, register tile
 // For 4 or 8 coils per block the output tile lives in registers: warp w owns the rows
 // [4w, 4w + 4) and lane (c, q) holds columns q, q + NQ, q + 2NQ, q + 3NQ of coil c, so the
-// tile is (4 * warps) x (4 * NQ) cells.  Per staged sample a warp whose rows the stencil
-// reaches folds the column weights into the coil value once (4 complex values per lane)
-// and then needs one broadcast load and 4 packed FMAs per row; there is no shared-memory
-// read-modify-write at all.  Columns outside the stencil carry a zero weight.
-constexpr int kRegRows = 4;  // rows per warp
-constexpr int kRegCols = 4;  // columns per lane
+// tile is (4 * warps) x (4 * NQ) cells.  There is no shared-memory read-modify-write.
+//
+// Samples are staged in double-buffered batches of 32 (one barrier per batch).  Warp 0
+// stages the x weight of every tile row for each sample (0 outside the stencil) and builds,
+// with ballots, the ordered list of samples whose stencil reaches each warp's rows; warp 1
+// stages the y weight of every tile column, stored [q][k] for column q + k*NQ so a lane
+// reads its 4 columns with one 16-byte load; the other warps gather the coil values.  A
+// warp then walks only its own list: per sample one load of its 4 row weights, one of its
+// 4 column weights, the coil value, 8 multiplies and 16 packed FMAs.  The summation order
+// is the sample order, fixed for a given trajectory.
+constexpr int kRegRows = 4;    // rows per warp
+constexpr int kRegCols = 4;    // columns per lane
+constexpr int kRegBatch = 32;  // samples per staged batch
+constexpr int kRegPad = 4;     // stride padding of the staged weight rows (bank spread, 16-byte aligned)
+
+__device__ __forceinline__ unsigned lanemask_lt(int lane) { return (1u << lane) - 1u; }
 
 template <int WT, int CG>
 __global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
     constexpr int NQ = 32 / CG;
+    constexpr int B = kRegBatch;
     extern __shared__ float4 smem_r2[];
     const Geom &g = a.g;
-    float *st_w = reinterpret_cast<float *>(smem_r2);                     // [batch][32]: wx[16], wy[16]
-    float2 *st_v = reinterpret_cast<float2 *>(st_w + kSpreadBatch * 32);  // [batch][CG]
-    int2 *st_r = reinterpret_cast<int2 *>(st_v + kSpreadBatch * CG);      // [batch]: signed first taps
+    const int TX = g.tile[0], TY = g.tile[1];  // TX = 4 * warps, TY = 4 * NQ (set by the host)
+    const int TXP = TX + kRegPad, TYP = TY + kRegPad;
+    const int nw = blockDim.x >> 5;
+    float *st_wr = reinterpret_cast<float *>(smem_r2);                     // [2][B][TXP]
+    float *st_wc = st_wr + 2 * B * TXP;                                    // [2][B][TYP]: [q][k]
+    float2 *st_v = reinterpret_cast<float2 *>(st_wc + 2 * B * TYP);        // [2][B][CG]
+    int *st_cnt = reinterpret_cast<int *>(st_v + 2 * B * CG);              // [2][8]
+    uint8_t *st_list = reinterpret_cast<uint8_t *>(st_cnt + 16);           // [2][8][B]
 
     const int4 sub = a.subs[blockIdx.x];
     const int cg0 = blockIdx.y * CG;
     const int grp = sub.x / g.ntiles;
     const int tile = sub.x % g.ntiles;
-    const int TX = g.tile[0], TY = g.tile[1];  // TX = 4 * warps, TY = 4 * NQ (set by the host)
     const int o0 = (tile / g.ntile[1]) * TX;
     const int o1 = (tile % g.ntile[1]) * TY;
     const int nf0 = g.nf[0], nf1 = g.nf[1];
@@ -306,67 +321,89 @@ __global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
 #pragma unroll
         for (int k = 0; k < kRegCols; ++k) acc[r][k] = make_float2(0.f, 0.f);
 
-    for (int base = 0; base < sub.z; base += kSpreadBatch) {
-        const int n = min(kSpreadBatch, sub.z - base);
-        __syncthreads();  // previous batch consumed
-        for (int i = threadIdx.x; i < n * 32; i += blockDim.x) {
-            const int s = i >> 5, k = i & 31, kq = k & 15;
-            const float4 p = a.pts[(int64_t)sub.y + base + s];
-            float val = 0.f;
-            if (kq < W) {
-                const float d = (k < 16 ? p.x : p.y) + (float)(ns - 1 - kq);
-                val = exp2f(-(k < 16 ? g.beta2[0] : g.beta2[1]) * d * d);
-            }
-            st_w[i] = val;
-            if (k == 0) {
+    for (int base = 0, buf = 0; base < sub.z; base += B, buf ^= 1) {
+        const int n = min(B, sub.z - base);
+        if (warp < 2) {
+            // warp 0: row weights and the per-warp lists; warp 1: column weights
+            const bool ok = lane < n;
+            int rx = 0, ry = 0;
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (ok) {
+                p = a.pts[(int64_t)sub.y + base + lane];
                 // signed local first-tap cell, in (-W, nf - W] (nf >= tile + W on this path)
                 int c0x, c0y, c0z;
                 unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
-                int rx = c0x - o0, ry = c0y - o1;
+                rx = c0x - o0;
+                ry = c0y - o1;
                 rx += rx < 0 ? nf0 : 0;
                 ry += ry < 0 ? nf1 : 0;
                 rx -= rx > nf0 - W ? nf0 : 0;
                 ry -= ry > nf1 - W ? nf1 : 0;
-                st_r[s] = make_int2(rx, ry);
             }
-        }
-        for (int i = threadIdx.x; i < n * CG; i += blockDim.x) {
-            const int s = i / CG, cc = i - s * CG;
-            const uint32_t j = a.idx[(int64_t)sub.y + base + s];
-            float2 v = make_float2(0.f, 0.f);
-            if (cg0 + cc < g.n_coil) {
-                v = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
-                if (a.weight) {
-                    const float sw = a.weight[j];
-                    v.x *= sw;
-                    v.y *= sw;
+            if (warp == 0) {
+                float *dst = st_wr + (buf * B + lane) * TXP;
+                for (int row = 0; row < TX; ++row) {
+                    const int tap = row - rx;
+                    float val = 0.f;
+                    if (ok && (unsigned)tap < (unsigned)W) {
+                        const float d = p.x + (float)(ns - 1 - tap);
+                        val = exp2f(-g.beta2[0] * d * d);
+                    }
+                    dst[row] = val;
+                }
+                for (int w = 0; w < nw; ++w) {
+                    const bool hit = ok && rx < w * kRegRows + kRegRows && rx + W > w * kRegRows;
+                    const unsigned m = __ballot_sync(0xffffffffu, hit);
+                    if (hit) st_list[(buf * 8 + w) * B + __popc(m & lanemask_lt(lane))] = (uint8_t)lane;
+                    if (lane == 0) st_cnt[buf * 8 + w] = __popc(m);
+                }
+            } else {
+                float *dst = st_wc + (buf * B + lane) * TYP;
+                for (int col = 0; col < TY; ++col) {
+                    const int tap = col - ry;
+                    float val = 0.f;
+                    if (ok && (unsigned)tap < (unsigned)W) {
+                        const float d = p.y + (float)(ns - 1 - tap);
+                        val = exp2f(-g.beta2[1] * d * d);
+                    }
+                    dst[(col % NQ) * 4 + col / NQ] = val;
                 }
             }
-            st_v[i] = v;
+        } else {
+            for (int i = threadIdx.x - 64; i < n * CG; i += blockDim.x - 64) {
+                const int s = i / CG, cc = i - s * CG;
+                const uint32_t j = a.idx[(int64_t)sub.y + base + s];
+                float2 v = make_float2(0.f, 0.f);
+                if (cg0 + cc < g.n_coil) {
+                    v = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
+                    if (a.weight) {
+                        const float sw = a.weight[j];
+                        v.x *= sw;
+                        v.y *= sw;
+                    }
+                }
+                st_v[buf * B * CG + i] = v;
+            }
         }
+        // the other buffer was last read before this barrier's previous instance, so one
+        // barrier per batch suffices
         __syncthreads();
 
-        for (int s = 0; s < n; ++s) {
-            const int2 r = st_r[s];
-            if (r.x + W <= row0 || r.x >= row0 + kRegRows) continue;  // warp-uniform
-            const float *w = st_w + s * 32;
+        const int cnt = st_cnt[buf * 8 + warp];
+        const uint8_t *lst = st_list + (buf * 8 + warp) * B;
+        for (int i = 0; i < cnt; ++i) {
+            const int s = buf * B + lst[i];
+            const float4 wc = *reinterpret_cast<const float4 *>(st_wc + s * TYP + q * 4);
+            const float4 wr = *reinterpret_cast<const float4 *>(st_wr + s * TXP + row0);
             const float2 v = st_v[s * CG + c];
-            float2 wyv[kRegCols];
-#pragma unroll
-            for (int k = 0; k < kRegCols; ++k) {
-                const int ky = q + k * NQ - r.y;
-                const float wy = (unsigned)ky < (unsigned)W ? w[16 + (ky & 15)] : 0.f;
-                wyv[k] = make_float2(wy * v.x, wy * v.y);
-            }
+            const float2 u[kRegCols] = {make_float2(wc.x * v.x, wc.x * v.y), make_float2(wc.y * v.x, wc.y * v.y),
+                                        make_float2(wc.z * v.x, wc.z * v.y), make_float2(wc.w * v.x, wc.w * v.y)};
+            const float wrr[kRegRows] = {wr.x, wr.y, wr.z, wr.w};
 #pragma unroll
             for (int rr = 0; rr < kRegRows; ++rr) {
-                const int kx = row0 + rr - r.x;
-                if ((unsigned)kx < (unsigned)W) {
-                    const float wx = w[kx];
-                    const float2 wx2 = make_float2(wx, wx);
+                const float2 wx2 = make_float2(wrr[rr], wrr[rr]);
 #pragma unroll
-                    for (int k = 0; k < kRegCols; ++k) acc[rr][k] = __ffma2_rn(wx2, wyv[k], acc[rr][k]);
-                }
+                for (int k = 0; k < kRegCols; ++k) acc[rr][k] = __ffma2_rn(wx2, u[k], acc[rr][k]);
             }
         }
     }
@@ -394,9 +431,10 @@ __global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
     }
 }
 
-inline size_t spread2d_reg_smem_bytes(int cg) {
-    return kSpreadBatch * 32 * sizeof(float) + (size_t)kSpreadBatch * cg * sizeof(float2) +
-           kSpreadBatch * sizeof(int2);
+inline size_t spread2d_reg_smem_bytes(const Geom &g, int cg) {
+    return 2 * ((size_t)kRegBatch * (g.tile[0] + g.tile[1] + 2 * kRegPad) * sizeof(float) +
+                (size_t)kRegBatch * cg * sizeof(float2)) +
+           16 * sizeof(int) + 2 * 8 * kRegBatch;
 }
 
 inline size_t spread2d_smem_bytes(const Geom &g, int cg) {

@@ -265,24 +265,36 @@ __global__ void __launch_bounds__(256) k_spread3d(SpreadArgs a) {
 // For 4 or 8 coils per block: warp w owns the 4 (x, y) rows  rho = 4w .. 4w+3  of the tile
 // (TY a multiple of 4, so they share x and have consecutive y) and lane (c, q) holds z
 // cells q, q + NQ, q + 2NQ, q + 3NQ of coil c in registers: tile (4*warps/TY) x TY x 4*NQ.
-// Per staged sample a warp whose x the stencil reaches folds the z weights into the coil
-// value (4 complex values per lane), then needs one broadcast load and 4 packed FMAs per
-// row; no shared-memory read-modify-write.
+// No shared-memory read-modify-write.
+//
+// Staging as in k_spread2d_reg (double-buffered batches of 32, one barrier per batch):
+// warp 0 stages the weight of every tile x plane and builds the ordered per-warp sample
+// lists (the stencil reaches the warp's x plane and one of its 4 y rows), warp 1 the
+// weight of every y row, warp 2 of every z column ([q][k] for column q + k*NQ), the other
+// warps gather the coil values.  Per listed sample a warp loads its plane weight, its 4
+// row weights and its 4 column weights, folds the plane and column weights into the coil
+// value (10 multiplies) and issues 16 packed FMAs.
 template <int WT, int CG>
 __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
     constexpr int NQ = 32 / CG;
+    constexpr int B = kRegBatch;
     extern __shared__ float4 smem_r3[];
     const Geom &g = a.g;
-    float *st_w = reinterpret_cast<float *>(smem_r3);                        // [batch][48]: wx, wy, wz
-    float2 *st_v = reinterpret_cast<float2 *>(st_w + kSpread3dBatch * 48);   // [batch][CG]
-    int4 *st_r = reinterpret_cast<int4 *>(st_v + kSpread3dBatch * CG);       // [batch]: signed first taps
+    const int TX = g.tile[0], TY = g.tile[1], TZ = g.tile[2];
+    // per staged sample: y rows [0, TY), z columns [TY, TY + TZ) as [q][k], x planes after
+    // them; the stride is padded to a multiple of 4 (16-byte loads) plus a bank offset
+    const int TWP = ((TX + TY + TZ + 3) & ~3) + kRegPad;
+    const int nw = blockDim.x >> 5;
+    float *st_w = reinterpret_cast<float *>(smem_r3);                  // [2][B][TWP]
+    float2 *st_v = reinterpret_cast<float2 *>(st_w + 2 * B * TWP);     // [2][B][CG]
+    int *st_cnt = reinterpret_cast<int *>(st_v + 2 * B * CG);          // [2][8]
+    uint8_t *st_list = reinterpret_cast<uint8_t *>(st_cnt + 16);       // [2][8][B]
 
     const int4 sub = a.subs[blockIdx.x];
     const int cg0 = blockIdx.y * CG;
     const int grp = sub.x / g.ntiles;
     int o[3], e[3];
     tile_coords<3>(g, sub.x % g.ntiles, o, e);
-    const int TY = g.tile[1];
     const int W = WT ? WT : g.W;
     const int ns = g.ns;
 
@@ -296,73 +308,87 @@ __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
 #pragma unroll
         for (int k = 0; k < kRegCols; ++k) acc[r][k] = make_float2(0.f, 0.f);
 
-    for (int base = 0; base < sub.z; base += kSpread3dBatch) {
-        const int n = min(kSpread3dBatch, sub.z - base);
-        __syncthreads();
-        for (int i = threadIdx.x; i < n * 48; i += blockDim.x) {
-            const int s = i / 48, k = i - s * 48, d = k >> 4, kq = k & 15;
-            const float4 p = a.pts[(int64_t)sub.y + base + s];
-            float val = 0.f;
-            if (kq < W) {
-                const float f = d == 0 ? p.x : (d == 1 ? p.y : p.z);
-                const float dd = f + (float)(ns - 1 - kq);
-                val = exp2f(-g.beta2[d] * dd * dd);
-            }
-            st_w[i] = val;
-            if (k == 0) {
+    for (int base = 0, buf = 0; base < sub.z; base += B, buf ^= 1) {
+        const int n = min(B, sub.z - base);
+        if (warp < 3) {
+            const bool ok = lane < n;
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+            int r[3] = {0, 0, 0};
+            if (ok) {
+                p = a.pts[(int64_t)sub.y + base + lane];
                 int c0[3];
                 unpack_cells(3, __float_as_uint(p.w), c0[0], c0[1], c0[2]);
-                int r[3];
 #pragma unroll
-                for (int dd = 0; dd < 3; ++dd) {
-                    int rr = c0[dd] - o[dd];
-                    rr += rr < 0 ? g.nf[dd] : 0;
-                    rr -= rr > g.nf[dd] - W ? g.nf[dd] : 0;
-                    r[dd] = rr;
-                }
-                st_r[s] = make_int4(r[0], r[1], r[2], 0);
-            }
-        }
-        for (int i = threadIdx.x; i < n * CG; i += blockDim.x) {
-            const int s = i / CG, cc = i - s * CG;
-            const uint32_t j = a.idx[(int64_t)sub.y + base + s];
-            float2 v = make_float2(0.f, 0.f);
-            if (cg0 + cc < g.n_coil) {
-                v = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
-                if (a.weight) {
-                    const float sw = a.weight[j];
-                    v.x *= sw;
-                    v.y *= sw;
+                for (int d = 0; d < 3; ++d) {
+                    int rr = c0[d] - o[d];
+                    rr += rr < 0 ? g.nf[d] : 0;
+                    rr -= rr > g.nf[d] - W ? g.nf[d] : 0;
+                    r[d] = rr;
                 }
             }
-            st_v[i] = v;
+            // warp 0: x planes (+ lists), warp 1: y rows, warp 2: z columns
+            const int d = warp == 0 ? 0 : (warp == 1 ? 1 : 2);
+            const int len = d == 0 ? TX : (d == 1 ? TY : TZ);
+            const int rd = d == 0 ? r[0] : (d == 1 ? r[1] : r[2]);
+            const float f = d == 0 ? p.x : (d == 1 ? p.y : p.z);
+            const float bd = d == 0 ? g.beta2[0] : (d == 1 ? g.beta2[1] : g.beta2[2]);
+            float *dst = st_w + (buf * B + lane) * TWP;
+            for (int k = 0; k < len; ++k) {
+                const int tap = k - rd;
+                float val = 0.f;
+                if (ok && (unsigned)tap < (unsigned)W) {
+                    const float dd = f + (float)(ns - 1 - tap);
+                    val = exp2f(-bd * dd * dd);
+                }
+                const int slot = d == 0 ? TY + TZ + k : (d == 1 ? k : TY + (k % NQ) * 4 + k / NQ);
+                dst[slot] = val;
+            }
+            if (warp == 0) {
+                for (int w = 0; w < nw; ++w) {
+                    const int wx = (w * kRegRows) / TY, wy0 = w * kRegRows - wx * TY;
+                    const bool hit = ok && (unsigned)(wx - r[0]) < (unsigned)W && r[1] < wy0 + kRegRows &&
+                                     r[1] + W > wy0;
+                    const unsigned m = __ballot_sync(0xffffffffu, hit);
+                    if (hit) st_list[(buf * 8 + w) * B + __popc(m & lanemask_lt(lane))] = (uint8_t)lane;
+                    if (lane == 0) st_cnt[buf * 8 + w] = __popc(m);
+                }
+            }
+        } else {
+            for (int i = threadIdx.x - 96; i < n * CG; i += blockDim.x - 96) {
+                const int s = i / CG, cc = i - s * CG;
+                const uint32_t j = a.idx[(int64_t)sub.y + base + s];
+                float2 v = make_float2(0.f, 0.f);
+                if (cg0 + cc < g.n_coil) {
+                    v = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
+                    if (a.weight) {
+                        const float sw = a.weight[j];
+                        v.x *= sw;
+                        v.y *= sw;
+                    }
+                }
+                st_v[buf * B * CG + i] = v;
+            }
         }
-        __syncthreads();
+        __syncthreads();  // one barrier per batch: the other buffer is free (double buffering)
 
-        for (int s = 0; s < n; ++s) {
-            const int4 r = st_r[s];
-            const int kx = xw - r.x;
-            if ((unsigned)kx >= (unsigned)W) continue;                     // warp-uniform
-            if (y0 + kRegRows <= r.y || y0 >= r.y + W) continue;          // warp-uniform
-            const float *w = st_w + s * 48;
-            const float2 v = st_v[s * CG + c];
-            const float wx = w[kx];
-            float2 wzv[kRegCols];
-#pragma unroll
-            for (int k = 0; k < kRegCols; ++k) {
-                const int kz = q + k * NQ - r.z;
-                const float wz = (unsigned)kz < (unsigned)W ? wx * w[32 + (kz & 15)] : 0.f;
-                wzv[k] = make_float2(wz * v.x, wz * v.y);
-            }
+        const int cnt = st_cnt[buf * 8 + warp];
+        const uint8_t *lst = st_list + (buf * 8 + warp) * B;
+        for (int i = 0; i < cnt; ++i) {
+            const int s = buf * B + lst[i];
+            const float *w = st_w + s * TWP;
+            const float2 v0 = st_v[s * CG + c];
+            const float wx = w[TY + TZ + xw];
+            const float2 v = make_float2(wx * v0.x, wx * v0.y);
+            const float4 wz = *reinterpret_cast<const float4 *>(w + TY + q * 4);
+            const float4 wy = *reinterpret_cast<const float4 *>(w + y0);
+            const float2 u[kRegCols] = {make_float2(wz.x * v.x, wz.x * v.y), make_float2(wz.y * v.x, wz.y * v.y),
+                                        make_float2(wz.z * v.x, wz.z * v.y), make_float2(wz.w * v.x, wz.w * v.y)};
+            const float wyr[kRegRows] = {wy.x, wy.y, wy.z, wy.w};
 #pragma unroll
             for (int rr = 0; rr < kRegRows; ++rr) {
-                const int ky = y0 + rr - r.y;
-                if ((unsigned)ky < (unsigned)W) {
-                    const float wy = w[16 + ky];
-                    const float2 wy2 = make_float2(wy, wy);
+                const float2 wy2 = make_float2(wyr[rr], wyr[rr]);
 #pragma unroll
-                    for (int k = 0; k < kRegCols; ++k) acc[rr][k] = __ffma2_rn(wy2, wzv[k], acc[rr][k]);
-                }
+                for (int k = 0; k < kRegCols; ++k) acc[rr][k] = __ffma2_rn(wy2, u[k], acc[rr][k]);
             }
         }
     }
@@ -389,9 +415,10 @@ __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
     }
 }
 
-inline size_t spread3d_reg_smem_bytes(int cg) {
-    return kSpread3dBatch * 48 * sizeof(float) + (size_t)kSpread3dBatch * cg * sizeof(float2) +
-           kSpread3dBatch * sizeof(int4);
+inline size_t spread3d_reg_smem_bytes(const Geom &g, int cg) {
+    const int twp = ((g.tile[0] + g.tile[1] + g.tile[2] + 3) & ~3) + kRegPad;
+    return 2 * ((size_t)kRegBatch * twp * sizeof(float) + (size_t)kRegBatch * cg * sizeof(float2)) +
+           16 * sizeof(int) + 2 * 8 * kRegBatch;
 }
 
 inline size_t spread3d_smem_bytes(const Geom &g, int cg) {
