@@ -67,9 +67,11 @@ typedef struct {
     int32_t spread_tile[3]; /* output tile of the spread kernel, cells per dim */
     int32_t interp_tile[3]; /* home bin of the interp kernel, cells per dim */
     int32_t max_subproblem; /* samples per thread block before a bin is split */
-    int32_t coil_group;     /* coils per thread block: 1, 2, 4 or 8 */
+    int32_t coil_group;     /* coils per spread thread block: 1, 2, 4 or 8 */
     int32_t threads;        /* threads per spread block: 128, 256 or 512 */
     int32_t interp_threads; /* threads per interp block: 128, 256 or 512 */
+    int32_t interp_coil_group; /* coils per interp thread block: 1, 2, 4 or 8 (0: the
+                                  group that pads the coil count least) */
 } gbn_plan_desc;
 
 typedef struct {
@@ -89,6 +91,7 @@ typedef struct {
     int32_t interp_threads;
     int32_t max_subproblem;
     int64_t device_bytes;   /* device memory held by the plan */
+    int32_t interp_coil_group;
 } gbn_plan_info;
 
 /* element strides (in complex64 elements) of a strided complex array */

@@ -39,7 +39,7 @@ class PlanDesc(ctypes.Structure):
         ("df", ctypes.c_double), ("n_coil", ctypes.c_int32), ("n_traj", ctypes.c_int32),
         ("spread_tile", ctypes.c_int32 * 3), ("interp_tile", ctypes.c_int32 * 3),
         ("max_subproblem", ctypes.c_int32), ("coil_group", ctypes.c_int32), ("threads", ctypes.c_int32),
-        ("interp_threads", ctypes.c_int32),
+        ("interp_threads", ctypes.c_int32), ("interp_coil_group", ctypes.c_int32),
     ]
 
 
@@ -51,6 +51,7 @@ class PlanInfo(ctypes.Structure):
         ("spread_entries", ctypes.c_int64), ("spread_tile", ctypes.c_int32 * 3),
         ("interp_tile", ctypes.c_int32 * 3), ("coil_group", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("interp_threads", ctypes.c_int32), ("max_subproblem", ctypes.c_int32), ("device_bytes", ctypes.c_int64),
+        ("interp_coil_group", ctypes.c_int32),
     ]
 
 

@@ -78,7 +78,7 @@ struct gbn_plan {
     int nf[3] = {1, 1, 1};
     double tau = 0;
     Geom gs{}, gi{};
-    int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256;
+    int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256, interp_coil_group = 0;
     int64_t G = 1, n_inst = 1;
     size_t device_bytes = 0;
     int smem_optin = 0;
@@ -235,8 +235,22 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
     return GBN_OK;
 }
 
+// Interp coils per block: the caller's choice, else the group size that pads the coil
+// count least (every padded lane still reads the window), counting 2 lanes of fixed cost
+// per block: 12 coils -> 3 groups of 4, 8 -> 1 of 8, 5 -> 1 of 8, 3 -> 1 of 4.
 int interp_cg(const gbn_plan *p) {
-    int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
+    const int n = std::max(1, (int)p->desc.n_coil);
+    int cg = p->interp_coil_group;
+    if (cg <= 0) {
+        int best = 1 << 30;
+        for (int cand : {8, 4, 2, 1}) {
+            const int cost = ((n + cand - 1) / cand) * (cand + 2);
+            if (cost < best) {
+                best = cost;
+                cg = cand;
+            }
+        }
+    }
     while (cg > 1 && interp_smem_bytes(p->gi, cg) > smem_budget(p)) cg /= 2;
     return cg;
 }
@@ -466,6 +480,12 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         delete p;
         return fail(GBN_ERR_ARG, "coil_group must be 1, 2, 4 or 8");
     }
+    p->interp_coil_group = desc->interp_coil_group;
+    if (p->interp_coil_group != 0 && p->interp_coil_group != 1 && p->interp_coil_group != 2 &&
+        p->interp_coil_group != 4 && p->interp_coil_group != 8) {
+        delete p;
+        return fail(GBN_ERR_ARG, "interp_coil_group must be 0, 1, 2, 4 or 8");
+    }
     p->threads = desc->threads > 0 ? desc->threads : 256;
     p->interp_threads = desc->interp_threads > 0 ? desc->interp_threads : (p->dim == 2 ? 512 : 256);
     for (int t : {p->threads, p->interp_threads}) {
@@ -625,6 +645,7 @@ int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     o->threads = p->threads;
     o->interp_threads = p->interp_threads;
     o->max_subproblem = p->max_sub;
+    o->interp_coil_group = interp_cg(p);
     o->device_bytes = (int64_t)p->device_bytes;
     return GBN_OK;
 }

@@ -32,6 +32,18 @@ __device__ __forceinline__ int wrap_mod(int v, int n) {
     return v < 0 ? v + n : v;
 }
 
+// v in [-n, inf): wrapped into [0, n) without a division (the loop runs only when a window
+// is wider than the grid)
+__device__ __forceinline__ int wrap_fast(int v, int n) {
+    v += v < 0 ? n : 0;
+    while (v >= n) v -= n;
+    return v;
+}
+
+// a / b for 0 <= a < 2^20 and 1 <= b, with rb = 1.0f / b: (a + 0.5) * rb is within
+// 2^-21 (a/b) of the true quotient, far less than the 0.5/b to the nearest integer
+__device__ __forceinline__ int div_small(int a, float rb) { return (int)(((float)a + 0.5f) * rb); }
+
 // --------------------------------------------------------------------------------- interp
 template <int WT, int CG>
 __global__ void __launch_bounds__(512) k_interp2d(InterpArgs a) {
@@ -50,19 +62,19 @@ __global__ void __launch_bounds__(512) k_interp2d(InterpArgs a) {
     const int WX = g.tile[0] + W - 1, WY = g.tile[1] + W - 1;
     const int nf0 = g.nf[0], nf1 = g.nf[1];
 
-    // stage the window (periodic wrap), all CG coils of a cell contiguous
+    // stage the window (periodic wrap), all CG coils of a cell contiguous; coil fastest
+    // across threads, so the shared-memory stores are consecutive 8-byte words and each
+    // warp's global loads are CG runs of 32/CG consecutive cells
     {
         const int ws0 = o0 - (ns - 1), ws1 = o1 - (ns - 1);
         const float2 *base = a.grid + ((int64_t)grp * g.n_coil + cg0) * g.G;
-        const int ncell = WX * WY;
-        for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
-            const int wx = i / WY, wy = i - wx * WY;
-            const int gx = wrap_mod(ws0 + wx, nf0), gy = wrap_mod(ws1 + wy, nf1);
-            const float2 *src = base + (int64_t)gx * nf1 + gy;
-            float2 *dst = win + (size_t)i * CG;
-#pragma unroll
-            for (int c = 0; c < CG; ++c)
-                dst[c] = (cg0 + c < g.n_coil) ? src[(int64_t)c * g.G] : make_float2(0.f, 0.f);
+        const int nitem = WX * WY * CG;
+        const float rWY = 1.f / (float)WY;
+        for (int i = threadIdx.x; i < nitem; i += blockDim.x) {
+            const int c = i % CG, cell = i / CG;  // CG is a power of two
+            const int wx = div_small(cell, rWY), wy = cell - wx * WY;
+            const int gx = wrap_fast(ws0 + wx, nf0), gy = wrap_fast(ws1 + wy, nf1);
+            win[i] = (cg0 + c < g.n_coil) ? base[(int64_t)c * g.G + (int64_t)gx * nf1 + gy] : make_float2(0.f, 0.f);
         }
     }
     __syncthreads();
@@ -103,23 +115,29 @@ __global__ void __launch_bounds__(512) k_interp2d(InterpArgs a) {
             const float v = __shfl_sync(0xffffffffu, myw, 16 + (ky < 16 ? ky : 15));
             wy[t] = ky < W ? v : 0.f;
         }
-        float ax = 0.f, ay = 0.f;
+        // a lane's y taps are fixed, so it sums wx * G over x per tap slot and applies its
+        // y weights once at the end: one load and one packed FMA per tap
+        float2 acc[L::KT];
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) acc[t] = make_float2(0.f, 0.f);
         const float2 *rowbase = win + ((size_t)rel0 * WY + rel1) * CG + c;
 #pragma unroll
         for (int kx = 0; kx < L::WMAX; ++kx) {
             if (WT == 0 && kx >= W) break;
             const float wx = __shfl_sync(0xffffffffu, myw, kx);
+            const float2 wx2 = make_float2(wx, wx);
             const float2 *row = rowbase + (size_t)kx * WY * CG;
 #pragma unroll
             for (int t = 0; t < L::KT; ++t) {
                 const int ky = q + t * L::NQ;
-                if (ky < W) {
-                    const float2 v = row[ky * CG];
-                    const float w = wx * wy[t];
-                    ax = fmaf(w, v.x, ax);
-                    ay = fmaf(w, v.y, ay);
-                }
+                if (ky < W) acc[t] = __ffma2_rn(wx2, row[ky * CG], acc[t]);
             }
+        }
+        float ax = 0.f, ay = 0.f;
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) {
+            ax = fmaf(wy[t], acc[t].x, ax);
+            ay = fmaf(wy[t], acc[t].y, ay);
         }
 #pragma unroll
         for (int off = CG; off < 32; off <<= 1) {

@@ -47,15 +47,17 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
     {
         const int ws0 = o[0] - (ns - 1), ws1 = o[1] - (ns - 1), ws2 = o[2] - (ns - 1);
         const float2 *base = a.grid + ((int64_t)grp * g.n_coil + cg0) * g.G;
-        const int ncell = WX * WY * WZ;
-        for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
-            const int wz = i % WZ, wy = (i / WZ) % WY, wx = i / (WZ * WY);
-            const int gx = wrap_mod(ws0 + wx, nf0), gy = wrap_mod(ws1 + wy, nf1), gz = wrap_mod(ws2 + wz, nf2);
-            const float2 *src = base + ((int64_t)gx * nf1 + gy) * nf2 + gz;
-            float2 *dst = win + (size_t)i * CG;
-#pragma unroll
-            for (int c = 0; c < CG; ++c)
-                dst[c] = (cg0 + c < g.n_coil) ? src[(int64_t)c * g.G] : make_float2(0.f, 0.f);
+        // coil fastest across threads: consecutive shared-memory words, CG runs of
+        // consecutive z cells per warp load
+        const int nitem = WX * WY * WZ * CG;
+        const float rWZ = 1.f / (float)WZ, rWY = 1.f / (float)WY;
+        for (int i = threadIdx.x; i < nitem; i += blockDim.x) {
+            const int c = i % CG, cell = i / CG;  // CG is a power of two
+            const int xy = div_small(cell, rWZ), wz = cell - xy * WZ;
+            const int wx = div_small(xy, rWY), wy = xy - wx * WY;
+            const int gx = wrap_fast(ws0 + wx, nf0), gy = wrap_fast(ws1 + wy, nf1), gz = wrap_fast(ws2 + wz, nf2);
+            win[i] = (cg0 + c < g.n_coil) ? base[(int64_t)c * g.G + ((int64_t)gx * nf1 + gy) * nf2 + gz]
+                                          : make_float2(0.f, 0.f);
         }
     }
     __syncthreads();
@@ -101,7 +103,10 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
             const float d = p.z + (float)(ns - 1 - kz);
             wz[t] = kz < W ? exp2f(-g.beta2[2] * d * d) : 0.f;
         }
-        float2 acc = make_float2(0.f, 0.f);
+        // a lane's z taps are fixed: sum wx wy * G per tap slot, apply wz once at the end
+        float2 at[L::KT];
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) at[t] = make_float2(0.f, 0.f);
         const float2 *base = win + (((size_t)rel[0] * WY + rel[1]) * WZ + rel[2]) * CG + c;
 #pragma unroll 1
         for (int kx = 0; kx < W; ++kx) {
@@ -111,16 +116,20 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
             for (int ky = 0; ky < L::WMAX; ++ky) {
                 if (WT == 0 && ky >= W) break;
                 const float wxy = wx * wy[ky];
+                const float2 wxy2 = make_float2(wxy, wxy);
                 const float2 *row = plane + (size_t)ky * WZ * CG;
 #pragma unroll
                 for (int t = 0; t < L::KT; ++t) {
                     const int kz = q + t * L::NQ;
-                    if (kz < W) {
-                        const float w = wxy * wz[t];
-                        acc = __ffma2_rn(make_float2(w, w), row[kz * CG], acc);
-                    }
+                    if (kz < W) at[t] = __ffma2_rn(wxy2, row[kz * CG], at[t]);
                 }
             }
+        }
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) {
+            acc.x = fmaf(wz[t], at[t].x, acc.x);
+            acc.y = fmaf(wz[t], at[t].y, acc.y);
         }
 #pragma unroll
         for (int off = CG; off < 32; off <<= 1) {

@@ -187,7 +187,7 @@ __device__ __forceinline__ void load_window(const Geom &g, const float2 *__restr
     }
     const int wcell = wd[0] * wd[1] * wd[2];
     for (int i = threadIdx.x; i < wcell * CG; i += blockDim.x) {
-        const int c = i / wcell, w = i - c * wcell;
+        const int c = i % CG, w = i / CG;  // coil fastest: consecutive shared-memory words
         const int w2 = w % wd[2], w1 = (w / wd[2]) % wd[1], w0 = w / (wd[2] * wd[1]);
         int gx = (ws[0] + w0) % g.nf[0]; gx += gx < 0 ? g.nf[0] : 0;
         int gy = D > 1 ? (ws[1] + w1) % g.nf[1] : 0; gy += gy < 0 ? g.nf[1] : 0;

@@ -51,22 +51,24 @@ class Tuning:
     """Kernel tiling chosen by the autotuner (0 = library default)."""
 
     def __init__(self, spread_tile=(0, 0, 0), interp_tile=(0, 0, 0), max_subproblem=0, coil_group=0, threads=0,
-                 interp_threads=0):
+                 interp_threads=0, interp_coil_group=0):
         self.spread_tile = tuple(spread_tile) + (0,) * (3 - len(spread_tile))
         self.interp_tile = tuple(interp_tile) + (0,) * (3 - len(interp_tile))
         self.max_subproblem = max_subproblem
         self.coil_group = coil_group
         self.threads = threads
         self.interp_threads = interp_threads
+        self.interp_coil_group = interp_coil_group
 
     def key(self):
         return (self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
-                self.interp_threads)
+                self.interp_threads, self.interp_coil_group)
 
     def __repr__(self):
         return ("Tuning(spread_tile=%s, interp_tile=%s, max_subproblem=%d, coil_group=%d, threads=%d, "
-                "interp_threads=%d)" % (self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group,
-                                        self.threads, self.interp_threads))
+                "interp_threads=%d, interp_coil_group=%d)" % (
+                    self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
+                    self.interp_threads, self.interp_coil_group))
 
 
 class Graph:
@@ -123,6 +125,7 @@ class NufftPlan:
         d.coil_group = int(self.tuning.coil_group)
         d.threads = int(self.tuning.threads)
         d.interp_threads = int(self.tuning.interp_threads)
+        d.interp_coil_group = int(self.tuning.interp_coil_group)
         self._lib = N.lib()
         h = ctypes.c_void_p()
         N.check(self._lib.gbn_plan_create(ctypes.byref(d), ctypes.byref(h)))
@@ -152,7 +155,7 @@ class NufftPlan:
             "spread_entries": inf.spread_entries, "spread_tile": tuple(inf.spread_tile[:self.dim]),
             "interp_tile": tuple(inf.interp_tile[:self.dim]), "coil_group": inf.coil_group,
             "threads": inf.threads, "interp_threads": inf.interp_threads, "max_subproblem": inf.max_subproblem,
-            "device_bytes": inf.device_bytes,
+            "device_bytes": inf.device_bytes, "interp_coil_group": inf.interp_coil_group,
         }
 
     def grid(self):

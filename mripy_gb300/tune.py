@@ -21,10 +21,33 @@ from .plan import NufftPlan, Tuning
 _CACHE = {}
 
 
+def _spread_candidates(dim, n_coil):
+    """(tile, threads, coil_group) triples: the register-tile kernels' own tiles (rows of 4
+    per warp, 4 columns per lane) for 4 and 8 coils per block, plus shared-memory tiles."""
+    out = []
+    groups = [cg for cg in (8, 4) if n_coil >= cg]
+    if dim == 2:
+        for cg in groups:
+            for th in (128, 256):
+                out.append(((4 * th // 32, 4 * 32 // cg), th, cg))
+        out += [((16, 32), 256, 8), ((32, 32), 256, 8)]
+    elif dim == 3:
+        for cg in groups:
+            for th in (128, 256):
+                rows = 4 * th // 32
+                for ty in (4, 8, 16):
+                    if rows % ty == 0:
+                        out.append(((rows // ty, ty, 4 * 32 // cg), th, cg))
+        out += [((8, 8, 32), 256, 8)]
+    else:
+        out = [((t,), 256, 8) for t in (1024, 512, 2048)]
+    return out
+
+
 def _candidates(dim):
     if dim == 2:
         spread = [(16, 32), (8, 32), (32, 32), (16, 64), (32, 16)]
-        interp = [(16, 16), (8, 32), (16, 32), (8, 16)]
+        interp = [(16, 16), (8, 32), (16, 32), (8, 16), (32, 32)]
     elif dim == 3:
         spread = [(8, 8, 32), (8, 8, 16), (4, 8, 32), (8, 16, 16)]
         interp = [(8, 8, 8), (4, 8, 16), (8, 8, 16), (4, 4, 16)]
@@ -96,37 +119,38 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
             t = Tuning(**stored[key])
             _CACHE[key] = t
             return t
-    spread_c, interp_c = _candidates(dim)
+    _, interp_c = _candidates(dim)
     best_s = best_i = None
     # spread tiling (interp at default), then interp tiling (spread at the winner)
-    for tile in spread_c:
-        for th in (128, 256):
-            tu = Tuning(spread_tile=tile, threads=th)
-            try:
-                t_s, _ = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
-            except Exception:
-                continue
-            if verbose:
-                print("spread", tile, th, t_s)
-            if best_s is None or t_s < best_s[0]:
-                best_s = (t_s, tile, th)
+    for tile, th, cg in _spread_candidates(dim, n_coil):
+        tu = Tuning(spread_tile=tile, threads=th, coil_group=cg)
+        try:
+            t_s, _ = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
+        except Exception:
+            continue
+        if verbose:
+            print("spread", tile, th, cg, t_s)
+        if best_s is None or t_s < best_s[0]:
+            best_s = (t_s, tile, th, cg)
+    icg = [0] + [cg for cg in (8, 4, 2) if cg <= n_coil]
     for tile in interp_c:
         for th in ((256, 512) if dim == 2 else (128, 256)):
-            tu = Tuning(interp_tile=tile, interp_threads=th)
-            try:
-                _, t_i = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
-            except Exception:
-                continue
-            if verbose:
-                print("interp", tile, th, t_i)
-            if best_i is None or t_i < best_i[0]:
-                best_i = (t_i, tile, th)
+            for cg in icg:
+                tu = Tuning(interp_tile=tile, interp_threads=th, interp_coil_group=cg)
+                try:
+                    _, t_i = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
+                except Exception:
+                    continue
+                if verbose:
+                    print("interp", tile, th, cg, t_i)
+                if best_i is None or t_i < best_i[0]:
+                    best_i = (t_i, tile, th, cg)
     if best_s is None or best_i is None:
         raise RuntimeError("no tuning candidate ran")
     best = None
-    for ms in (128, 256, 512):
-        tu = Tuning(spread_tile=best_s[1], threads=best_s[2], interp_tile=best_i[1], interp_threads=best_i[2],
-                    max_subproblem=ms)
+    for ms in (64, 128, 256, 512):
+        tu = Tuning(spread_tile=best_s[1], threads=best_s[2], coil_group=best_s[3], interp_tile=best_i[1],
+                    interp_threads=best_i[2], interp_coil_group=best_i[3], max_subproblem=ms)
         t_s, t_i = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
         if verbose:
             print("max_subproblem", ms, t_s + t_i)
@@ -141,7 +165,8 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
                 stored = json.load(f)
         stored[key] = {"spread_tile": list(tuning.spread_tile), "interp_tile": list(tuning.interp_tile),
                        "max_subproblem": tuning.max_subproblem, "coil_group": tuning.coil_group,
-                       "threads": tuning.threads, "interp_threads": tuning.interp_threads}
+                       "threads": tuning.threads, "interp_threads": tuning.interp_threads,
+                       "interp_coil_group": tuning.interp_coil_group}
         with open(cache_file, "w") as f:
             json.dump(stored, f, indent=1)
     return tuning
