@@ -44,6 +44,7 @@ typedef struct CUstream_st *gbn_stream_t; /* == cudaStream_t; NULL = legacy defa
 #define GBN_ERR_STATE 5     /* call order: e.g. transform before gbn_set_points */
 #define GBN_ERR_CAPACITY 6  /* size beyond a documented limit */
 #define GBN_ERR_INTERNAL 7  /* unexpected host-side failure */
+#define GBN_ERR_TIMEOUT 8   /* a kernel's bounded wait gave up (reported by gbn_plan_status) */
 
 #define GBN_COORD_F32 0
 #define GBN_COORD_F64 1
@@ -72,6 +73,8 @@ typedef struct {
     int32_t interp_threads; /* threads per interp block: 128, 256 or 512 */
     int32_t interp_coil_group; /* coils per interp thread block: 1, 2, 4 or 8 (0: the
                                   group that pads the coil count least) */
+    int32_t interp_staging;    /* 2-D interp windows: 0 = tensor-memory-access copies
+                                  where the grid allows (default), 1 = thread loads */
 } gbn_plan_desc;
 
 typedef struct {
@@ -116,6 +119,11 @@ int gbn_grid_params(int dim, int ms, int mt, int mu, double eps, int max_nspread
 int gbn_plan_create(const gbn_plan_desc *desc, gbn_plan **out);
 int gbn_plan_destroy(gbn_plan *plan);
 int gbn_plan_get_info(const gbn_plan *plan, gbn_plan_info *out);
+/* Synchronises the stream and reads the plan's device status word: GBN_ERR_TIMEOUT if
+ * a kernel's bounded wait (the TMA window copies of the 2-D interp) gave up since the
+ * last call, which also clears it; else GBN_OK.  No counterpart in the reference (its
+ * kernels have no waits). */
+int gbn_plan_status(gbn_plan *plan, gbn_stream_t stream);
 
 /* Sorts the samples into spatial bins (device coordinates, float32 or float64,
  * x/y/z each of length traj_offsets[n_traj]; unused dims may be NULL).

@@ -11,12 +11,14 @@
 // whose stencil reaches it, so the two run as separate kernels with the sample values
 // (n_coil complex per sample) kept in a plan-owned buffer between them.
 #include <cub/cub.cuh>
+#include <cudaTypedefs.h>
 #include <cufft.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -79,6 +81,7 @@ struct gbn_plan {
     double tau = 0;
     Geom gs{}, gi{};
     int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256, interp_coil_group = 0;
+    int interp_staging = 0;  // 0: tensor copies where the grid allows, 1: thread loads
     int64_t G = 1, n_inst = 1;
     size_t device_bytes = 0;
     int smem_optin = 0;
@@ -86,8 +89,14 @@ struct gbn_plan {
     // fixed buffers
     float2 *grid = nullptr;
     float *tab[3] = {nullptr, nullptr, nullptr};
+    uint32_t *kstatus = nullptr;  // device status word: bits set by kernels whose bounded waits gave up
     cufftHandle fft = 0;
     bool fft_ok = false;
+
+    // tensor map of the last grid the TMA interp read (re-encoded when the grid changes)
+    CUtensorMap tmap{};
+    const void *tmap_grid = nullptr;
+    int tmap_cg = 0, tmap_bx = 0, tmap_by = 0;
 
     // point-dependent buffers (grow-only)
     bool points_set = false;
@@ -255,6 +264,50 @@ int interp_cg(const gbn_plan *p) {
     return cg;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against the
+// driver library); null when the driver does not provide it
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// Tensor map of a 2-D plan grid as a 3-D tensor (y innermost, x, instance) of 8-byte
+// cells, box BY x BX x coils; cached for the last grid pointer and box.  False when the
+// grid is not 16-byte aligned, its rows are not a multiple of 16 bytes, or the driver
+// lacks the encoder: the caller then uses the thread-staged kernel.
+bool grid_tensor_map(gbn_plan *p, const float2 *grid, int cg, const TmaWin &t) {
+    if (p->tmap_grid == grid && p->tmap_cg == cg && p->tmap_bx == t.BX && p->tmap_by == t.BY) return true;
+    p->tmap_grid = nullptr;
+    if ((reinterpret_cast<uintptr_t>(grid) & 15) || (p->nf[1] & 1)) return false;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)p->nf[1], (cuuint64_t)p->nf[0], (cuuint64_t)p->n_inst};
+    const cuuint64_t strides[2] = {(cuuint64_t)p->nf[1] * sizeof(float2),
+                                   (cuuint64_t)p->nf[0] * p->nf[1] * sizeof(float2)};
+    const cuuint32_t box[3] = {(cuuint32_t)t.BY, (cuuint32_t)t.BX, (cuuint32_t)cg};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = enc(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<float2 *>(grid), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    p->tmap_grid = grid;
+    p->tmap_cg = cg;
+    p->tmap_bx = t.BX;
+    p->tmap_by = t.BY;
+    return true;
+}
+
 int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const float *weight, cudaStream_t s) {
     InterpArgs a;
     a.g = p->gi;
@@ -267,6 +320,13 @@ int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const flo
     a.c_coil = L.coil_stride;
     a.weight = weight;
     const int cg = interp_cg(p);
+    // 2-D: windows staged by tensor copies when the grid admits a tensor map
+    TmaWin t{};
+    if (p->interp_staging == 0 && tma_window(p->gi, cg, p->n_interp_sub, t) &&
+        tma_interp_smem_bytes(t) <= (size_t)p->smem_optin && grid_tensor_map(p, grid, cg, t)) {
+        GBN_CUDA(launch_interp2d_tma(a, t, p->tmap, cg, p->interp_threads, p->kstatus, s));
+        return GBN_OK;
+    }
     if (interp_smem_bytes(p->gi, cg) > (size_t)p->smem_optin)
         return fail(GBN_ERR_CAPACITY, "interp window does not fit in shared memory");
     GBN_CUDA(launch_interp(a, p->n_interp_sub, cg, p->interp_threads, s));
@@ -486,6 +546,11 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         delete p;
         return fail(GBN_ERR_ARG, "interp_coil_group must be 0, 1, 2, 4 or 8");
     }
+    if (desc->interp_staging != 0 && desc->interp_staging != 1) {
+        delete p;
+        return fail(GBN_ERR_ARG, "interp_staging must be 0 or 1");
+    }
+    p->interp_staging = desc->interp_staging;
     p->threads = desc->threads > 0 ? desc->threads : 256;
     p->interp_threads = desc->interp_threads > 0 ? desc->interp_threads : (p->dim == 2 ? 512 : 256);
     for (int t : {p->threads, p->interp_threads}) {
@@ -549,7 +614,14 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         }
         p->device_bytes += sizeof(float) * p->m[d];
     }
-    e = launch_build_tables(p->dim, p->m, p->nf, p->tau, p->tab[0], p->tab[1], p->tab[2], 0);
+    e = cudaMalloc((void **)&p->kstatus, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        p->kstatus = nullptr;
+        return bail(fail(GBN_ERR_ALLOC, "status word allocation failed"));
+    }
+    e = cudaMemset(p->kstatus, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = launch_build_tables(p->dim, p->m, p->nf, p->tau, p->tab[0], p->tab[1], p->tab[2], 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return bail(fail(GBN_ERR_CUDA, std::string("table build: ") + cudaGetErrorString(e)));
 
@@ -584,6 +656,7 @@ const char *gbn_status_string(int status) {
         case GBN_ERR_STATE: return "invalid call order";
         case GBN_ERR_CAPACITY: return "size beyond a supported limit";
         case GBN_ERR_INTERNAL: return "internal error";
+        case GBN_ERR_TIMEOUT: return "a kernel's bounded wait gave up";
         default: return "unknown status";
     }
 }
@@ -612,6 +685,7 @@ int gbn_plan_destroy(gbn_plan *p) {
     if (!p) return GBN_OK;
     if (p->fft_ok) cufftDestroy(p->fft);
     if (p->grid) cudaFree(p->grid);
+    if (p->kstatus) cudaFree(p->kstatus);
     for (int d = 0; d < 3; ++d)
         if (p->tab[d]) cudaFree(p->tab[d]);
     DevBuf *bufs[] = {&p->traj_off_d, &p->grp_scale, &p->pts, &p->home_key, &p->home_keys_sorted,
@@ -623,6 +697,17 @@ int gbn_plan_destroy(gbn_plan *p) {
     for (DevBuf *b : bufs) release(*b);
     delete p;
     return GBN_OK;
+}
+
+int gbn_plan_status(gbn_plan *p, gbn_stream_t stream) {
+    if (!p) return fail(GBN_ERR_ARG, "null plan");
+    const cudaStream_t s = (cudaStream_t)stream;
+    uint32_t st = 0;
+    GBN_CUDA(cudaStreamSynchronize(s));
+    GBN_CUDA(cudaMemcpy(&st, p->kstatus, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st == 0) return GBN_OK;
+    GBN_CUDA(cudaMemset(p->kstatus, 0, sizeof(uint32_t)));
+    return fail(GBN_ERR_TIMEOUT, "status word " + std::to_string(st) + ": a TMA window wait gave up");
 }
 
 int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {

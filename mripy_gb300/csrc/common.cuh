@@ -10,6 +10,7 @@
 //   subs      int4 {tile id, start, length, flags} work items of <= max_subproblem samples
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (TMA descriptors); the library calls no driver API directly
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -137,6 +138,20 @@ cudaError_t launch_interp_grad(const GradArgs &a, int64_t n_sub, int coil_group,
                                cudaStream_t s);
 size_t spread_smem_bytes(const Geom &g, int coil_group);
 size_t interp_smem_bytes(const Geom &g, int coil_group);
+
+// TMA-staged 2-D interp (interp2d_tma.cuh): window box geometry and launcher
+struct TmaWin {
+    int BX, BY;           // box: x rows, y cells per row (BY even, both cover the window)
+    int CS;               // cells per coil in a staged window = BX * BY
+    int n_cg;             // coil groups
+    int64_t n_items;      // interp subproblems x coil groups
+    uint32_t box_bytes;   // bytes one box copy delivers: BX * BY * CG * 8
+    uint32_t buf_elems;   // float2 per buffer: CG * CS rounded up to 16 (128-byte buffers)
+};
+bool tma_window(const Geom &g, int coil_group, int64_t n_sub, TmaWin &t);
+size_t tma_interp_smem_bytes(const TmaWin &t);
+cudaError_t launch_interp2d_tma(const InterpArgs &a, const TmaWin &t, const CUtensorMap &map, int coil_group,
+                                int threads, uint32_t *status, cudaStream_t s);
 
 // deapod.cu
 struct DeapodArgs {

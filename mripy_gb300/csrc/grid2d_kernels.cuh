@@ -300,9 +300,24 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
 constexpr int kRegRows = 4;    // rows per warp
 constexpr int kRegCols = 4;    // columns per lane
 constexpr int kRegBatch = 32;  // samples per staged batch
-constexpr int kRegPad = 4;     // stride padding of the staged weight rows (bank spread, 16-byte aligned)
+
+// Stride (floats) of a staged per-sample weight row of n floats: a multiple of 4 for
+// 16-byte loads and stores, and an odd number of 16-byte units so that the 16-byte stores
+// of 8 consecutive lanes fill the 32 banks exactly once (conflict-free staging).
+__host__ __device__ inline int reg_stride(int n) {
+    int n4 = (n + 3) / 4;
+    n4 += (n4 % 2 == 0) ? 1 : 0;
+    return 4 * n4;
+}
 
 __device__ __forceinline__ unsigned lanemask_lt(int lane) { return (1u << lane) - 1u; }
+
+// Gaussian weight of tap `tap` (0 outside [0, W)) for in-cell fraction f
+__device__ __forceinline__ float tap_weight(bool ok, int tap, int W, float f, int ns, float beta2) {
+    if (!ok || (unsigned)tap >= (unsigned)W) return 0.f;
+    const float d = f + (float)(ns - 1 - tap);
+    return exp2f(-beta2 * d * d);
+}
 
 template <int WT, int CG>
 __global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
@@ -311,7 +326,7 @@ __global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
     extern __shared__ float4 smem_r2[];
     const Geom &g = a.g;
     const int TX = g.tile[0], TY = g.tile[1];  // TX = 4 * warps, TY = 4 * NQ (set by the host)
-    const int TXP = TX + kRegPad, TYP = TY + kRegPad;
+    const int TXP = reg_stride(TX), TYP = reg_stride(TY);
     const int nw = blockDim.x >> 5;
     float *st_wr = reinterpret_cast<float *>(smem_r2);                     // [2][B][TXP]
     float *st_wc = st_wr + 2 * B * TXP;                                    // [2][B][TYP]: [q][k]
@@ -360,14 +375,11 @@ __global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
             }
             if (warp == 0) {
                 float *dst = st_wr + (buf * B + lane) * TXP;
-                for (int row = 0; row < TX; ++row) {
-                    const int tap = row - rx;
-                    float val = 0.f;
-                    if (ok && (unsigned)tap < (unsigned)W) {
-                        const float d = p.x + (float)(ns - 1 - tap);
-                        val = exp2f(-g.beta2[0] * d * d);
-                    }
-                    dst[row] = val;
+                for (int r4 = 0; r4 < TX; r4 += 4) {
+                    const float b = g.beta2[0];
+                    *reinterpret_cast<float4 *>(dst + r4) =
+                        make_float4(tap_weight(ok, r4 - rx, W, p.x, ns, b), tap_weight(ok, r4 + 1 - rx, W, p.x, ns, b),
+                                    tap_weight(ok, r4 + 2 - rx, W, p.x, ns, b), tap_weight(ok, r4 + 3 - rx, W, p.x, ns, b));
                 }
                 for (int w = 0; w < nw; ++w) {
                     const bool hit = ok && rx < w * kRegRows + kRegRows && rx + W > w * kRegRows;
@@ -377,15 +389,13 @@ __global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
                 }
             } else {
                 float *dst = st_wc + (buf * B + lane) * TYP;
-                for (int col = 0; col < TY; ++col) {
-                    const int tap = col - ry;
-                    float val = 0.f;
-                    if (ok && (unsigned)tap < (unsigned)W) {
-                        const float d = p.y + (float)(ns - 1 - tap);
-                        val = exp2f(-g.beta2[1] * d * d);
-                    }
-                    dst[(col % NQ) * 4 + col / NQ] = val;
-                }
+                const float b = g.beta2[1];
+#pragma unroll
+                for (int cq = 0; cq < NQ; ++cq)  // columns cq + k*NQ, k = 0..3, as one 16-byte store
+                    *reinterpret_cast<float4 *>(dst + cq * 4) =
+                        make_float4(tap_weight(ok, cq - ry, W, p.y, ns, b), tap_weight(ok, cq + NQ - ry, W, p.y, ns, b),
+                                    tap_weight(ok, cq + 2 * NQ - ry, W, p.y, ns, b),
+                                    tap_weight(ok, cq + 3 * NQ - ry, W, p.y, ns, b));
             }
         } else {
             for (int i = threadIdx.x - 64; i < n * CG; i += blockDim.x - 64) {
@@ -450,7 +460,7 @@ __global__ void __launch_bounds__(256) k_spread2d_reg(SpreadArgs a) {
 }
 
 inline size_t spread2d_reg_smem_bytes(const Geom &g, int cg) {
-    return 2 * ((size_t)kRegBatch * (g.tile[0] + g.tile[1] + 2 * kRegPad) * sizeof(float) +
+    return 2 * ((size_t)kRegBatch * (reg_stride(g.tile[0]) + reg_stride(g.tile[1])) * sizeof(float) +
                 (size_t)kRegBatch * cg * sizeof(float2)) +
            16 * sizeof(int) + 2 * 8 * kRegBatch;
 }

@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
     const int TX = g.tile[0], TY = g.tile[1], TZ = g.tile[2];
     // per staged sample: y rows [0, TY), z columns [TY, TY + TZ) as [q][k], x planes after
     // them; the stride is padded to a multiple of 4 (16-byte loads) plus a bank offset
-    const int TWP = ((TX + TY + TZ + 3) & ~3) + kRegPad;
+    const int TWP = reg_stride(TY + TZ + 4 * ((TX + 3) / 4));
     const int nw = blockDim.x >> 5;
     float *st_w = reinterpret_cast<float *>(smem_r3);                  // [2][B][TWP]
     float2 *st_v = reinterpret_cast<float2 *>(st_w + 2 * B * TWP);     // [2][B][CG]
@@ -335,22 +335,31 @@ __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
                     r[d] = rr;
                 }
             }
-            // warp 0: x planes (+ lists), warp 1: y rows, warp 2: z columns
-            const int d = warp == 0 ? 0 : (warp == 1 ? 1 : 2);
-            const int len = d == 0 ? TX : (d == 1 ? TY : TZ);
-            const int rd = d == 0 ? r[0] : (d == 1 ? r[1] : r[2]);
-            const float f = d == 0 ? p.x : (d == 1 ? p.y : p.z);
-            const float bd = d == 0 ? g.beta2[0] : (d == 1 ? g.beta2[1] : g.beta2[2]);
+            // warp 0: x planes (+ lists), warp 1: y rows, warp 2: z columns; 16-byte stores
             float *dst = st_w + (buf * B + lane) * TWP;
-            for (int k = 0; k < len; ++k) {
-                const int tap = k - rd;
-                float val = 0.f;
-                if (ok && (unsigned)tap < (unsigned)W) {
-                    const float dd = f + (float)(ns - 1 - tap);
-                    val = exp2f(-bd * dd * dd);
-                }
-                const int slot = d == 0 ? TY + TZ + k : (d == 1 ? k : TY + (k % NQ) * 4 + k / NQ);
-                dst[slot] = val;
+            if (warp == 0) {
+                const float b = g.beta2[0];
+                for (int k4 = 0; k4 < TX; k4 += 4)  // planes past TX get harmless unused weights
+                    *reinterpret_cast<float4 *>(dst + TY + TZ + k4) =
+                        make_float4(tap_weight(ok, k4 - r[0], W, p.x, ns, b), tap_weight(ok, k4 + 1 - r[0], W, p.x, ns, b),
+                                    tap_weight(ok, k4 + 2 - r[0], W, p.x, ns, b),
+                                    tap_weight(ok, k4 + 3 - r[0], W, p.x, ns, b));
+            } else if (warp == 1) {
+                const float b = g.beta2[1];
+                for (int k4 = 0; k4 < TY; k4 += 4)
+                    *reinterpret_cast<float4 *>(dst + k4) =
+                        make_float4(tap_weight(ok, k4 - r[1], W, p.y, ns, b), tap_weight(ok, k4 + 1 - r[1], W, p.y, ns, b),
+                                    tap_weight(ok, k4 + 2 - r[1], W, p.y, ns, b),
+                                    tap_weight(ok, k4 + 3 - r[1], W, p.y, ns, b));
+            } else {
+                const float b = g.beta2[2];
+#pragma unroll
+                for (int cq = 0; cq < NQ; ++cq)  // columns cq + k*NQ, k = 0..3
+                    *reinterpret_cast<float4 *>(dst + TY + cq * 4) =
+                        make_float4(tap_weight(ok, cq - r[2], W, p.z, ns, b),
+                                    tap_weight(ok, cq + NQ - r[2], W, p.z, ns, b),
+                                    tap_weight(ok, cq + 2 * NQ - r[2], W, p.z, ns, b),
+                                    tap_weight(ok, cq + 3 * NQ - r[2], W, p.z, ns, b));
             }
             if (warp == 0) {
                 for (int w = 0; w < nw; ++w) {
@@ -425,7 +434,7 @@ __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
 }
 
 inline size_t spread3d_reg_smem_bytes(const Geom &g, int cg) {
-    const int twp = ((g.tile[0] + g.tile[1] + g.tile[2] + 3) & ~3) + kRegPad;
+    const int twp = reg_stride(g.tile[1] + g.tile[2] + 4 * ((g.tile[0] + 3) / 4));
     return 2 * ((size_t)kRegBatch * twp * sizeof(float) + (size_t)kRegBatch * cg * sizeof(float2)) +
            16 * sizeof(int) + 2 * 8 * kRegBatch;
 }

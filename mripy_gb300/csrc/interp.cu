@@ -1,10 +1,15 @@
 // Interp (type-2 gridding) and trajectory-gradient launchers.
 //
-// 2-D with at most 16 taps per dimension: k_interp2d (one warp per sample, coils across
-// lanes).  Otherwise (1-D, 3-D, wide stencils): k_interp (one thread per sample).
+// 2-D with at most 16 taps per dimension: k_interp2d_tma (persistent, windows staged by
+// tensor copies; the caller supplies the tensor map) or k_interp2d (one block per
+// subproblem, windows gathered by the threads).  3-D with at most 16 taps: k_interp3d.
+// Otherwise (1-D, wide stencils): k_interp (one thread per sample).
+#include <algorithm>
+
 #include "dispatch.cuh"
 #include "grid2d_kernels.cuh"
 #include "grid3d_kernels.cuh"
+#include "interp2d_tma.cuh"
 
 namespace gbn {
 
@@ -58,6 +63,69 @@ cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, in
             err = cudaGetLastError();
         }
     })));
+    return err;
+}
+
+// ---------------------------------------------------------------- TMA-staged 2-D interp
+
+// Box of a staged window: BX >= WX rows and BY >= WY + 1 cells (even, since the window may
+// start one cell into a row), smallest area such that the coil stride CS = BX * BY puts the
+// CG coil runs of a half-warp's 8-byte loads on distinct banks: CS = 2 (mod 4) for 8 coils,
+// 4 (mod 8) for 4, 8 (mod 16) for 2.
+bool tma_window(const Geom &g, int cg, int64_t n_sub, TmaWin &t) {
+    if (g.dim != 2 || g.W > 16 || (g.nf[1] & 1)) return false;
+    const int WX = g.tile[0] + g.W - 1, WY = g.tile[1] + g.W - 1;
+    const int mod = cg == 8 ? 4 : (cg == 4 ? 8 : (cg == 2 ? 16 : 1));
+    const int want = cg == 8 ? 2 : (cg == 4 ? 4 : (cg == 2 ? 8 : 0));
+    int best = 0;
+    for (int bx = WX; bx < WX + 16; ++bx)
+        for (int by = (WY + 2) & ~1; by < WY + 18; by += 2) {
+            if (bx > g.nf[0] || by > g.nf[1] || bx > 256 || by > 256) continue;
+            if ((bx * by) % mod != want) continue;
+            if (best == 0 || bx * by < best) {
+                best = bx * by;
+                t.BX = bx;
+                t.BY = by;
+            }
+        }
+    if (best == 0) return false;
+    t.CS = t.BX * t.BY;
+    t.n_cg = (g.n_coil + cg - 1) / cg;
+    t.n_items = n_sub * t.n_cg;
+    t.box_bytes = (uint32_t)t.CS * cg * (uint32_t)sizeof(float2);
+    t.buf_elems = (uint32_t)((t.CS * cg + 15) & ~15);
+    return true;
+}
+
+size_t tma_interp_smem_bytes(const TmaWin &t) { return 2 * (size_t)t.buf_elems * sizeof(float2); }
+
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+cudaError_t launch_interp2d_tma(const InterpArgs &a, const TmaWin &t, const CUtensorMap &map, int coil_group,
+                                int threads, uint32_t *status, cudaStream_t s) {
+    if (t.n_items == 0) return cudaSuccess;
+    const size_t smem = tma_interp_smem_bytes(t);
+    cudaError_t err = cudaSuccess;
+    GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
+        auto kern = k_interp2d_tma<WT, CG>;
+        err = set_smem(kern, smem);
+        int per_sm = 0;
+        if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+        if (err == cudaSuccess) {
+            const int64_t blocks = std::min<int64_t>(t.n_items, (int64_t)std::max(per_sm, 1) * sm_count());
+            kern<<<(unsigned)blocks, threads, smem, s>>>(a, map, t, status);
+            err = cudaGetLastError();
+        }
+    }));
     return err;
 }
 

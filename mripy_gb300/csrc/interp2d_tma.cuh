@@ -1,0 +1,254 @@
+// 2-D interp with grid windows staged by TMA (the forward direction's hot kernel).
+//
+// Persistent blocks walk the work items (interp subproblem x coil group) with a stride of
+// the grid size.  Each item needs the window of its home bin: (tile + W - 1) cells per
+// dimension around the bin, CG coils.  For bins whose window lies inside the grid one
+// elected thread loads it with a single 3-D tensor copy (cp.async.bulk.tensor: box
+// BY x BX x CG of 8-byte cells, y innermost) that completes on an mbarrier; windows that
+// wrap around the periodic grid edge are gathered by all threads with ordinary loads.
+// Two window buffers alternate, and the copy for item k + 2 is issued as soon as item k's
+// buffer is released, so a block computes on one window while the next is in flight.
+//
+// Shared-memory layout per buffer: [coil][x][y] with row pitch BY and coil stride
+// CS = BX * BY, exactly the order the tensor copy writes.  BX, BY are chosen on the host
+// so that a warp's reads (CG coils x 32/CG consecutive y cells) fall on distinct banks.
+// The box's inner extent BY is even and its y start is rounded down to an even cell
+// (16-byte boundary), so the window may start one cell into the row (off1).
+//
+// Every mbarrier wait is bounded: after kTmaWaitLimit polls the block records
+// kStatusTmaTimeout in the plan's status word (read by gbn_plan_status) and goes on, so
+// no launch can hang.  The sample loop is the k_interp2d one (warp per sample, lanes =
+// coils x tap slots, per-slot sums of wx * G, y weights applied once).
+#pragma once
+
+#include <cuda.h>
+
+#include "grid2d_kernels.cuh"
+
+namespace gbn {
+
+constexpr uint32_t kTmaWaitLimit = 1u << 24;  // mbarrier probes before a wait gives up
+constexpr uint32_t kStatusTmaTimeout = 2u;    // status-word bit: a bounded wait gave up
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// non-blocking probe: has the phase with the given parity completed?
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait for the phase with the given parity to complete: at most kTmaWaitLimit
+// probes with a short sleep between them (well under a second in all)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kTmaWaitLimit; ++i) {
+        if (mbar_test_wait(bar, parity)) return true;
+        if (i >= 32) __nanosleep(32);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// order this thread's earlier generic-proxy shared-memory accesses before async-proxy ones
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
+struct TmaItem {
+    int4 sub;
+    int grp, cg0, o0, o1, ws0, ws1, ys;
+    bool tma;  // the window lies inside the grid: one box copy
+};
+
+template <int CG>
+__device__ __forceinline__ TmaItem tma_item(const InterpArgs &a, const TmaWin &t, int64_t item) {
+    const Geom &g = a.g;
+    TmaItem r;
+    const int64_t si = item / t.n_cg;
+    r.cg0 = (int)(item - si * t.n_cg) * CG;
+    r.sub = a.subs[si];
+    r.grp = r.sub.x / g.ntiles;
+    const int tile = r.sub.x % g.ntiles;
+    r.o0 = (tile / g.ntile[1]) * g.tile[0];
+    r.o1 = (tile % g.ntile[1]) * g.tile[1];
+    r.ws0 = r.o0 - (g.ns - 1);
+    r.ws1 = r.o1 - (g.ns - 1);
+    r.ys = r.ws1 - (r.ws1 & 1);  // even y start (16-byte boundary); used only when ws1 >= 0
+    r.tma = r.ws0 >= 0 && r.ws0 + t.BX <= g.nf[0] && r.ws1 >= 0 && r.ys + t.BY <= g.nf[1];
+    return r;
+}
+
+template <int CG>
+__device__ __forceinline__ void tma_issue(const InterpArgs &a, const TmaWin &t, const CUtensorMap *map,
+                                          const TmaItem &it, float2 *buf, uint64_t *bar) {
+    fence_proxy_async_smem();  // the buffer's previous readers are ordered before the copy
+    mbar_arrive_expect_tx(bar, t.box_bytes);
+    tma_load_3d(buf, map, it.ys, it.ws0, it.grp * a.g.n_coil + it.cg0, bar);
+}
+
+template <int WT, int CG>
+__global__ void __launch_bounds__(512) k_interp2d_tma(InterpArgs a, const __grid_constant__ CUtensorMap map,
+                                                      TmaWin t, uint32_t *status) {
+    using L = Lanes2D<WT, CG>;
+    extern __shared__ __align__(128) float4 smem_t2[];
+    float2 *bufs = reinterpret_cast<float2 *>(smem_t2);  // [2][buf_elems]
+    __shared__ __align__(8) uint64_t bar[2];
+    const Geom &g = a.g;
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+    const int WX = g.tile[0] + W - 1, WY = g.tile[1] + W - 1;
+    const int nf0 = g.nf[0], nf1 = g.nf[1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const int kk = lane & 15;
+    const float beta = lane < 16 ? g.beta2[0] : g.beta2[1];
+    const int64_t stride = gridDim.x;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+        // prologue: the first two items of this block, where a box copy serves them
+        for (int b = 0; b < 2; ++b) {
+            const int64_t item = blockIdx.x + b * stride;
+            if (item < t.n_items) {
+                const TmaItem it = tma_item<CG>(a, t, item);
+                if (it.tma) tma_issue<CG>(a, t, &map, it, bufs + (size_t)b * t.buf_elems, &bar[b]);
+            }
+        }
+    }
+    __syncthreads();
+
+    uint32_t parity0 = 0u, parity1 = 0u;  // phase parity expected next on each buffer's barrier
+    int k = 0;
+    for (int64_t item = blockIdx.x; item < t.n_items; item += stride, ++k) {
+        const int b = k & 1;
+        float2 *win = bufs + (size_t)b * t.buf_elems;
+        const TmaItem it = tma_item<CG>(a, t, item);
+        int off1 = 0;
+        if (it.tma) {
+            if (!mbar_wait_bounded(&bar[b], b ? parity1 : parity0) && lane == 0) atomicOr(status, kStatusTmaTimeout);
+            if (b) parity1 ^= 1u;
+            else parity0 ^= 1u;
+            off1 = it.ws1 - it.ys;
+        } else {
+            // the window wraps: gather it with periodic indices, y fastest (coalesced)
+            const float2 *base = a.grid + ((int64_t)it.grp * g.n_coil + it.cg0) * g.G;
+            const int n = CG * WX * WY;
+            const float rWY = 1.f / (float)WY, rWX = 1.f / (float)WX;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int row = div_small(i, rWY), wy = i - row * WY;
+                const int cc = div_small(row, rWX), wx = row - cc * WX;
+                const int gx = wrap_fast(it.ws0 + wx, nf0), gy = wrap_fast(it.ws1 + wy, nf1);
+                win[cc * t.CS + wx * t.BY + wy] = (it.cg0 + cc < g.n_coil)
+                                                      ? base[(int64_t)cc * g.G + (int64_t)gx * nf1 + gy]
+                                                      : make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+        }
+
+        const int4 sub = it.sub;
+        float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t j_next = 0;
+        if (warp < sub.z) {
+            p_next = a.pts[(int64_t)sub.y + warp];
+            j_next = a.idx[(int64_t)sub.y + warp];
+        }
+        for (int s = warp; s < sub.z; s += nw) {
+            const float4 p = p_next;
+            const uint32_t j = j_next;
+            if (s + nw < sub.z) {
+                p_next = a.pts[(int64_t)sub.y + s + nw];
+                j_next = a.idx[(int64_t)sub.y + s + nw];
+            }
+            int c0x, c0y, c0z;
+            unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
+            int ccx = c0x + ns - 1, ccy = c0y + ns - 1;
+            ccx -= ccx >= nf0 ? nf0 : 0;
+            ccy -= ccy >= nf1 ? nf1 : 0;
+            const int rel0 = ccx - it.o0, rel1 = ccy - it.o1;
+            float myw = 0.f;
+            if (kk < W) {
+                const float d = (lane < 16 ? p.x : p.y) + (float)(ns - 1 - kk);
+                myw = exp2f(-beta * d * d);
+            }
+            float wy[L::KT];
+#pragma unroll
+            for (int tt = 0; tt < L::KT; ++tt) {
+                const int ky = q + tt * L::NQ;
+                const float v = __shfl_sync(0xffffffffu, myw, 16 + (ky < 16 ? ky : 15));
+                wy[tt] = ky < W ? v : 0.f;
+            }
+            float2 acc[L::KT];
+#pragma unroll
+            for (int tt = 0; tt < L::KT; ++tt) acc[tt] = make_float2(0.f, 0.f);
+            const float2 *rowbase = win + c * t.CS + rel0 * t.BY + rel1 + off1;
+#pragma unroll
+            for (int kx = 0; kx < L::WMAX; ++kx) {
+                if (WT == 0 && kx >= W) break;
+                const float wx = __shfl_sync(0xffffffffu, myw, kx);
+                const float2 wx2 = make_float2(wx, wx);
+                const float2 *row = rowbase + kx * t.BY;
+#pragma unroll
+                for (int tt = 0; tt < L::KT; ++tt) {
+                    const int ky = q + tt * L::NQ;
+                    if (ky < W) acc[tt] = __ffma2_rn(wx2, row[ky], acc[tt]);
+                }
+            }
+            float ax = 0.f, ay = 0.f;
+#pragma unroll
+            for (int tt = 0; tt < L::KT; ++tt) {
+                ax = fmaf(wy[tt], acc[tt].x, ax);
+                ay = fmaf(wy[tt], acc[tt].y, ay);
+            }
+#pragma unroll
+            for (int off = CG; off < 32; off <<= 1) {
+                ax += __shfl_xor_sync(0xffffffffu, ax, off);
+                ay += __shfl_xor_sync(0xffffffffu, ay, off);
+            }
+            if (q == 0 && it.cg0 + c < g.n_coil) {
+                const float sc = a.weight ? a.weight[j] : 1.f;
+                a.c[(int64_t)j * a.c_elem + (int64_t)(it.cg0 + c) * a.c_coil] = make_float2(ax * sc, ay * sc);
+            }
+        }
+        __syncthreads();  // every read of this buffer is done: it can be refilled
+        if (threadIdx.x == 0) {
+            const int64_t next = item + 2 * stride;
+            if (next < t.n_items) {
+                const TmaItem nt = tma_item<CG>(a, t, next);
+                if (nt.tma) tma_issue<CG>(a, t, &map, nt, win, &bar[b]);
+            }
+        }
+    }
+}
+
+}  // namespace gbn

@@ -51,7 +51,7 @@ class Tuning:
     """Kernel tiling chosen by the autotuner (0 = library default)."""
 
     def __init__(self, spread_tile=(0, 0, 0), interp_tile=(0, 0, 0), max_subproblem=0, coil_group=0, threads=0,
-                 interp_threads=0, interp_coil_group=0):
+                 interp_threads=0, interp_coil_group=0, interp_staging=0):
         self.spread_tile = tuple(spread_tile) + (0,) * (3 - len(spread_tile))
         self.interp_tile = tuple(interp_tile) + (0,) * (3 - len(interp_tile))
         self.max_subproblem = max_subproblem
@@ -59,16 +59,17 @@ class Tuning:
         self.threads = threads
         self.interp_threads = interp_threads
         self.interp_coil_group = interp_coil_group
+        self.interp_staging = interp_staging  # 2-D: 0 tensor copies (TMA) where possible, 1 thread loads
 
     def key(self):
         return (self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
-                self.interp_threads, self.interp_coil_group)
+                self.interp_threads, self.interp_coil_group, self.interp_staging)
 
     def __repr__(self):
         return ("Tuning(spread_tile=%s, interp_tile=%s, max_subproblem=%d, coil_group=%d, threads=%d, "
-                "interp_threads=%d, interp_coil_group=%d)" % (
+                "interp_threads=%d, interp_coil_group=%d, interp_staging=%d)" % (
                     self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
-                    self.interp_threads, self.interp_coil_group))
+                    self.interp_threads, self.interp_coil_group, self.interp_staging))
 
 
 class Graph:
@@ -126,6 +127,7 @@ class NufftPlan:
         d.threads = int(self.tuning.threads)
         d.interp_threads = int(self.tuning.interp_threads)
         d.interp_coil_group = int(self.tuning.interp_coil_group)
+        d.interp_staging = int(self.tuning.interp_staging)
         self._lib = N.lib()
         h = ctypes.c_void_p()
         N.check(self._lib.gbn_plan_create(ctypes.byref(d), ctypes.byref(h)))
@@ -157,6 +159,10 @@ class NufftPlan:
             "threads": inf.threads, "interp_threads": inf.interp_threads, "max_subproblem": inf.max_subproblem,
             "device_bytes": inf.device_bytes, "interp_coil_group": inf.interp_coil_group,
         }
+
+    def status(self, stream=None):
+        """Synchronise and raise GbnError(GBN_ERR_TIMEOUT) if a kernel's bounded wait gave up."""
+        N.check(self._lib.gbn_plan_status(self._h, _stream(stream)))
 
     def grid(self):
         """The plan's oversampled grid buffer as a (n_traj*n_coil, *nf) complex64 view."""
