@@ -75,6 +75,9 @@ typedef struct {
                                   group that pads the coil count least) */
     int32_t interp_staging;    /* 2-D interp windows: 0 = tensor-memory-access copies
                                   where the grid allows (default), 1 = thread loads */
+    int32_t dense_tile_samples; /* 3-D spread: tiles with at least this many samples (the
+                                   k-space centre of radial data) accumulate with Kahan-
+                                   compensated FP32 sums; 0 = 32768, negative = never */
 } gbn_plan_desc;
 
 typedef struct {
@@ -95,6 +98,7 @@ typedef struct {
     int32_t max_subproblem;
     int64_t device_bytes;   /* device memory held by the plan */
     int32_t interp_coil_group;
+    int64_t dense_subproblems; /* spread subproblems with compensated accumulation */
 } gbn_plan_info;
 
 /* element strides (in complex64 elements) of a strided complex array */

@@ -40,7 +40,7 @@ class PlanDesc(ctypes.Structure):
         ("spread_tile", ctypes.c_int32 * 3), ("interp_tile", ctypes.c_int32 * 3),
         ("max_subproblem", ctypes.c_int32), ("coil_group", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("interp_threads", ctypes.c_int32), ("interp_coil_group", ctypes.c_int32),
-        ("interp_staging", ctypes.c_int32),
+        ("interp_staging", ctypes.c_int32), ("dense_tile_samples", ctypes.c_int32),
     ]
 
 
@@ -52,7 +52,7 @@ class PlanInfo(ctypes.Structure):
         ("spread_entries", ctypes.c_int64), ("spread_tile", ctypes.c_int32 * 3),
         ("interp_tile", ctypes.c_int32 * 3), ("coil_group", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("interp_threads", ctypes.c_int32), ("max_subproblem", ctypes.c_int32), ("device_bytes", ctypes.c_int64),
-        ("interp_coil_group", ctypes.c_int32),
+        ("interp_coil_group", ctypes.c_int32), ("dense_subproblems", ctypes.c_int64),
     ]
 
 

@@ -82,6 +82,8 @@ struct gbn_plan {
     Geom gs{}, gi{};
     int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256, interp_coil_group = 0;
     int interp_staging = 0;  // 0: tensor copies where the grid allows, 1: thread loads
+    int dense_min = kDenseDefault;  // 3-D spread tiles with this many samples use compensated sums (0: never)
+    int64_t n_dense_sub = 0;
     int64_t G = 1, n_inst = 1;
     size_t device_bytes = 0;
     int smem_optin = 0;
@@ -236,6 +238,7 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
     a.c_coil = L.coil_stride;
     a.weight = weight;
     a.grid = grid;
+    a.any_dense = p->n_dense_sub > 0 ? 1 : 0;
     int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
     while (cg > 1 && spread_smem_bytes(p->gs, cg) > smem_budget(p)) cg /= 2;
     if (spread_smem_bytes(p->gs, cg) > (size_t)p->smem_optin)
@@ -351,7 +354,7 @@ int key_bits(uint64_t max_key) {
 
 // count -> tile offsets (exclusive), subproblem table
 int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, DevBuf &subs, int every_tile,
-               int64_t *n_sub_out, cudaStream_t s) {
+               uint32_t dense_min, uint32_t *n_dense, int64_t *n_sub_out, cudaStream_t s) {
     const int64_t T = (int64_t)g.ntiles * g.n_traj;
     GBN_TRY(ensure(p, tile_off, sizeof(uint32_t) * T));
     GBN_TRY(ensure(p, p->nsub, sizeof(uint32_t) * T));
@@ -373,7 +376,7 @@ int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, De
     const int64_t n_sub = (int64_t)last[0] + last[1];
     if (n_sub > 0x7FFFFFFF) return fail(GBN_ERR_CAPACITY, "too many subproblems");
     GBN_TRY(ensure(p, subs, sizeof(int4) * (size_t)std::max<int64_t>(n_sub, 1)));
-    GBN_CUDA(launch_build_subs(count, toff, soff, T, p->max_sub, every_tile, subs.as<int4>(), s));
+    GBN_CUDA(launch_build_subs(count, toff, soff, T, p->max_sub, every_tile, dense_min, n_dense, subs.as<int4>(), s));
     *n_sub_out = n_sub;
     return GBN_OK;
 }
@@ -479,9 +482,19 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
         }));
         GBN_CUDA(launch_gather_pts(p->pts.as<float4>(), vout, M, p->home_pts.as<float4>(), s));
     }
-    GBN_TRY(build_subs(p, p->gs, scount, p->spread_tile_off, p->spread_subs, 1, &p->n_spread_sub, s));
-    GBN_TRY(build_subs(p, p->gi, home_count, p->home_tile_off, p->interp_subs, 0, &p->n_interp_sub, s));
+    // 3-D: spread tiles with at least dense_min samples (the k-space centre of radial
+    // trajectories) accumulate with compensated sums; their subproblem count lands in
+    // the second status word
+    const uint32_t dense_min = p->dim == 3 && p->dense_min > 0 ? (uint32_t)p->dense_min : 0u;
+    GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, sizeof(uint32_t), s));
+    GBN_TRY(build_subs(p, p->gs, scount, p->spread_tile_off, p->spread_subs, 1, dense_min, p->kstatus + 1,
+                       &p->n_spread_sub, s));
+    GBN_TRY(build_subs(p, p->gi, home_count, p->home_tile_off, p->interp_subs, 0, 0u, nullptr, &p->n_interp_sub,
+                       s));
+    uint32_t n_dense = 0;
+    GBN_CUDA(cudaMemcpyAsync(&n_dense, p->kstatus + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     GBN_CUDA(cudaStreamSynchronize(s));
+    p->n_dense_sub = n_dense;
     p->points_set = true;
     return GBN_OK;
 }
@@ -551,6 +564,8 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         return fail(GBN_ERR_ARG, "interp_staging must be 0 or 1");
     }
     p->interp_staging = desc->interp_staging;
+    p->dense_min = desc->dense_tile_samples > 0 ? desc->dense_tile_samples
+                                                : (desc->dense_tile_samples < 0 ? 0 : kDenseDefault);
     p->threads = desc->threads > 0 ? desc->threads : 256;
     p->interp_threads = desc->interp_threads > 0 ? desc->interp_threads : (p->dim == 2 ? 512 : 256);
     for (int t : {p->threads, p->interp_threads}) {
@@ -614,13 +629,14 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         }
         p->device_bytes += sizeof(float) * p->m[d];
     }
-    e = cudaMalloc((void **)&p->kstatus, sizeof(uint32_t));
+    // word 0: kernel status bits; word 1: dense spread subproblems (written by set_points)
+    e = cudaMalloc((void **)&p->kstatus, 2 * sizeof(uint32_t));
     if (e != cudaSuccess) {
         cudaGetLastError();
         p->kstatus = nullptr;
         return bail(fail(GBN_ERR_ALLOC, "status word allocation failed"));
     }
-    e = cudaMemset(p->kstatus, 0, sizeof(uint32_t));
+    e = cudaMemset(p->kstatus, 0, 2 * sizeof(uint32_t));
     if (e == cudaSuccess) e = launch_build_tables(p->dim, p->m, p->nf, p->tau, p->tab[0], p->tab[1], p->tab[2], 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return bail(fail(GBN_ERR_CUDA, std::string("table build: ") + cudaGetErrorString(e)));
@@ -731,6 +747,7 @@ int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     o->interp_threads = p->interp_threads;
     o->max_subproblem = p->max_sub;
     o->interp_coil_group = interp_cg(p);
+    o->dense_subproblems = p->n_dense_sub;
     o->device_bytes = (int64_t)p->device_bytes;
     return GBN_OK;
 }

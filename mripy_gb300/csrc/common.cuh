@@ -21,6 +21,11 @@ namespace gbn {
 constexpr int kMaxW = 40;          // 2*nspread; nspread <= 20 (eps down to 1e-33 in 2-D gives 17)
 constexpr int kSplitFlag = 1;      // tile is covered by more than one subproblem
 constexpr int kFirstFlag = 2;      // first subproblem of its tile
+constexpr int kDenseFlag = 4;      // tile above the dense-sample threshold: compensated sums
+// default dense threshold (samples per 3-D spread tile).  Measured on GB300 for the 8-coil
+// 20000 x 128 centre-out radial workload: 32768 flags 10% of the work items and costs 8% of
+// the spread time; 2048 flags 41% and costs 27%.
+constexpr int kDenseDefault = 32768;
 
 struct Geom {
     int dim;
@@ -90,9 +95,11 @@ cudaError_t launch_dup_keys(const float4 *pts, int64_t M, const int64_t *d_traj_
                             uint32_t *tile_count, cudaStream_t s);
 cudaError_t launch_gather_pts(const float4 *pts, const uint32_t *idx, int64_t n, float4 *out,
                               cudaStream_t s);
+// dense_min > 0: subproblems of tiles with at least dense_min samples get kDenseFlag and
+// are counted into *n_dense (may be null)
 cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
-                              int64_t ntiles_total, int max_sub, int every_tile, int4 *subs,
-                              cudaStream_t s);
+                              int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min,
+                              uint32_t *n_dense, int4 *subs, cudaStream_t s);
 cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int every_tile,
                               uint32_t *n_sub, cudaStream_t s);
 
@@ -106,6 +113,7 @@ struct SpreadArgs {
     int64_t c_elem, c_coil;   // strides (complex elements)
     const float *weight;      // per sample (original index) or null: density compensation
     float2 *grid;
+    int any_dense;            // some subproblems carry kDenseFlag (compensated accumulation)
 };
 struct InterpArgs {
     Geom g;

@@ -283,11 +283,31 @@ __global__ void __launch_bounds__(256) k_spread3d(SpreadArgs a) {
 // warps gather the coil values.  Per listed sample a warp loads its plane weight, its 4
 // row weights and its 4 column weights, folds the plane and column weights into the coil
 // value (10 multiplies) and issues 16 packed FMAs.
-template <int WT, int CG>
+//
+// KAHAN: the instance for the subproblems flagged kDenseFlag (tiles above the dense-sample
+// threshold: the k-space centre of radial data, where a cell sums thousands of terms).
+// Blocked Kahan summation: each staged batch (32 samples) accumulates plainly into a
+// register partial, and the partial is added once per batch to the cell's total with a
+// compensation term (the low-order part lost by that addition is carried into the next
+// one); the flush writes total - compensation.  The rounding error then grows with the
+// batch length rather than the tile's sample count, at 16 compensated additions per
+// lane per batch.  The plain instance skips dense subproblems and the Kahan instance the
+// others, so the two launches together cover every subproblem once.
+__device__ __forceinline__ void kahan_add(float2 &s, float2 &cmp, float2 v) {
+    const float yx = v.x - cmp.x, yy = v.y - cmp.y;
+    const float tx = s.x + yx, ty = s.y + yy;
+    cmp.x = (tx - s.x) - yx;
+    cmp.y = (ty - s.y) - yy;
+    s.x = tx;
+    s.y = ty;
+}
+
+template <int WT, int CG, bool KAHAN>
 __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
     constexpr int NQ = 32 / CG;
     constexpr int B = kRegBatch;
     extern __shared__ float4 smem_r3[];
+    if (((a.subs[blockIdx.x].w & kDenseFlag) != 0) != KAHAN) return;  // the other launch's subproblem
     const Geom &g = a.g;
     const int TX = g.tile[0], TY = g.tile[1], TZ = g.tile[2];
     // per staged sample: y rows [0, TY), z columns [TY, TY + TZ) as [q][k], x planes after
@@ -312,10 +332,21 @@ __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
     const int rho0 = warp * kRegRows;
     const int xw = rho0 / TY, y0 = rho0 - xw * TY;
     float2 acc[kRegRows][kRegCols];
+    // Kahan instance: compensated totals and their compensation terms
+    float2 tot[KAHAN ? kRegRows : 1][KAHAN ? kRegCols : 1], cmp[KAHAN ? kRegRows : 1][KAHAN ? kRegCols : 1];
 #pragma unroll
     for (int r = 0; r < kRegRows; ++r)
 #pragma unroll
         for (int k = 0; k < kRegCols; ++k) acc[r][k] = make_float2(0.f, 0.f);
+    if constexpr (KAHAN) {
+#pragma unroll
+        for (int r = 0; r < kRegRows; ++r)
+#pragma unroll
+            for (int k = 0; k < kRegCols; ++k) {
+                tot[r][k] = make_float2(0.f, 0.f);
+                cmp[r][k] = make_float2(0.f, 0.f);
+            }
+    }
 
     for (int base = 0, buf = 0; base < sub.z; base += B, buf ^= 1) {
         const int n = min(B, sub.z - base);
@@ -409,6 +440,23 @@ __global__ void __launch_bounds__(256) k_spread3d_reg(SpreadArgs a) {
                 for (int k = 0; k < kRegCols; ++k) acc[rr][k] = __ffma2_rn(wy2, u[k], acc[rr][k]);
             }
         }
+        if constexpr (KAHAN) {
+            // fold this batch's partial sums into the compensated totals
+#pragma unroll
+            for (int rr = 0; rr < kRegRows; ++rr)
+#pragma unroll
+                for (int k = 0; k < kRegCols; ++k) {
+                    kahan_add(tot[rr][k], cmp[rr][k], acc[rr][k]);
+                    acc[rr][k] = make_float2(0.f, 0.f);
+                }
+        }
+    }
+    if constexpr (KAHAN) {
+#pragma unroll
+        for (int rr = 0; rr < kRegRows; ++rr)
+#pragma unroll
+            for (int k = 0; k < kRegCols; ++k)
+                acc[rr][k] = make_float2(tot[rr][k].x - cmp[rr][k].x, tot[rr][k].y - cmp[rr][k].y);
     }
 
     if (cg0 + c >= g.n_coil || xw >= e[0]) return;

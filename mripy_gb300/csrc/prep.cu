@@ -143,17 +143,19 @@ __global__ void k_count_subs(const uint32_t *__restrict__ count, int64_t n, int 
 
 __global__ void k_build_subs(const uint32_t *__restrict__ count, const uint32_t *__restrict__ tile_off,
                              const uint32_t *__restrict__ sub_off, int64_t n, int max_sub, int every_tile,
-                             int4 *__restrict__ subs) {
+                             uint32_t dense_min, uint32_t *__restrict__ n_dense, int4 *__restrict__ subs) {
     int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= n) return;
     uint32_t c = count[t];
     uint32_t s = (c + (uint32_t)max_sub - 1) / (uint32_t)max_sub;
     if (every_tile && s == 0) s = 1;
     uint32_t o = sub_off[t];
+    const bool dense = dense_min > 0 && c >= dense_min;
+    if (dense && n_dense) atomicAdd(n_dense, s);
     for (uint32_t k = 0; k < s; ++k) {
         uint32_t start = k * (uint32_t)max_sub;
         uint32_t len = c > start ? min((uint32_t)max_sub, c - start) : 0u;
-        int flags = (s > 1 ? kSplitFlag : 0) | (k == 0 ? kFirstFlag : 0);
+        int flags = (s > 1 ? kSplitFlag : 0) | (k == 0 ? kFirstFlag : 0) | (dense ? kDenseFlag : 0);
         subs[o + k] = make_int4((int)t, (int)(tile_off[t] + start), (int)len, flags);
     }
 }
@@ -204,10 +206,11 @@ cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int
 }
 
 cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
-                              int64_t ntiles_total, int max_sub, int every_tile, int4 *subs, cudaStream_t s) {
+                              int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min,
+                              uint32_t *n_dense, int4 *subs, cudaStream_t s) {
     if (ntiles_total == 0) return cudaSuccess;
     k_build_subs<<<blocks_for(ntiles_total, 256), 256, 0, s>>>(count, tile_off, sub_off, ntiles_total, max_sub,
-                                                               every_tile, subs);
+                                                               every_tile, dense_min, n_dense, subs);
     return cudaGetLastError();
 }
 

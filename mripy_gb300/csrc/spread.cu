@@ -64,12 +64,15 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
     if (grid3d_applies(a.g) && (coil_group == 4 || coil_group == 8) && threads <= 256 &&
         a.g.tile[1] % kRegRows == 0 && a.g.tile[0] * a.g.tile[1] == kRegRows * (threads / 32) &&
         a.g.tile[2] == kRegCols * (32 / coil_group)) {
+        // plain sums for ordinary tiles, then (if any) Kahan-compensated sums for dense ones
         const size_t rsmem = spread3d_reg_smem_bytes(a.g, coil_group);
         GBN_DISPATCH_W(a.g.W, {
             if (coil_group == 8) {
-                k_spread3d_reg<WT, 8><<<grid, threads, rsmem, s>>>(a);
+                k_spread3d_reg<WT, 8, false><<<grid, threads, rsmem, s>>>(a);
+                if (a.any_dense) k_spread3d_reg<WT, 8, true><<<grid, threads, rsmem, s>>>(a);
             } else {
-                k_spread3d_reg<WT, 4><<<grid, threads, rsmem, s>>>(a);
+                k_spread3d_reg<WT, 4, false><<<grid, threads, rsmem, s>>>(a);
+                if (a.any_dense) k_spread3d_reg<WT, 4, true><<<grid, threads, rsmem, s>>>(a);
             }
             err = cudaGetLastError();
         });

@@ -96,7 +96,9 @@ class Graph:
 
 class NufftPlan:
     def __init__(self, dim, shape, n_coil=1, n_traj=1, eps=1e-15, iflag=1, df=1.0, max_nspread=None,
-                 tuning=None):
+                 tuning=None, dense_tile_samples=0):
+        """dense_tile_samples (3-D): spread tiles with at least this many samples accumulate
+        with Kahan-compensated FP32 sums; 0 = library default (32768), negative = never."""
         shape = tuple(int(s) for s in shape)
         if len(shape) != dim:
             raise ValueError("shape must have %d entries" % dim)
@@ -128,6 +130,7 @@ class NufftPlan:
         d.interp_threads = int(self.tuning.interp_threads)
         d.interp_coil_group = int(self.tuning.interp_coil_group)
         d.interp_staging = int(self.tuning.interp_staging)
+        d.dense_tile_samples = int(dense_tile_samples)
         self._lib = N.lib()
         h = ctypes.c_void_p()
         N.check(self._lib.gbn_plan_create(ctypes.byref(d), ctypes.byref(h)))
@@ -158,6 +161,7 @@ class NufftPlan:
             "interp_tile": tuple(inf.interp_tile[:self.dim]), "coil_group": inf.coil_group,
             "threads": inf.threads, "interp_threads": inf.interp_threads, "max_subproblem": inf.max_subproblem,
             "device_bytes": inf.device_bytes, "interp_coil_group": inf.interp_coil_group,
+            "dense_subproblems": inf.dense_subproblems,
         }
 
     def status(self, stream=None):
