@@ -14,7 +14,10 @@ replayed from one CUDA graph; value = (samples x coils) / step time.  Also repor
   e2e          the same step through the C ABI with pinned host buffers, H2D and D2H inside
                the timed region (gbn_type2_host + gbn_type1_host)
   roofline     dominant gridding kernel: algorithmic bytes / its CUDA-event time vs the
-               measured HBM copy bandwidth, with the FP32 rate beside it
+               measured HBM copy bandwidth, with the FP32 rate beside it; "binding" gives
+               the fraction of the resource that bounds the kernel (HBM, FP32 or shared memory)
+  tiling       tiles, threads and coils per block, chosen by the autotuner on the
+               workload's trajectory before the timed region (--tune off: library defaults)
   cpu_baseline the FP64 C restatement of mripy's CPU NUFFT on the host cores
   accuracy     relative L2 error vs the FP64 NUDFT on a subset
   solver       c2: 20 CG-SENSE iterations through the graph-captured normal operator
@@ -265,7 +268,7 @@ def run_gpu(args, wl):
         from mripy_gb300.tune import autotune
         t0 = time.perf_counter()
         tuning = autotune(wl.dim, wl.shape, coords, n_coil=n_coil, n_traj=wl.n_traj, traj_offsets=wl.offsets,
-                          eps=wl.eps)
+                          eps=wl.eps, cache_file=args.tune_cache)
         tune_s = time.perf_counter() - t0
     plan = NufftPlan(wl.dim, wl.shape, n_coil=n_coil, n_traj=wl.n_traj, eps=wl.eps, max_nspread=wl.max_nspread,
                      tuning=tuning)
@@ -570,6 +573,9 @@ def main():
     ap.add_argument("--tune", default="auto", choices=["auto", "off"],
                     help="auto: the autotuner picks tiles / threads / coils per block on the workload's "
                          "trajectory before the timed region; off: library defaults")
+    ap.add_argument("--tune-cache", default=None,
+                    help="JSON file of autotuner results: read if it holds this workload's key, else "
+                         "written; lets a profiler run reuse the tiling of an earlier run")
     args = ap.parse_args()
     if args.impl == "gb300":
         args.warmup = max(args.warmup, 3)

@@ -84,6 +84,7 @@ struct gbn_plan {
     int interp_staging = 0;  // 0: tensor copies where the grid allows, 1: thread loads
     int dense_min = kDenseDefault;  // 3-D spread tiles with this many samples use compensated sums (0: never)
     int64_t n_dense_sub = 0;
+    int64_t n_split = 0;  // spread tiles covered by more than one subproblem (listed in split_tiles)
     int64_t G = 1, n_inst = 1;
     size_t device_bytes = 0;
     int smem_optin = 0;
@@ -107,7 +108,7 @@ struct gbn_plan {
     DevBuf traj_off_d, grp_scale, pts, home_key, home_keys_sorted, touch_count, touch_off, home_count,
         iota, home_idx, home_pts, dup_keys, dup_vals, dup_keys_sorted, dup_idx, dup_pts, spread_count,
         spread_tile_off, home_tile_off, nsub, sub_off, spread_subs, interp_subs, cub_tmp, scratch,
-        stage_in, stage_out, stage_w;
+        stage_in, stage_out, stage_w, split_tiles;
     int64_t n_dup = 0, n_spread_sub = 0, n_interp_sub = 0;
 };
 
@@ -227,7 +228,7 @@ int dir_type1(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_FORWARD : 
 int dir_type2(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_INVERSE : GBN_FFT_FORWARD; }
 
 int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, float2 *grid, cudaStream_t s) {
-    GBN_CUDA(launch_zero_split(p->gs, p->spread_subs.as<int4>(), p->n_spread_sub, grid, s));
+    GBN_CUDA(launch_zero_split(p->gs, p->split_tiles.as<uint32_t>(), p->n_split, grid, s));
     SpreadArgs a;
     a.g = p->gs;
     a.subs = p->spread_subs.as<int4>();
@@ -354,7 +355,8 @@ int key_bits(uint64_t max_key) {
 
 // count -> tile offsets (exclusive), subproblem table
 int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, DevBuf &subs, int every_tile,
-               uint32_t dense_min, uint32_t *n_dense, int64_t *n_sub_out, cudaStream_t s) {
+               uint32_t dense_min, uint32_t *n_dense, uint32_t *split_list, uint32_t *n_split, int64_t *n_sub_out,
+               cudaStream_t s) {
     const int64_t T = (int64_t)g.ntiles * g.n_traj;
     GBN_TRY(ensure(p, tile_off, sizeof(uint32_t) * T));
     GBN_TRY(ensure(p, p->nsub, sizeof(uint32_t) * T));
@@ -376,7 +378,8 @@ int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, De
     const int64_t n_sub = (int64_t)last[0] + last[1];
     if (n_sub > 0x7FFFFFFF) return fail(GBN_ERR_CAPACITY, "too many subproblems");
     GBN_TRY(ensure(p, subs, sizeof(int4) * (size_t)std::max<int64_t>(n_sub, 1)));
-    GBN_CUDA(launch_build_subs(count, toff, soff, T, p->max_sub, every_tile, dense_min, n_dense, subs.as<int4>(), s));
+    GBN_CUDA(launch_build_subs(count, toff, soff, T, p->max_sub, every_tile, dense_min, n_dense, split_list, n_split,
+                               subs.as<int4>(), s));
     *n_sub_out = n_sub;
     return GBN_OK;
 }
@@ -486,15 +489,19 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
     // trajectories) accumulate with compensated sums; their subproblem count lands in
     // the second status word
     const uint32_t dense_min = p->dim == 3 && p->dense_min > 0 ? (uint32_t)p->dense_min : 0u;
-    GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, sizeof(uint32_t), s));
+    // the list of split spread tiles (zeroed before each spread) and its length in the
+    // third status word
+    GBN_TRY(ensure(p, p->split_tiles, sizeof(uint32_t) * (size_t)std::max<int64_t>(Ts, 1)));
+    GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, 2 * sizeof(uint32_t), s));
     GBN_TRY(build_subs(p, p->gs, scount, p->spread_tile_off, p->spread_subs, 1, dense_min, p->kstatus + 1,
-                       &p->n_spread_sub, s));
-    GBN_TRY(build_subs(p, p->gi, home_count, p->home_tile_off, p->interp_subs, 0, 0u, nullptr, &p->n_interp_sub,
-                       s));
-    uint32_t n_dense = 0;
-    GBN_CUDA(cudaMemcpyAsync(&n_dense, p->kstatus + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+                       p->split_tiles.as<uint32_t>(), p->kstatus + 2, &p->n_spread_sub, s));
+    GBN_TRY(build_subs(p, p->gi, home_count, p->home_tile_off, p->interp_subs, 0, 0u, nullptr, nullptr, nullptr,
+                       &p->n_interp_sub, s));
+    uint32_t counts[2] = {0, 0};
+    GBN_CUDA(cudaMemcpyAsync(counts, p->kstatus + 1, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     GBN_CUDA(cudaStreamSynchronize(s));
-    p->n_dense_sub = n_dense;
+    p->n_dense_sub = counts[0];
+    p->n_split = counts[1];
     p->points_set = true;
     return GBN_OK;
 }
@@ -629,14 +636,15 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         }
         p->device_bytes += sizeof(float) * p->m[d];
     }
-    // word 0: kernel status bits; word 1: dense spread subproblems (written by set_points)
-    e = cudaMalloc((void **)&p->kstatus, 2 * sizeof(uint32_t));
+    // word 0: kernel status bits; words 1, 2: dense spread subproblems and split spread
+    // tiles (counted by set_points)
+    e = cudaMalloc((void **)&p->kstatus, 3 * sizeof(uint32_t));
     if (e != cudaSuccess) {
         cudaGetLastError();
         p->kstatus = nullptr;
         return bail(fail(GBN_ERR_ALLOC, "status word allocation failed"));
     }
-    e = cudaMemset(p->kstatus, 0, 2 * sizeof(uint32_t));
+    e = cudaMemset(p->kstatus, 0, 3 * sizeof(uint32_t));
     if (e == cudaSuccess) e = launch_build_tables(p->dim, p->m, p->nf, p->tau, p->tab[0], p->tab[1], p->tab[2], 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return bail(fail(GBN_ERR_CUDA, std::string("table build: ") + cudaGetErrorString(e)));
@@ -709,7 +717,7 @@ int gbn_plan_destroy(gbn_plan *p) {
                       &p->dup_keys, &p->dup_vals, &p->dup_keys_sorted, &p->dup_idx, &p->dup_pts,
                       &p->spread_count, &p->spread_tile_off, &p->home_tile_off, &p->nsub, &p->sub_off,
                       &p->spread_subs, &p->interp_subs, &p->cub_tmp, &p->scratch, &p->stage_in,
-                      &p->stage_out, &p->stage_w};
+                      &p->stage_out, &p->stage_w, &p->split_tiles};
     for (DevBuf *b : bufs) release(*b);
     delete p;
     return GBN_OK;

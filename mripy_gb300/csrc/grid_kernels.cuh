@@ -156,16 +156,16 @@ __global__ void __launch_bounds__(512) k_spread(SpreadArgs a) {
     }
 }
 
-// zero the tiles that several subproblems accumulate into (first subproblem's block)
+// zero the tiles that several subproblems accumulate into: one block per (listed tile,
+// coil); the list holds only split tiles (built when the points are set)
 template <int D>
-__global__ void k_zero_split(Geom g, const int4 *__restrict__ subs, float2 *__restrict__ grid) {
-    const int4 sub = subs[blockIdx.x];
-    if (!((sub.w & kSplitFlag) && (sub.w & kFirstFlag))) return;
-    const int grp = sub.x / g.ntiles;
+__global__ void k_zero_split(Geom g, const uint32_t *__restrict__ split_tiles, float2 *__restrict__ grid) {
+    const uint32_t t = split_tiles[blockIdx.x];
+    const int grp = (int)(t / (uint32_t)g.ntiles);
     int o[3], e[3];
-    tile_coords<D>(g, sub.x % g.ntiles, o, e);
+    tile_coords<D>(g, (int)(t % (uint32_t)g.ntiles), o, e);
     const int ecell = e[0] * e[1] * e[2];
-    for (int coil = 0; coil < g.n_coil; ++coil) {
+    for (int coil = blockIdx.y; coil < g.n_coil; coil += gridDim.y) {
         float2 *dst = grid + ((int64_t)grp * g.n_coil + coil) * g.G;
         for (int i = threadIdx.x; i < ecell; i += blockDim.x) {
             const int l2 = i % e[2], l1 = (i / e[2]) % e[1], l0 = i / (e[2] * e[1]);

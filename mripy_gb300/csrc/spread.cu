@@ -23,9 +23,14 @@ size_t spread_smem_bytes(const Geom &g, int coil_group) {
     return cells * (size_t)coil_group * sizeof(float2);
 }
 
-cudaError_t launch_zero_split(const Geom &g, const int4 *subs, int64_t n_sub, float2 *grid, cudaStream_t s) {
-    if (n_sub == 0) return cudaSuccess;
-    GBN_DISPATCH_D(g.dim, (k_zero_split<D><<<(unsigned)n_sub, 256, 0, s>>>(g, subs, grid)));
+cudaError_t launch_zero_split(const Geom &g, const uint32_t *split_tiles, int64_t n_split, float2 *grid,
+                              cudaStream_t s) {
+    if (n_split == 0 || g.n_coil == 0) return cudaSuccess;
+    int cells = 1;
+    for (int d = 0; d < g.dim; ++d) cells *= g.tile[d];
+    const int th = cells >= 256 ? 256 : (cells >= 128 ? 128 : 64);
+    const dim3 blocks((unsigned)n_split, (unsigned)(g.n_coil < 65535 ? g.n_coil : 65535));
+    GBN_DISPATCH_D(g.dim, (k_zero_split<D><<<blocks, th, 0, s>>>(g, split_tiles, grid)));
     return cudaGetLastError();
 }
 
