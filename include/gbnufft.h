@@ -225,10 +225,14 @@ int gbn_spread2d_noalloc(int coord_dtype, const void *x, const void *y, int64_t 
                          void *grid, gbn_stream_t stream);
 
 /* ---- host-buffer entry points (the reference's numpy-in / numpy-out calls) ---- */
-/* One call = H2D of the inputs, the transform, D2H of the result, on the plan's
- * staging buffers (pinned host memory recommended for the caller's arrays).
- * Layouts are the reference's: image (ms, mt[, mu], n_coil) coil-last per
- * trajectory group, samples (M_total, n_coil) coil-last; complex64. */
+/* One call = inputs from host memory, the transform, the result into host memory,
+ * synchronised.  Pageable arrays go through the plan's staging buffers (H2D copy,
+ * transform, D2H copy).  Pinned (page-locked) arrays are read and written by the
+ * kernels directly over the host link where the access pattern allows (image in the
+ * pad, samples out of the interp, image out of the crop), which overlaps the transfer
+ * with the compute; the samples of type-1 are always copied in bulk (the spread reads
+ * each several times).  Layouts are the reference's: image (ms, mt[, mu], n_coil)
+ * coil-last per trajectory group, samples (M_total, n_coil) coil-last; complex64. */
 int gbn_type1_host(gbn_plan *plan, const void *h_c, void *h_img, gbn_stream_t stream);
 int gbn_type2_host(gbn_plan *plan, const void *h_img, void *h_c, gbn_stream_t stream);
 int gbn_type21_host(gbn_plan *plan, const void *h_img, void *h_out, const float *h_dcf,

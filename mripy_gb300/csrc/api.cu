@@ -962,17 +962,36 @@ static gbn_layout host_img_layout(const gbn_plan *p) {
 }
 static gbn_layout host_sample_layout(const gbn_plan *p) { return gbn_layout{0, 1, p->desc.n_coil}; }
 
+// Device address of a pinned (page-locked, mapped) host buffer, or null for pageable
+// memory.  Kernels given it read or write the host memory directly over the host link, so
+// the transfer overlaps the kernel instead of preceding or following it.
+static void *mapped_host(const void *h) {
+    if (!h) return nullptr;
+    void *d = nullptr;
+    if (cudaHostGetDevicePointer(&d, const_cast<void *>(h), 0) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return d;
+}
+
 int gbn_type1_host(gbn_plan *p, const void *h_c, void *h_img, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, true));
     if ((!h_c && p->M > 0) || !h_img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     const size_t cb = sizeof(float2) * (size_t)p->M * p->desc.n_coil, ib = sizeof(float2) * image_elems(p);
+    // the spread gathers each sample several times (once per tile its stencil reaches):
+    // the samples are copied in bulk; a pinned output image is written by the crop directly
     GBN_TRY(ensure(p, p->stage_in, cb));
-    GBN_TRY(ensure(p, p->stage_out, ib));
     GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_c, cb, cudaMemcpyHostToDevice, s));
-    GBN_TRY(gbn_type1(p, p->stage_in.p, host_sample_layout(p), nullptr, p->stage_out.p, host_img_layout(p),
-                      stream));
-    GBN_CUDA(cudaMemcpyAsync(h_img, p->stage_out.p, ib, cudaMemcpyDeviceToHost, s));
+    if (void *d_img = mapped_host(h_img)) {
+        GBN_TRY(gbn_type1(p, p->stage_in.p, host_sample_layout(p), nullptr, d_img, host_img_layout(p), stream));
+    } else {
+        GBN_TRY(ensure(p, p->stage_out, ib));
+        GBN_TRY(gbn_type1(p, p->stage_in.p, host_sample_layout(p), nullptr, p->stage_out.p, host_img_layout(p),
+                          stream));
+        GBN_CUDA(cudaMemcpyAsync(h_img, p->stage_out.p, ib, cudaMemcpyDeviceToHost, s));
+    }
     GBN_CUDA(cudaStreamSynchronize(s));
     return GBN_OK;
 }
@@ -982,11 +1001,21 @@ int gbn_type2_host(gbn_plan *p, const void *h_img, void *h_c, gbn_stream_t strea
     if ((!h_c && p->M > 0) || !h_img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     const size_t cb = sizeof(float2) * (size_t)p->M * p->desc.n_coil, ib = sizeof(float2) * image_elems(p);
-    GBN_TRY(ensure(p, p->stage_in, ib));
-    GBN_TRY(ensure(p, p->stage_out, cb));
-    GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_img, ib, cudaMemcpyHostToDevice, s));
-    GBN_TRY(gbn_type2(p, p->stage_in.p, host_img_layout(p), p->stage_out.p, host_sample_layout(p), stream));
-    GBN_CUDA(cudaMemcpyAsync(h_c, p->stage_out.p, cb, cudaMemcpyDeviceToHost, s));
+    // pinned buffers: the pad reads the image and the interp writes the samples directly
+    const void *src = mapped_host(h_img);
+    void *dst = p->M > 0 ? mapped_host(h_c) : nullptr;
+    if (!src) {
+        GBN_TRY(ensure(p, p->stage_in, ib));
+        GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_img, ib, cudaMemcpyHostToDevice, s));
+        src = p->stage_in.p;
+    }
+    if (!dst) {
+        GBN_TRY(ensure(p, p->stage_out, cb));
+        GBN_TRY(gbn_type2(p, src, host_img_layout(p), p->stage_out.p, host_sample_layout(p), stream));
+        GBN_CUDA(cudaMemcpyAsync(h_c, p->stage_out.p, cb, cudaMemcpyDeviceToHost, s));
+    } else {
+        GBN_TRY(gbn_type2(p, src, host_img_layout(p), dst, host_sample_layout(p), stream));
+    }
     GBN_CUDA(cudaStreamSynchronize(s));
     return GBN_OK;
 }
@@ -1004,9 +1033,15 @@ int gbn_type21_host(gbn_plan *p, const void *h_img, void *h_out, const float *h_
         GBN_CUDA(cudaMemcpyAsync(p->stage_w.p, h_dcf, sizeof(float) * (size_t)p->M, cudaMemcpyHostToDevice, s));
         dcf = p->stage_w.as<float>();
     }
-    GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_img, ib, cudaMemcpyHostToDevice, s));
-    GBN_TRY(gbn_type21(p, p->stage_in.p, host_img_layout(p), p->stage_out.p, host_img_layout(p), dcf, stream));
-    GBN_CUDA(cudaMemcpyAsync(h_out, p->stage_out.p, ib, cudaMemcpyDeviceToHost, s));
+    // pinned buffers: the pad reads and the crop writes them directly
+    const void *src = mapped_host(h_img);
+    void *dst = mapped_host(h_out);
+    if (!src) {
+        GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_img, ib, cudaMemcpyHostToDevice, s));
+        src = p->stage_in.p;
+    }
+    GBN_TRY(gbn_type21(p, src, host_img_layout(p), dst ? dst : p->stage_out.p, host_img_layout(p), dcf, stream));
+    if (!dst) GBN_CUDA(cudaMemcpyAsync(h_out, p->stage_out.p, ib, cudaMemcpyDeviceToHost, s));
     GBN_CUDA(cudaStreamSynchronize(s));
     return GBN_OK;
 }

@@ -347,6 +347,42 @@ def test_tma_interp_matches_thread_staging(shape, nc, eps, tile, icg):
     assert rel(k[:counts[0]], ref) < TOL_REF
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_host_entry_points_pinned_and_pageable(dim):
+    """gbn_type{1,2,21}_host give the device path's results whether the caller's arrays are
+    pageable (staged copies) or pinned (read and written by the kernels directly)."""
+    import ctypes
+    from mripy_gb300 import _native as N
+    rng = np.random.default_rng(25)
+    shape, nc, M = ((64, 48), 4, 6000) if dim == 2 else ((20, 18, 16), 4, 5000)
+    xs = rng.uniform(-np.pi, np.pi, (dim, M))
+    xs[:, :2000] *= 0.1                                          # split tiles (atomic flush)
+    p = NufftPlan(dim, shape, n_coil=nc, eps=5e-6, max_nspread=6 if dim == 3 else None)
+    p.set_points([cuda(v) for v in xs])
+    img = cvec(rng, (1,) + shape + (nc,))
+    c = cvec(rng, (M, nc))
+    dcf = rng.uniform(0.5, 1.5, M).astype(np.float32)
+    k_dev = p.type2(cuda(img)).cpu()
+    F_dev = p.type1(cuda(c)).cpu()
+    N_dev = p.type21(cuda(img), dcf=cuda(dcf)).cpu()
+    lib = N.lib()
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    for pinned in (False, True):
+        pin = (lambda t: t.pin_memory()) if pinned else (lambda t: t)
+        h_img, h_c = pin(torch.from_numpy(img)), pin(torch.from_numpy(c))
+        h_dcf = pin(torch.from_numpy(dcf))
+        o_k = pin(torch.empty((M, nc), dtype=torch.complex64))
+        o_F = pin(torch.empty((1,) + shape + (nc,), dtype=torch.complex64))
+        o_N = pin(torch.empty((1,) + shape + (nc,), dtype=torch.complex64))
+        N.check(lib.gbn_type2_host(p._h, vp(h_img), vp(o_k), sp))
+        N.check(lib.gbn_type1_host(p._h, vp(h_c), vp(o_F), sp))
+        N.check(lib.gbn_type21_host(p._h, vp(h_img), vp(o_N), vp(h_dcf), sp))
+        assert torch.equal(o_k, k_dev), pinned          # interp: fixed summation order
+        assert rel(o_F, F_dev) < 1e-6, pinned           # split tiles flush with atomics
+        assert rel(o_N, N_dev) < 1e-6, pinned
+
+
 def test_kahan_centre_bins_3d_radial():
     """Dense k-space-centre tiles of 3-D centre-out radial data accumulate with Kahan-
     compensated FP32 sums: against the FP64 oracle spread the centre cells' error drops
