@@ -94,10 +94,14 @@ bool tma_window(const Geom &g, int cg, int64_t n_sub, TmaWin &t) {
     t.n_items = n_sub * t.n_cg;
     t.box_bytes = (uint32_t)t.CS * cg * (uint32_t)sizeof(float2);
     t.buf_elems = (uint32_t)((t.CS * cg + 15) & ~15);
+    // as many buffers (2..4) as fit in 96 KB, leaving room for two blocks per SM
+    const size_t buf_bytes = (size_t)t.buf_elems * sizeof(float2);
+    t.stages = 2;
+    while (t.stages < kTmaMaxStages && (size_t)(t.stages + 1) * buf_bytes <= 96 * 1024) ++t.stages;
     return true;
 }
 
-size_t tma_interp_smem_bytes(const TmaWin &t) { return 2 * (size_t)t.buf_elems * sizeof(float2); }
+size_t tma_interp_smem_bytes(const TmaWin &t) { return (size_t)t.stages * t.buf_elems * sizeof(float2); }
 
 static int sm_count() {
     static int n = 0;

@@ -6,8 +6,11 @@
 // elected thread loads it with a single 3-D tensor copy (cp.async.bulk.tensor: box
 // BY x BX x CG of 8-byte cells, y innermost) that completes on an mbarrier; windows that
 // wrap around the periodic grid edge are gathered by all threads with ordinary loads.
-// Two window buffers alternate, and the copy for item k + 2 is issued as soon as item k's
-// buffer is released, so a block computes on one window while the next is in flight.
+// A ring of S window buffers (2 to 4, as many as fit the shared-memory budget) holds the
+// block's next S items: the copy for item k + S is issued as soon as item k's buffer is
+// released, so a block computes on one window while the next S - 1 are in flight.  The
+// issuing thread also leaves the item's decoded geometry beside its buffer.  Waits
+// suspend the threads in hardware (mbarrier.try_wait) instead of spinning.
 //
 // Shared-memory layout per buffer: [coil][x][y] with row pitch BY and coil stride
 // CS = BX * BY, exactly the order the tensor copy writes.  BX, BY are chosen on the host
@@ -27,7 +30,9 @@
 
 namespace gbn {
 
-constexpr uint32_t kTmaWaitLimit = 1u << 24;  // mbarrier probes before a wait gives up
+constexpr uint32_t kTmaWaitLimit = 1u << 21;  // mbarrier probes before a wait gives up
+constexpr uint32_t kTmaSuspendNs = 1000;      // suspend-time hint of one probe
+constexpr int kTmaMaxStages = 4;              // window buffers per block (ring)
 constexpr uint32_t kStatusTmaTimeout = 2u;    // status-word bit: a bounded wait gave up
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -43,26 +48,25 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                  : "memory");
 }
 
-// non-blocking probe: has the phase with the given parity completed?
-__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
+// potentially blocking probe: the thread is suspended until the phase with the given
+// parity completes or about kTmaSuspendNs nanoseconds pass (it issues nothing meanwhile)
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(kTmaSuspendNs)
         : "memory");
     return ok != 0;
 }
 
 // bounded wait for the phase with the given parity to complete: at most kTmaWaitLimit
-// probes with a short sleep between them (well under a second in all)
+// suspended probes of ~kTmaSuspendNs each (about two seconds in all)
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kTmaWaitLimit; ++i) {
-        if (mbar_test_wait(bar, parity)) return true;
-        if (i >= 32) __nanosleep(32);
-    }
+    for (uint32_t i = 0; i < kTmaWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
 
@@ -120,8 +124,9 @@ __global__ void __launch_bounds__(512) k_interp2d_tma(InterpArgs a, const __grid
                                                       TmaWin t, uint32_t *status) {
     using L = Lanes2D<WT, CG>;
     extern __shared__ __align__(128) float4 smem_t2[];
-    float2 *bufs = reinterpret_cast<float2 *>(smem_t2);  // [2][buf_elems]
-    __shared__ __align__(8) uint64_t bar[2];
+    float2 *bufs = reinterpret_cast<float2 *>(smem_t2);  // [stages][buf_elems]
+    __shared__ __align__(8) uint64_t bar[kTmaMaxStages];
+    __shared__ TmaItem ring[kTmaMaxStages];  // geometry of the item each buffer holds / awaits
     const Geom &g = a.g;
     const int W = WT ? WT : g.W;
     const int ns = g.ns;
@@ -132,33 +137,31 @@ __global__ void __launch_bounds__(512) k_interp2d_tma(InterpArgs a, const __grid
     const int kk = lane & 15;
     const float beta = lane < 16 ? g.beta2[0] : g.beta2[1];
     const int64_t stride = gridDim.x;
+    const int S = t.stages;
 
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int b = 0; b < S; ++b) mbar_init(&bar[b], 1);
         fence_barrier_init();
-        // prologue: the first two items of this block, where a box copy serves them
-        for (int b = 0; b < 2; ++b) {
+        // prologue: the first S items of this block (box copies where the window is inside)
+        for (int b = 0; b < S; ++b) {
             const int64_t item = blockIdx.x + b * stride;
             if (item < t.n_items) {
-                const TmaItem it = tma_item<CG>(a, t, item);
-                if (it.tma) tma_issue<CG>(a, t, &map, it, bufs + (size_t)b * t.buf_elems, &bar[b]);
+                ring[b] = tma_item<CG>(a, t, item);
+                if (ring[b].tma) tma_issue<CG>(a, t, &map, ring[b], bufs + (size_t)b * t.buf_elems, &bar[b]);
             }
         }
     }
     __syncthreads();
 
-    uint32_t parity0 = 0u, parity1 = 0u;  // phase parity expected next on each buffer's barrier
-    int k = 0;
-    for (int64_t item = blockIdx.x; item < t.n_items; item += stride, ++k) {
-        const int b = k & 1;
+    uint32_t parity = 0u;  // bit b: phase parity expected next on buffer b's barrier
+    int b = 0;
+    for (int64_t item = blockIdx.x; item < t.n_items; item += stride, b = (b + 1 == S) ? 0 : b + 1) {
         float2 *win = bufs + (size_t)b * t.buf_elems;
-        const TmaItem it = tma_item<CG>(a, t, item);
+        const TmaItem it = ring[b];
         int off1 = 0;
         if (it.tma) {
-            if (!mbar_wait_bounded(&bar[b], b ? parity1 : parity0) && lane == 0) atomicOr(status, kStatusTmaTimeout);
-            if (b) parity1 ^= 1u;
-            else parity0 ^= 1u;
+            if (!mbar_wait_bounded(&bar[b], (parity >> b) & 1u) && lane == 0) atomicOr(status, kStatusTmaTimeout);
+            parity ^= 1u << b;
             off1 = it.ws1 - it.ys;
         } else {
             // the window wraps: gather it with periodic indices, y fastest (coalesced)
@@ -240,12 +243,12 @@ __global__ void __launch_bounds__(512) k_interp2d_tma(InterpArgs a, const __grid
                 a.c[(int64_t)j * a.c_elem + (int64_t)(it.cg0 + c) * a.c_coil] = make_float2(ax * sc, ay * sc);
             }
         }
-        __syncthreads();  // every read of this buffer is done: it can be refilled
+        __syncthreads();  // every read of this buffer (and of ring[b]) is done: refill both
         if (threadIdx.x == 0) {
-            const int64_t next = item + 2 * stride;
+            const int64_t next = item + (int64_t)S * stride;
             if (next < t.n_items) {
-                const TmaItem nt = tma_item<CG>(a, t, next);
-                if (nt.tma) tma_issue<CG>(a, t, &map, nt, win, &bar[b]);
+                ring[b] = tma_item<CG>(a, t, next);
+                if (ring[b].tma) tma_issue<CG>(a, t, &map, ring[b], win, &bar[b]);
             }
         }
     }
