@@ -287,7 +287,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // Tensor map of a 2-D plan grid as a 3-D tensor (y innermost, x, instance) of 8-byte
-// cells, box BY x BX x coils; cached for the last grid pointer and box.  False when the
+// cells, box BY x BX x cg coils (an item's coils); cached for the last grid pointer and box.  False when the
 // grid is not 16-byte aligned, its rows are not a multiple of 16 bytes, or the driver
 // lacks the encoder: the caller then uses the thread-staged kernel.
 bool grid_tensor_map(gbn_plan *p, const float2 *grid, int cg, const TmaWin &t) {
@@ -327,7 +327,7 @@ int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const flo
     // 2-D: windows staged by tensor copies when the grid admits a tensor map
     TmaWin t{};
     if (p->interp_staging == 0 && tma_window(p->gi, cg, p->n_interp_sub, t) &&
-        tma_interp_smem_bytes(t) <= (size_t)p->smem_optin && grid_tensor_map(p, grid, cg, t)) {
+        tma_interp_smem_bytes(t) <= (size_t)p->smem_optin && grid_tensor_map(p, grid, cg * t.passes, t)) {
         GBN_CUDA(launch_interp2d_tma(a, t, p->tmap, cg, p->interp_threads, p->kstatus, s));
         return GBN_OK;
     }

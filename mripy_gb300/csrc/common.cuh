@@ -158,6 +158,7 @@ struct TmaWin {
     uint32_t box_bytes;   // bytes one box copy delivers: BX * BY * CG * 8
     uint32_t buf_elems;   // float2 per buffer: CG * CS rounded up to 16 (128-byte buffers)
     int stages;           // window buffers per block (2..4)
+    int passes;           // coil groups of CG per item: a window holds CG * passes coils
 };
 bool tma_window(const Geom &g, int coil_group, int64_t n_sub, TmaWin &t);
 size_t tma_interp_smem_bytes(const TmaWin &t);

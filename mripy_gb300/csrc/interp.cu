@@ -90,11 +90,22 @@ bool tma_window(const Geom &g, int cg, int64_t n_sub, TmaWin &t) {
         }
     if (best == 0) return false;
     t.CS = t.BX * t.BY;
-    t.n_cg = (g.n_coil + cg - 1) / cg;
+    // Coil passes per item: as many groups of cg coils as let two buffers fit in the
+    // budget (two blocks per SM), so the sample weights and the per-item work are shared
+    // by more coils (12 coils in groups of 4: one item of 3 passes instead of 3 items).
+    constexpr size_t kBudget = 112 * 1024;
+    const int groups = (g.n_coil + cg - 1) / cg;
+    const size_t pass_bytes = (size_t)t.CS * cg * sizeof(float2);
+    t.passes = 1;
+    while (t.passes < groups && cg * (t.passes + 1) <= 256 && 2 * (t.passes + 1) * pass_bytes <= kBudget)
+        ++t.passes;
+    const int coils = cg * t.passes;
+    t.n_cg = (g.n_coil + coils - 1) / coils;
     t.n_items = n_sub * t.n_cg;
-    t.box_bytes = (uint32_t)t.CS * cg * (uint32_t)sizeof(float2);
-    t.buf_elems = (uint32_t)((t.CS * cg + 15) & ~15);
-    // as many buffers (2..4) as fit in 96 KB, leaving room for two blocks per SM
+    t.box_bytes = (uint32_t)t.CS * coils * (uint32_t)sizeof(float2);
+    t.buf_elems = (uint32_t)((t.CS * coils + 15) & ~15);
+    // as many buffers (2..4) as fit in 96 KB (measured: a third 36 KB buffer costs more in
+    // blocks per SM than it gains in prefetch depth on the 8-coil 512^2 radial workload)
     const size_t buf_bytes = (size_t)t.buf_elems * sizeof(float2);
     t.stages = 2;
     while (t.stages < kTmaMaxStages && (size_t)(t.stages + 1) * buf_bytes <= 96 * 1024) ++t.stages;
@@ -120,7 +131,7 @@ cudaError_t launch_interp2d_tma(const InterpArgs &a, const TmaWin &t, const CUte
     const size_t smem = tma_interp_smem_bytes(t);
     cudaError_t err = cudaSuccess;
     GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
-        auto kern = k_interp2d_tma<WT, CG>;
+        auto kern = t.passes > 1 ? k_interp2d_tma<WT, CG, true> : k_interp2d_tma<WT, CG, false>;
         err = set_smem(kern, smem);
         int per_sm = 0;
         if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);

@@ -98,7 +98,7 @@ __device__ __forceinline__ TmaItem tma_item(const InterpArgs &a, const TmaWin &t
     const Geom &g = a.g;
     TmaItem r;
     const int64_t si = item / t.n_cg;
-    r.cg0 = (int)(item - si * t.n_cg) * CG;
+    r.cg0 = (int)(item - si * t.n_cg) * CG * t.passes;
     r.sub = a.subs[si];
     r.grp = r.sub.x / g.ntiles;
     const int tile = r.sub.x % g.ntiles;
@@ -119,7 +119,9 @@ __device__ __forceinline__ void tma_issue(const InterpArgs &a, const TmaWin &t, 
     tma_load_3d(buf, map, it.ys, it.ws0, it.grp * a.g.n_coil + it.cg0, bar);
 }
 
-template <int WT, int CG>
+// MULTI: items hold several coil groups (t.passes > 1); the single-group instance keeps
+// fewer registers (x weights shuffled per tap row instead of kept).
+template <int WT, int CG, bool MULTI>
 __global__ void __launch_bounds__(512) k_interp2d_tma(InterpArgs a, const __grid_constant__ CUtensorMap map,
                                                       TmaWin t, uint32_t *status) {
     using L = Lanes2D<WT, CG>;
@@ -166,7 +168,7 @@ __global__ void __launch_bounds__(512) k_interp2d_tma(InterpArgs a, const __grid
         } else {
             // the window wraps: gather it with periodic indices, y fastest (coalesced)
             const float2 *base = a.grid + ((int64_t)it.grp * g.n_coil + it.cg0) * g.G;
-            const int n = CG * WX * WY;
+            const int n = CG * t.passes * WX * WY;
             const float rWY = 1.f / (float)WY, rWX = 1.f / (float)WX;
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int row = div_small(i, rWY), wy = i - row * WY;
@@ -211,36 +213,47 @@ __global__ void __launch_bounds__(512) k_interp2d_tma(InterpArgs a, const __grid
                 const float v = __shfl_sync(0xffffffffu, myw, 16 + (ky < 16 ? ky : 15));
                 wy[tt] = ky < W ? v : 0.f;
             }
-            float2 acc[L::KT];
+            float wxs[MULTI ? L::WMAX : 1];  // MULTI: x weights kept for every coil pass
+            if constexpr (MULTI) {
 #pragma unroll
-            for (int tt = 0; tt < L::KT; ++tt) acc[tt] = make_float2(0.f, 0.f);
-            const float2 *rowbase = win + c * t.CS + rel0 * t.BY + rel1 + off1;
+                for (int kx = 0; kx < L::WMAX; ++kx) wxs[kx] = __shfl_sync(0xffffffffu, myw, kx);
+            }
+            const float sc = (q == 0 && a.weight) ? a.weight[j] : 1.f;
+            // the item's coils in passes of CG (lanes = CG coils x tap slots)
+            const int passes = MULTI ? t.passes : 1;
+            for (int ps = 0; ps < passes; ++ps) {
+                const int coil = it.cg0 + ps * CG + c;
+                float2 acc[L::KT];
 #pragma unroll
-            for (int kx = 0; kx < L::WMAX; ++kx) {
-                if (WT == 0 && kx >= W) break;
-                const float wx = __shfl_sync(0xffffffffu, myw, kx);
-                const float2 wx2 = make_float2(wx, wx);
-                const float2 *row = rowbase + kx * t.BY;
+                for (int tt = 0; tt < L::KT; ++tt) acc[tt] = make_float2(0.f, 0.f);
+                const float2 *rowbase = win + (ps * CG + c) * t.CS + rel0 * t.BY + rel1 + off1;
+#pragma unroll
+                for (int kx = 0; kx < L::WMAX; ++kx) {
+                    if (WT == 0 && kx >= W) break;
+                    float wx;
+                    if constexpr (MULTI) wx = wxs[kx];
+                    else wx = __shfl_sync(0xffffffffu, myw, kx);
+                    const float2 wx2 = make_float2(wx, wx);
+                    const float2 *row = rowbase + kx * t.BY;
+#pragma unroll
+                    for (int tt = 0; tt < L::KT; ++tt) {
+                        const int ky = q + tt * L::NQ;
+                        if (ky < W) acc[tt] = __ffma2_rn(wx2, row[ky], acc[tt]);
+                    }
+                }
+                float ax = 0.f, ay = 0.f;
 #pragma unroll
                 for (int tt = 0; tt < L::KT; ++tt) {
-                    const int ky = q + tt * L::NQ;
-                    if (ky < W) acc[tt] = __ffma2_rn(wx2, row[ky], acc[tt]);
+                    ax = fmaf(wy[tt], acc[tt].x, ax);
+                    ay = fmaf(wy[tt], acc[tt].y, ay);
                 }
-            }
-            float ax = 0.f, ay = 0.f;
 #pragma unroll
-            for (int tt = 0; tt < L::KT; ++tt) {
-                ax = fmaf(wy[tt], acc[tt].x, ax);
-                ay = fmaf(wy[tt], acc[tt].y, ay);
-            }
-#pragma unroll
-            for (int off = CG; off < 32; off <<= 1) {
-                ax += __shfl_xor_sync(0xffffffffu, ax, off);
-                ay += __shfl_xor_sync(0xffffffffu, ay, off);
-            }
-            if (q == 0 && it.cg0 + c < g.n_coil) {
-                const float sc = a.weight ? a.weight[j] : 1.f;
-                a.c[(int64_t)j * a.c_elem + (int64_t)(it.cg0 + c) * a.c_coil] = make_float2(ax * sc, ay * sc);
+                for (int off = CG; off < 32; off <<= 1) {
+                    ax += __shfl_xor_sync(0xffffffffu, ax, off);
+                    ay += __shfl_xor_sync(0xffffffffu, ay, off);
+                }
+                if (q == 0 && coil < g.n_coil)
+                    a.c[(int64_t)j * a.c_elem + (int64_t)coil * a.c_coil] = make_float2(ax * sc, ay * sc);
             }
         }
         __syncthreads();  // every read of this buffer (and of ring[b]) is done: refill both
