@@ -264,7 +264,7 @@ int interp_cg(const gbn_plan *p) {
             }
         }
     }
-    while (cg > 1 && interp_smem_bytes(p->gi, cg) > smem_budget(p)) cg /= 2;
+    while (cg > 1 && interp_smem_bytes(p->gi, cg, p->interp_threads) > smem_budget(p)) cg /= 2;
     return cg;
 }
 
@@ -331,7 +331,7 @@ int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const flo
         GBN_CUDA(launch_interp2d_tma(a, t, p->tmap, cg, p->interp_threads, p->kstatus, s));
         return GBN_OK;
     }
-    if (interp_smem_bytes(p->gi, cg) > (size_t)p->smem_optin)
+    if (interp_smem_bytes(p->gi, cg, p->interp_threads) > (size_t)p->smem_optin)
         return fail(GBN_ERR_CAPACITY, "interp window does not fit in shared memory");
     GBN_CUDA(launch_interp(a, p->n_interp_sub, cg, p->interp_threads, s));
     return GBN_OK;
@@ -355,8 +355,8 @@ int key_bits(uint64_t max_key) {
 
 // count -> tile offsets (exclusive), subproblem table
 int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, DevBuf &subs, int every_tile,
-               uint32_t dense_min, uint32_t *n_dense, uint32_t *split_list, uint32_t *n_split, int64_t *n_sub_out,
-               cudaStream_t s) {
+               int max_sub, uint32_t dense_min, uint32_t *n_dense, uint32_t *split_list, uint32_t *n_split,
+               int64_t *n_sub_out, cudaStream_t s) {
     const int64_t T = (int64_t)g.ntiles * g.n_traj;
     GBN_TRY(ensure(p, tile_off, sizeof(uint32_t) * T));
     GBN_TRY(ensure(p, p->nsub, sizeof(uint32_t) * T));
@@ -365,7 +365,7 @@ int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, De
     GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
         return cub::DeviceScan::ExclusiveSum(tmp, bytes, count, toff, (int)T, s);
     }));
-    GBN_CUDA(launch_count_subs(count, T, p->max_sub, every_tile, p->nsub.as<uint32_t>(), s));
+    GBN_CUDA(launch_count_subs(count, T, max_sub, every_tile, p->nsub.as<uint32_t>(), s));
     uint32_t *soff = p->sub_off.as<uint32_t>();
     uint32_t *ns_ = p->nsub.as<uint32_t>();
     GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
@@ -378,7 +378,7 @@ int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, De
     const int64_t n_sub = (int64_t)last[0] + last[1];
     if (n_sub > 0x7FFFFFFF) return fail(GBN_ERR_CAPACITY, "too many subproblems");
     GBN_TRY(ensure(p, subs, sizeof(int4) * (size_t)std::max<int64_t>(n_sub, 1)));
-    GBN_CUDA(launch_build_subs(count, toff, soff, T, p->max_sub, every_tile, dense_min, n_dense, split_list, n_split,
+    GBN_CUDA(launch_build_subs(count, toff, soff, T, max_sub, every_tile, dense_min, n_dense, split_list, n_split,
                                subs.as<int4>(), s));
     *n_sub_out = n_sub;
     return GBN_OK;
@@ -493,10 +493,15 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
     // third status word
     GBN_TRY(ensure(p, p->split_tiles, sizeof(uint32_t) * (size_t)std::max<int64_t>(Ts, 1)));
     GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, 2 * sizeof(uint32_t), s));
-    GBN_TRY(build_subs(p, p->gs, scount, p->spread_tile_off, p->spread_subs, 1, dense_min, p->kstatus + 1,
-                       p->split_tiles.as<uint32_t>(), p->kstatus + 2, &p->n_spread_sub, s));
-    GBN_TRY(build_subs(p, p->gi, home_count, p->home_tile_off, p->interp_subs, 0, 0u, nullptr, nullptr, nullptr,
-                       &p->n_interp_sub, s));
+    GBN_TRY(build_subs(p, p->gs, scount, p->spread_tile_off, p->spread_subs, 1, p->max_sub, dense_min,
+                       p->kstatus + 1, p->split_tiles.as<uint32_t>(), p->kstatus + 2, &p->n_spread_sub, s));
+    // the plane-streaming 3-D interp holds a chunk of kPlaneSamples samples' state; work
+    // items of at most that size stream each window once
+    const int interp_max_sub = interp3d_planes_smem(p->gi, interp_cg(p), p->interp_threads) > 0
+                                   ? std::min(p->max_sub, kPlaneSamples)
+                                   : p->max_sub;
+    GBN_TRY(build_subs(p, p->gi, home_count, p->home_tile_off, p->interp_subs, 0, interp_max_sub, 0u, nullptr,
+                       nullptr, nullptr, &p->n_interp_sub, s));
     uint32_t counts[2] = {0, 0};
     GBN_CUDA(cudaMemcpyAsync(counts, p->kstatus + 1, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     GBN_CUDA(cudaStreamSynchronize(s));

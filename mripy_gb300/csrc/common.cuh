@@ -147,7 +147,10 @@ cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, in
 cudaError_t launch_interp_grad(const GradArgs &a, int64_t n_sub, int coil_group, int threads,
                                cudaStream_t s);
 size_t spread_smem_bytes(const Geom &g, int coil_group);
-size_t interp_smem_bytes(const Geom &g, int coil_group);
+size_t interp_smem_bytes(const Geom &g, int coil_group, int threads);
+// shared memory of the plane-streaming 3-D interp, 0 where it does not apply
+size_t interp3d_planes_smem(const Geom &g, int coil_group, int threads);
+constexpr int kPlaneSamples = 64;  // samples per chunk of the plane-streaming 3-D interp
 
 // TMA-staged 2-D interp (interp2d_tma.cuh): window box geometry and launcher
 struct TmaWin {

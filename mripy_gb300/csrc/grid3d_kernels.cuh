@@ -143,6 +143,172 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
     }
 }
 
+// ------------------------------------------------------------------ interp, plane streaming
+// For 4 or 8 coils per block.  A bin's (TX+W-1) x (TY+W-1) x (TZ+W-1) window does not fit in
+// shared memory at 8 coils (439 KB for 8^3 bins), so it is streamed one x plane at a time:
+// two plane buffers, the next plane prefetched into registers while the current one is
+// used.  Up to kPlaneSamples samples of the bin are processed together; their weights
+// (16 slots per dimension), home-relative first taps and per-coil accumulators live in
+// shared memory.  For each plane every warp walks its samples (sample s belongs to warp
+// s mod warps); a sample whose x stencil covers the plane adds wx * sum_y wy sum_z wz G over
+// the plane's W x W taps: lanes = (coil, z slot) as in k_interp3d, per-slot sums applied
+// with wz once, a shuffle reduction over the slots, and one lane per coil adding the result
+// to the sample's accumulator (no other warp touches it).
+constexpr int kPlanePrefetch = 12;  // plane elements (cell x coil) per thread held in registers
+
+template <int CG>
+__device__ __forceinline__ void plane_load(float2 (&pf)[kPlanePrefetch], const float2 *__restrict__ base,
+                                           const Geom &g, int cg0, int gx, int ws1, int ws2, int WZ, int PC,
+                                           float rWZ) {
+    const float2 *pb = base + (int64_t)gx * g.nf[1] * g.nf[2];
+#pragma unroll
+    for (int i = 0; i < kPlanePrefetch; ++i) {
+        const int el = threadIdx.x + i * blockDim.x;
+        float2 v = make_float2(0.f, 0.f);
+        if (el < PC) {
+            const int cc = el % CG, cell = el / CG;  // coil fastest: consecutive shared words
+            const int wy = div_small(cell, rWZ), wz = cell - wy * WZ;
+            const int gy = wrap_fast(ws1 + wy, g.nf[1]), gz = wrap_fast(ws2 + wz, g.nf[2]);
+            if (cg0 + cc < g.n_coil) v = pb[(int64_t)cc * g.G + (int64_t)gy * g.nf[2] + gz];
+        }
+        pf[i] = v;
+    }
+}
+
+__device__ __forceinline__ void plane_store(const float2 (&pf)[kPlanePrefetch], float2 *dst, int PC) {
+#pragma unroll
+    for (int i = 0; i < kPlanePrefetch; ++i) {
+        const int el = threadIdx.x + i * blockDim.x;
+        if (el < PC) dst[el] = pf[i];
+    }
+}
+
+template <int WT, int CG>
+__global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
+    using L = Lanes2D<WT, CG>;
+    constexpr int NS = kPlaneSamples;
+    extern __shared__ float4 smem_p3[];
+    const Geom &g = a.g;
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+    const int WX = g.tile[0] + W - 1, WY = g.tile[1] + W - 1, WZ = g.tile[2] + W - 1;
+    const int PC = WY * WZ * CG;                                   // float2 per plane
+    float2 *planes = reinterpret_cast<float2 *>(smem_p3);          // [2][PC], [y][z][coil]
+    float *st_w = reinterpret_cast<float *>(planes + 2 * PC);      // [NS][48]: wx, wy, wz
+    int4 *st_r = reinterpret_cast<int4 *>(st_w + NS * 48);         // [NS]: rel0, rel1, rel2, sample
+    float2 *st_acc = reinterpret_cast<float2 *>(st_r + NS);        // [NS][CG]
+
+    const int4 sub = a.subs[blockIdx.x];
+    const int cg0 = blockIdx.y * CG;
+    const int grp = sub.x / g.ntiles;
+    int o[3], e[3];
+    tile_coords<3>(g, sub.x % g.ntiles, o, e);
+    const int ws0 = o[0] - (ns - 1), ws1 = o[1] - (ns - 1), ws2 = o[2] - (ns - 1);
+    const float2 *base = a.grid + ((int64_t)grp * g.n_coil + cg0) * g.G;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const float rWZ = 1.f / (float)WZ;
+    float2 pf[kPlanePrefetch];
+
+    for (int base_s = 0; base_s < sub.z; base_s += NS) {
+        const int n = min(NS, sub.z - base_s);
+        __syncthreads();  // the previous chunk's state and planes are consumed
+        for (int i = threadIdx.x; i < n * 48; i += blockDim.x) {
+            const int s = i / 48, k = i - s * 48, d = k >> 4, kq = k & 15;
+            const float4 p = a.pts[(int64_t)sub.y + base_s + s];
+            const float f = d == 0 ? p.x : (d == 1 ? p.y : p.z);
+            const float b = d == 0 ? g.beta2[0] : (d == 1 ? g.beta2[1] : g.beta2[2]);
+            st_w[i] = tap_weight(true, kq, W, f, ns, b);
+            if (k == 0) {
+                int c0[3];
+                unpack_cells(3, __float_as_uint(p.w), c0[0], c0[1], c0[2]);
+                int rel[3];
+#pragma unroll
+                for (int dd = 0; dd < 3; ++dd) {
+                    int cc = c0[dd] + ns - 1;
+                    cc -= cc >= g.nf[dd] ? g.nf[dd] : 0;
+                    rel[dd] = cc - o[dd];
+                }
+                st_r[s] = make_int4(rel[0], rel[1], rel[2], (int)a.idx[(int64_t)sub.y + base_s + s]);
+            }
+        }
+        for (int i = threadIdx.x; i < n * CG; i += blockDim.x) st_acc[i] = make_float2(0.f, 0.f);
+        plane_load<CG>(pf, base, g, cg0, wrap_fast(ws0, g.nf[0]), ws1, ws2, WZ, PC, rWZ);
+        plane_store(pf, planes, PC);
+        __syncthreads();
+
+        for (int px = 0; px < WX; ++px) {
+            const float2 *cur = planes + (px & 1) * PC;
+            if (px + 1 < WX) plane_load<CG>(pf, base, g, cg0, wrap_fast(ws0 + px + 1, g.nf[0]), ws1, ws2, WZ, PC, rWZ);
+            for (int s = warp; s < n; s += nw) {
+                const int4 r = st_r[s];
+                const int kx = px - r.x;
+                if ((unsigned)kx >= (unsigned)W) continue;  // warp-uniform: stencil misses this plane
+                const float *w = st_w + s * 48;
+                float2 at[L::KT];
+#pragma unroll
+                for (int t = 0; t < L::KT; ++t) at[t] = make_float2(0.f, 0.f);
+                const float2 *rowbase = cur + ((size_t)r.y * WZ + r.z) * CG + c;
+#pragma unroll
+                for (int ky = 0; ky < L::WMAX; ++ky) {
+                    if (WT == 0 && ky >= W) break;
+                    const float wy = w[16 + ky];
+                    const float2 wy2 = make_float2(wy, wy);
+                    const float2 *row = rowbase + (size_t)ky * WZ * CG;
+#pragma unroll
+                    for (int t = 0; t < L::KT; ++t) {
+                        const int kz = q + t * L::NQ;
+                        if (kz < W) at[t] = __ffma2_rn(wy2, row[kz * CG], at[t]);
+                    }
+                }
+                float ax = 0.f, ay = 0.f;
+#pragma unroll
+                for (int t = 0; t < L::KT; ++t) {
+                    const int kz = q + t * L::NQ;
+                    const float wz = kz < W ? w[32 + kz] : 0.f;
+                    ax = fmaf(wz, at[t].x, ax);
+                    ay = fmaf(wz, at[t].y, ay);
+                }
+#pragma unroll
+                for (int off = CG; off < 32; off <<= 1) {
+                    ax += __shfl_xor_sync(0xffffffffu, ax, off);
+                    ay += __shfl_xor_sync(0xffffffffu, ay, off);
+                }
+                if (q == 0) {
+                    const float wx = w[kx];
+                    float2 &acc = st_acc[s * CG + c];
+                    acc.x = fmaf(wx, ax, acc.x);
+                    acc.y = fmaf(wx, ay, acc.y);
+                }
+            }
+            if (px + 1 < WX) plane_store(pf, planes + ((px + 1) & 1) * PC, PC);
+            __syncthreads();
+        }
+
+        for (int i = threadIdx.x; i < n * CG; i += blockDim.x) {
+            const int s = i / CG, cc = i - s * CG;
+            if (cg0 + cc < g.n_coil) {
+                const uint32_t j = (uint32_t)st_r[s].w;
+                float2 v = st_acc[i];
+                if (a.weight) {
+                    const float sw = a.weight[j];
+                    v.x *= sw;
+                    v.y *= sw;
+                }
+                a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil] = v;
+            }
+        }
+    }
+}
+
+// shared memory of k_interp3d_planes, or 0 when a plane does not fit the register prefetch
+inline size_t interp3d_planes_smem_bytes(const Geom &g, int cg, int threads) {
+    const int PC = (g.tile[1] + g.W - 1) * (g.tile[2] + g.W - 1) * cg;
+    if (g.dim != 3 || g.W > 16 || (cg != 4 && cg != 8) || PC > kPlanePrefetch * threads) return 0;
+    return 2 * (size_t)PC * sizeof(float2) + kPlaneSamples * (48 * sizeof(float) + sizeof(int4)) +
+           (size_t)kPlaneSamples * cg * sizeof(float2);
+}
+
 // --------------------------------------------------------------------------------- spread
 constexpr int kSpread3dBatch = 32;
 

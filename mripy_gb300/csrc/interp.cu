@@ -2,7 +2,8 @@
 //
 // 2-D with at most 16 taps per dimension: k_interp2d_tma (persistent, windows staged by
 // tensor copies; the caller supplies the tensor map) or k_interp2d (one block per
-// subproblem, windows gathered by the threads).  3-D with at most 16 taps: k_interp3d.
+// subproblem, windows gathered by the threads).  3-D with at most 16 taps:
+// k_interp3d_planes (4 or 8 coils per block, window streamed by x planes) or k_interp3d.
 // Otherwise (1-D, wide stencils): k_interp (one thread per sample).
 #include <algorithm>
 
@@ -15,8 +16,15 @@ namespace gbn {
 
 static bool use_2d_path(const Geom &g) { return g.dim == 2 && g.W <= 16; }
 
-size_t interp_smem_bytes(const Geom &g, int coil_group) {
+size_t interp3d_planes_smem(const Geom &g, int coil_group, int threads) {
+    return interp3d_planes_smem_bytes(g, coil_group, threads > 256 ? 256 : threads);
+}
+
+// shared memory of the kernel launch_interp runs for this geometry, coil group and thread
+// count (the 3-D kernel depends on all three)
+size_t interp_smem_bytes(const Geom &g, int coil_group, int threads) {
     if (use_2d_path(g)) return interp2d_smem_bytes(g, coil_group);
+    if (const size_t ps = interp3d_planes_smem_bytes(g, coil_group, threads > 256 ? 256 : threads)) return ps;
     size_t cells = 1;
     for (int d = 0; d < g.dim; ++d) cells *= (size_t)(g.tile[d] + g.W - 1);
     return cells * (size_t)coil_group * sizeof(float2);
@@ -30,7 +38,7 @@ static size_t grad_smem_bytes(const Geom &g, int coil_group) {
 
 cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, int threads, cudaStream_t s) {
     if (n_sub == 0) return cudaSuccess;
-    const size_t smem = interp_smem_bytes(a.g, coil_group);
+    const size_t smem = interp_smem_bytes(a.g, coil_group, threads);
     const dim3 grid((unsigned)n_sub, (unsigned)((a.g.n_coil + coil_group - 1) / coil_group));
     cudaError_t err = cudaSuccess;
     if (use_2d_path(a.g)) {
@@ -45,11 +53,25 @@ cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, in
         return err;
     }
     if (a.g.dim == 3 && a.g.W <= 16) {
+        const int th = threads > 256 ? 256 : threads;
+        const size_t psmem = interp3d_planes_smem_bytes(a.g, coil_group, th);
+        if (psmem) {  // 4 or 8 coils per block: stream the window plane by plane
+            GBN_DISPATCH_W(a.g.W, {
+                auto kern = coil_group == 8 ? k_interp3d_planes<WT, 8> : k_interp3d_planes<WT, 4>;
+                err = set_smem(kern, psmem);
+                if (err == cudaSuccess) {
+                    kern<<<grid, th, psmem, s>>>(a);
+                    err = cudaGetLastError();
+                }
+            });
+            return err;
+        }
+        const size_t wsmem = interp3d_smem_bytes(a.g, coil_group);  // the whole staged window
         GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
             auto kern = k_interp3d<WT, CG>;
-            err = set_smem(kern, smem);
+            err = set_smem(kern, wsmem);
             if (err == cudaSuccess) {
-                kern<<<grid, threads > 256 ? 256 : threads, smem, s>>>(a);
+                kern<<<grid, th, wsmem, s>>>(a);
                 err = cudaGetLastError();
             }
         }));
