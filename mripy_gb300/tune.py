@@ -44,13 +44,32 @@ def _spread_candidates(dim, n_coil):
     return out
 
 
+def _interp_threads(dim):
+    return (256, 512) if dim == 2 else (128, 256)
+
+
+def _interp_coil_groups(n_coil):
+    return [0] + [cg for cg in (8, 4, 2) if cg <= n_coil]
+
+
+def candidate_tunings(dim, n_coil):
+    """Every configuration the search below can time: the spread candidates, then the interp
+    ones (each with the other kernel at library defaults)."""
+    _, interp_c = _candidates(dim)
+    out = [Tuning(spread_tile=t, threads=th, coil_group=cg) for t, th, cg in _spread_candidates(dim, n_coil)]
+    out += [Tuning(interp_tile=t, interp_threads=th, interp_coil_group=cg)
+            for t in interp_c for th in _interp_threads(dim) for cg in _interp_coil_groups(n_coil)]
+    return out
+
+
 def _candidates(dim):
     if dim == 2:
         spread = [(16, 32), (8, 32), (32, 32), (16, 64), (32, 16)]
         interp = [(16, 16), (8, 32), (16, 32), (8, 16), (32, 32)]
     elif dim == 3:
         spread = [(8, 8, 32), (8, 8, 16), (4, 8, 32), (8, 16, 16)]
-        interp = [(8, 8, 8), (4, 8, 16), (8, 8, 16), (4, 4, 16)]
+        # (8, 8, 8), (16, 8, 8), (8, 4, 8): planes the plane-streaming kernel takes at 8 coils
+        interp = [(8, 8, 8), (16, 8, 8), (8, 4, 8), (4, 8, 16), (8, 8, 16), (4, 4, 16)]
     else:
         spread = [(1024,), (512,), (2048,)]
         interp = [(1024,), (512,), (256,)]
@@ -132,9 +151,9 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
             print("spread", tile, th, cg, t_s)
         if best_s is None or t_s < best_s[0]:
             best_s = (t_s, tile, th, cg)
-    icg = [0] + [cg for cg in (8, 4, 2) if cg <= n_coil]
+    icg = _interp_coil_groups(n_coil)
     for tile in interp_c:
-        for th in ((256, 512) if dim == 2 else (128, 256)):
+        for th in _interp_threads(dim):
             for cg in icg:
                 tu = Tuning(interp_tile=tile, interp_threads=th, interp_coil_group=cg)
                 try:

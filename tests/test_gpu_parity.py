@@ -383,6 +383,30 @@ def test_host_entry_points_pinned_and_pageable(dim):
         assert rel(o_N, N_dev) < 1e-6, pinned
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_every_tuning_candidate_matches_oracle(dim):
+    """Each configuration the autotuner may time (tiles, threads, coils per block, kernel
+    variants they select) gives the oracle's type-2 and type-1 results."""
+    from mripy_gb300 import tune
+    rng = np.random.default_rng(26)
+    shape, nc, M = ((64, 56), 8, 8000) if dim == 2 else ((28, 26, 24), 8, 6000)
+    xs = rng.uniform(-np.pi, np.pi, (dim, M))
+    xs[:, :3000] *= 0.1                                          # dense centre: split tiles
+    img = cvec(rng, shape + (nc,))
+    c = cvec(rng, (M, nc))
+    co = tuple(xs)
+    ref2 = O.nufft_type2(co, img.astype(np.complex128), shape, eps=5e-6)
+    ref1 = O.nufft_type1(co, c.astype(np.complex128), shape, eps=5e-6)
+    coords = [cuda(v) for v in xs]
+    for tu in tune.candidate_tunings(dim, nc):
+        p = NufftPlan(dim, shape, n_coil=nc, eps=5e-6, max_nspread=6 if dim == 3 else None, tuning=tu)
+        p.set_points(coords)
+        assert rel(p.type2(cuda(img)[None]), ref2) < TOL_REF, tu
+        assert rel(p.type1(cuda(c))[0], ref1) < TOL_REF, tu
+        p.status()
+        p.close()
+
+
 def test_kahan_centre_bins_3d_radial():
     """Dense k-space-centre tiles of 3-D centre-out radial data accumulate with Kahan-
     compensated FP32 sums: against the FP64 oracle spread the centre cells' error drops
