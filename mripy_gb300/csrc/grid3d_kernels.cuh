@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
 // ------------------------------------------------------------------ interp, plane streaming
 // For 4 or 8 coils per block.  A bin's (TX+W-1) x (TY+W-1) x (TZ+W-1) window does not fit in
 // shared memory at 8 coils (439 KB for 8^3 bins), so it is streamed one x plane at a time:
-// two plane buffers, the next plane prefetched into registers while the current one is
+// two plane buffers, the next plane's cells copied by cp.async while the current one is
 // used.  Up to kPlaneSamples samples of the bin are processed together; their weights
 // (16 slots per dimension), home-relative first taps and per-coil accumulators live in
 // shared memory.  For each plane every warp walks its samples (sample s belongs to warp
@@ -154,32 +154,29 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
 // the plane's W x W taps: lanes = (coil, z slot) as in k_interp3d, per-slot sums applied
 // with wz once, a shuffle reduction over the slots, and one lane per coil adding the result
 // to the sample's accumulator (no other warp touches it).
-constexpr int kPlanePrefetch = 12;  // plane elements (cell x coil) per thread held in registers
+constexpr int kPlaneMaxElems = 4096;  // plane elements (cell x coil) the kernel accepts
 
-template <int CG>
-__device__ __forceinline__ void plane_load(float2 (&pf)[kPlanePrefetch], const float2 *__restrict__ base,
-                                           const Geom &g, int cg0, int gx, int ws1, int ws2, int WZ, int PC,
-                                           float rWZ) {
-    const float2 *pb = base + (int64_t)gx * g.nf[1] * g.nf[2];
-#pragma unroll
-    for (int i = 0; i < kPlanePrefetch; ++i) {
-        const int el = threadIdx.x + i * blockDim.x;
-        float2 v = make_float2(0.f, 0.f);
-        if (el < PC) {
-            const int cc = el % CG, cell = el / CG;  // coil fastest: consecutive shared words
-            const int wy = div_small(cell, rWZ), wz = cell - wy * WZ;
-            const int gy = wrap_fast(ws1 + wy, g.nf[1]), gz = wrap_fast(ws2 + wz, g.nf[2]);
-            if (cg0 + cc < g.n_coil) v = pb[(int64_t)cc * g.G + (int64_t)gy * g.nf[2] + gz];
-        }
-        pf[i] = v;
-    }
+// 8-byte asynchronous copy global -> shared (cp.async); src_bytes 0 writes zeros
+__device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
 }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-__device__ __forceinline__ void plane_store(const float2 (&pf)[kPlanePrefetch], float2 *dst, int PC) {
-#pragma unroll
-    for (int i = 0; i < kPlanePrefetch; ++i) {
-        const int el = threadIdx.x + i * blockDim.x;
-        if (el < PC) dst[el] = pf[i];
+// issue the copies of plane gx (periodic y/z indices, coil fastest) into dst; the caller
+// waits (cp_async_wait_all) and synchronises before reading it
+template <int CG>
+__device__ __forceinline__ void plane_copy(float2 *dst, const float2 *__restrict__ base, const Geom &g, int cg0,
+                                           int gx, int ws1, int ws2, int WZ, int PC, float rWZ) {
+    const float2 *pb = base + (int64_t)gx * g.nf[1] * g.nf[2];
+    for (int el = threadIdx.x; el < PC; el += blockDim.x) {
+        const int cc = el % CG, cell = el / CG;  // coil fastest: consecutive shared words
+        const int wy = div_small(cell, rWZ), wz = cell - wy * WZ;
+        const int gy = wrap_fast(ws1 + wy, g.nf[1]), gz = wrap_fast(ws2 + wz, g.nf[2]);
+        const bool ok = cg0 + cc < g.n_coil;
+        const float2 *src = ok ? pb + (int64_t)cc * g.G + (int64_t)gy * g.nf[2] + gz : pb;
+        cp_async8(dst + el, src, ok ? 8 : 0);
     }
 }
 
@@ -208,7 +205,6 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int c = lane % CG, q = lane / CG;
     const float rWZ = 1.f / (float)WZ;
-    float2 pf[kPlanePrefetch];
 
     for (int base_s = 0; base_s < sub.z; base_s += NS) {
         const int n = min(NS, sub.z - base_s);
@@ -233,13 +229,17 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
             }
         }
         for (int i = threadIdx.x; i < n * CG; i += blockDim.x) st_acc[i] = make_float2(0.f, 0.f);
-        plane_load<CG>(pf, base, g, cg0, wrap_fast(ws0, g.nf[0]), ws1, ws2, WZ, PC, rWZ);
-        plane_store(pf, planes, PC);
+        plane_copy<CG>(planes, base, g, cg0, wrap_fast(ws0, g.nf[0]), ws1, ws2, WZ, PC, rWZ);
+        cp_async_wait_all();
         __syncthreads();
 
         for (int px = 0; px < WX; ++px) {
             const float2 *cur = planes + (px & 1) * PC;
-            if (px + 1 < WX) plane_load<CG>(pf, base, g, cg0, wrap_fast(ws0 + px + 1, g.nf[0]), ws1, ws2, WZ, PC, rWZ);
+            // the next plane's copies run while this one is used (its buffer was last read
+            // before the previous barrier)
+            if (px + 1 < WX)
+                plane_copy<CG>(planes + ((px + 1) & 1) * PC, base, g, cg0, wrap_fast(ws0 + px + 1, g.nf[0]), ws1, ws2,
+                               WZ, PC, rWZ);
             for (int s = warp; s < n; s += nw) {
                 const int4 r = st_r[s];
                 const int kx = px - r.x;
@@ -249,10 +249,19 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
 #pragma unroll
                 for (int t = 0; t < L::KT; ++t) at[t] = make_float2(0.f, 0.f);
                 const float2 *rowbase = cur + ((size_t)r.y * WZ + r.z) * CG + c;
+                float wys[(L::WMAX + 3) & ~3];  // y weights by 16-byte broadcast loads
+#pragma unroll
+                for (int k4 = 0; k4 < (L::WMAX + 3) / 4; ++k4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(w + 16 + 4 * k4);
+                    wys[4 * k4] = v.x;
+                    wys[4 * k4 + 1] = v.y;
+                    wys[4 * k4 + 2] = v.z;
+                    wys[4 * k4 + 3] = v.w;
+                }
 #pragma unroll
                 for (int ky = 0; ky < L::WMAX; ++ky) {
                     if (WT == 0 && ky >= W) break;
-                    const float wy = w[16 + ky];
+                    const float wy = wys[ky];
                     const float2 wy2 = make_float2(wy, wy);
                     const float2 *row = rowbase + (size_t)ky * WZ * CG;
 #pragma unroll
@@ -281,7 +290,7 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
                     acc.y = fmaf(wx, ay, acc.y);
                 }
             }
-            if (px + 1 < WX) plane_store(pf, planes + ((px + 1) & 1) * PC, PC);
+            cp_async_wait_all();
             __syncthreads();
         }
 
@@ -304,7 +313,8 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
 // shared memory of k_interp3d_planes, or 0 when a plane does not fit the register prefetch
 inline size_t interp3d_planes_smem_bytes(const Geom &g, int cg, int threads) {
     const int PC = (g.tile[1] + g.W - 1) * (g.tile[2] + g.W - 1) * cg;
-    if (g.dim != 3 || g.W > 16 || (cg != 4 && cg != 8) || PC > kPlanePrefetch * threads) return 0;
+    (void)threads;
+    if (g.dim != 3 || g.W > 16 || (cg != 4 && cg != 8) || PC > kPlaneMaxElems) return 0;
     return 2 * (size_t)PC * sizeof(float2) + kPlaneSamples * (48 * sizeof(float) + sizeof(int4)) +
            (size_t)kPlaneSamples * cg * sizeof(float2);
 }
