@@ -228,7 +228,12 @@ int dir_type1(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_FORWARD : 
 int dir_type2(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_INVERSE : GBN_FFT_FORWARD; }
 
 int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, float2 *grid, cudaStream_t s) {
-    GBN_CUDA(launch_zero_split(p->gs, p->split_tiles.as<uint32_t>(), p->n_split, grid, s));
+    // tiles covered by several work items start from zero; when they are most of the grid
+    // (dense trajectories), one memset of the whole grid is cheaper than per-tile blocks
+    if (2 * p->n_split > (int64_t)p->gs.ntiles * p->gs.n_traj)
+        GBN_CUDA(cudaMemsetAsync(grid, 0, sizeof(float2) * (size_t)p->G * (size_t)p->n_inst, s));
+    else
+        GBN_CUDA(launch_zero_split(p->gs, p->split_tiles.as<uint32_t>(), p->n_split, grid, s));
     SpreadArgs a;
     a.g = p->gs;
     a.subs = p->spread_subs.as<int4>();
