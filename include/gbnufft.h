@@ -206,6 +206,49 @@ int gbn_graph_capture_normal(gbn_plan *plan, const void *x, gbn_layout x_layout,
 int gbn_graph_launch(gbn_graph *graph, gbn_stream_t stream);
 int gbn_graph_destroy(gbn_graph *graph);
 
+/* ---- solvers on the normal operator (pics/CS_MRI_solvers_func.py, pics/proximal_func.py) ---- */
+/* Vectors (x, rhs): with sens, one image per trajectory group, (n_traj, pixels); without,
+ * the plan's coil-last images (n_traj, pixels, n_coil); contiguous complex64, device.  The
+ * normal operator N is gbn_sense_normal (sens != NULL) or gbn_type21 (sens == NULL) with
+ * dcf (may be NULL).  Each iteration (operator + vector kernels) is one CUDA graph, captured
+ * on the first call and replayed while the operator inputs, the workspace and the points
+ * stay the same; all scalars stay in device memory, so the host never waits.  The plan
+ * allocates its solver workspace (5 vectors) on first use.  Calls on one plan must not
+ * overlap. */
+#define GBN_SOLVE_X0 1        /* x holds the initial guess (else the solve starts from 0) */
+#define GBN_SOLVE_NO_GRAPH 2  /* launch every kernel directly instead of replaying a graph */
+#define GBN_SOLVE_FISTA 4     /* gbn_ista_haar: FISTA (FIST_32) instead of IST (IST_32) */
+/* Linear CG on N x = rhs, n_iter iterations: the reference has no CG-SENSE routine (its
+ * linear CG on the normal equations, pics/proximal_func.py:379-406, is commented out), so
+ * this is that algorithm with forward_backward as N.  Inner products in FP64; res_norms
+ * (device double[n_iter], may be NULL) receives ||r|| after every iteration. */
+int gbn_cg_sense(gbn_plan *plan, const void *sens, gbn_layout sens_layout, const float *dcf,
+                 const void *rhs, void *x, int32_t n_iter, double *res_norms, int32_t flags,
+                 gbn_stream_t stream);
+/* IST_32 (CS_MRI_solvers_func.py:75-86) or FIST_32 (:207-224) with rhs = A^H b (the
+ * solvers' invAb), the transform T = level-`level` orthonormal Haar over the spatial axes
+ * (DWTnd('haar'), pics/operators_class.py:394-416; level 0 = identity: IST_22 / FIST_22) and
+ * prox_l1_Tf_soft_thresh2 (proximal_func.py:46-52).  Every image axis must be a multiple
+ * of 2^level and dim * level <= 12.  x receives the final iterate. */
+int gbn_ista_haar(gbn_plan *plan, const void *sens, gbn_layout sens_layout, const float *dcf,
+                  const void *rhs, void *x, int32_t n_iter, float step, float th, int32_t level,
+                  int32_t flags, gbn_stream_t stream);
+
+/* ---- wavelet and proximal operators (no plan) ------------------------------------- */
+/* Orthonormal level-`level` Haar transform of complex64 arrays (n_outer, s0[, s1[, s2]],
+ * n_inner) over the dim spatial axes (contiguous, device): DWTnd('haar', level, axes)
+ * .backward (image -> coefficients, inverse = 0) and .forward (inverse = 1), pics/
+ * operators_class.py:394-416, coefficients in the layout of pywt.coeffs_to_array
+ * (approximation block first along every axis, then each level's detail blocks, coarsest
+ * first).  in and out must differ.  Axis sizes multiples of 2^level; dim * level <= 12. */
+int gbn_haar_dwt(int32_t dim, const int32_t *shape, int32_t level, int64_t n_outer, int64_t n_inner,
+                 const void *in, void *out, int32_t inverse, gbn_stream_t stream);
+/* out = H^-1 soft(H in, th) with H the Haar transform above and soft the reference's
+ * prox_l1_soft_thresh2 (proximal_func.py:20-24): v / (|v| + 1e-6) * max(|v| - th, 0);
+ * prox_l1_Tf_soft_thresh2 (:46-52) with DWTnd('haar').  in == out allowed. */
+int gbn_prox_haar(int32_t dim, const int32_t *shape, int32_t level, int64_t n_outer, int64_t n_inner,
+                  const void *in, float th, void *out, gbn_stream_t stream);
+
 /* ---- allocation-free spread ------------------------------------------------------------ */
 /* No counterpart in the reference.  The 2-D spread of gbn_spread (samples -> oversampled
  * grid, (n_coil, nf1, nf2) complex64, nf from eps as gbn_grid_params) for callers that

@@ -110,6 +110,21 @@ struct gbn_plan {
         spread_tile_off, home_tile_off, nsub, sub_off, spread_subs, interp_subs, cub_tmp, scratch,
         stage_in, stage_out, stage_w, split_tiles;
     int64_t n_dup = 0, n_spread_sub = 0, n_interp_sub = 0;
+    uint64_t points_gen = 0;  // bumped by every gbn_set_points: captured graphs hold its buffers
+
+    // solvers: workspace (state, partial sums, residual norms, vectors) and the captured
+    // iteration graph of the last solve of each kind (CG, IST, FISTA)
+    DevBuf solve_ws;
+    struct SolveGraph {
+        cudaGraphExec_t exec = nullptr;
+        const void *sens = nullptr;
+        gbn_layout sl{};
+        const float *dcf = nullptr;
+        const void *ws = nullptr;
+        uint64_t gen = 0;
+        int cap = 0, level = -1;
+        float step = 0.f, th = 0.f;
+    } solve_graph[3];
 };
 
 struct gbn_graph {
@@ -512,6 +527,7 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
     GBN_CUDA(cudaStreamSynchronize(s));
     p->n_dense_sub = counts[0];
     p->n_split = counts[1];
+    p->points_gen += 1;
     p->points_set = true;
     return GBN_OK;
 }
@@ -727,7 +743,9 @@ int gbn_plan_destroy(gbn_plan *p) {
                       &p->dup_keys, &p->dup_vals, &p->dup_keys_sorted, &p->dup_idx, &p->dup_pts,
                       &p->spread_count, &p->spread_tile_off, &p->home_tile_off, &p->nsub, &p->sub_off,
                       &p->spread_subs, &p->interp_subs, &p->cub_tmp, &p->scratch, &p->stage_in,
-                      &p->stage_out, &p->stage_w, &p->split_tiles};
+                      &p->stage_out, &p->stage_w, &p->split_tiles, &p->solve_ws};
+    for (gbn_plan::SolveGraph &sg : p->solve_graph)
+        if (sg.exec) cudaGraphExecDestroy(sg.exec);
     for (DevBuf *b : bufs) release(*b);
     delete p;
     return GBN_OK;
@@ -959,6 +977,193 @@ int gbn_graph_destroy(gbn_graph *g) {
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
     delete g;
+    return GBN_OK;
+}
+
+}  // extern "C"
+
+// ---- solvers ------------------------------------------------------------------------------
+namespace {
+
+constexpr size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Vectors of a solve: x is one image per trajectory group, (n_traj, pixels) with sens, or
+// the plan's coil-last images (n_traj, pixels, n_coil) without; contiguous complex64.
+struct SolveVecs {
+    int64_t n = 0;            // complex elements per vector
+    gbn_layout layout{};      // of every vector, for the normal operator
+    HaarGeom h{};
+    SolveState *st = nullptr;
+    double *partial = nullptr, *norms = nullptr;
+    float2 *v[5] = {};
+    int cap = 0;
+};
+
+int solve_setup(gbn_plan *p, const void *sens, int n_iter, int level, SolveVecs &sv) {
+    const int64_t P = (int64_t)p->m[0] * p->m[1] * p->m[2];
+    const int64_t inner = sens ? 1 : p->desc.n_coil;
+    sv.n = P * inner * p->desc.n_traj;
+    sv.layout = sens ? gbn_layout{P, 0, 1} : gbn_layout{P * inner, 1, inner};
+    const int32_t shape[3] = {p->m[0], p->m[1], p->m[2]};
+    if (level >= 0) GBN_TRY(haar_geom(p->dim, shape, level, p->desc.n_traj, inner, sv.h));
+    sv.cap = 64;
+    while (sv.cap < n_iter) sv.cap *= 2;
+    const size_t vec = align256(sizeof(float2) * (size_t)sv.n);
+    const size_t off_partial = align256(sizeof(SolveState));
+    const size_t off_norms = off_partial + align256(sizeof(double) * kRedBlocks);
+    const size_t off_vec = off_norms + align256(sizeof(double) * (size_t)sv.cap);
+    GBN_TRY(ensure(p, p->solve_ws, off_vec + 5 * vec));
+    char *base = p->solve_ws.as<char>();
+    sv.st = (SolveState *)base;
+    sv.partial = (double *)(base + off_partial);
+    sv.norms = (double *)(base + off_norms);
+    for (int i = 0; i < 5; ++i) sv.v[i] = (float2 *)(base + off_vec + i * vec);
+    return GBN_OK;
+}
+
+int solve_normal(gbn_plan *p, const SolveVecs &sv, const void *sens, gbn_layout sl, const float *dcf,
+                 const float2 *in, float2 *out, cudaStream_t s) {
+    return sens ? gbn_sense_normal(p, in, sv.layout, sens, sl, dcf, out, sv.layout, (gbn_stream_t)s)
+                : gbn_type21(p, in, sv.layout, out, sv.layout, dcf, (gbn_stream_t)s);
+}
+
+// One solver iteration as a callable; with a graph it is captured once per (kind, operator
+// inputs, workspace, points) and replayed.
+template <typename F>
+int run_iterations(gbn_plan *p, int kind, const void *sens, gbn_layout sl, const float *dcf, const SolveVecs &sv,
+                   int level, float step, float th, int n, bool use_graph, cudaStream_t s, F &&iteration) {
+    if (n <= 0) return GBN_OK;
+    if (!use_graph) {
+        for (int i = 0; i < n; ++i) GBN_TRY(iteration(s));
+        return GBN_OK;
+    }
+    gbn_plan::SolveGraph &g = p->solve_graph[kind];
+    const bool hit = g.exec && g.sens == sens && g.sl.traj_stride == sl.traj_stride &&
+                     g.sl.coil_stride == sl.coil_stride && g.sl.elem_stride == sl.elem_stride && g.dcf == dcf &&
+                     g.ws == p->solve_ws.p && g.gen == p->points_gen && g.cap == sv.cap && g.level == level &&
+                     g.step == step && g.th == th;
+    if (!hit) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = gbn_plan::SolveGraph{};
+        cudaStream_t cs;
+        GBN_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        int st = GBN_OK;
+        cudaGraph_t graph = nullptr;
+        if (e == cudaSuccess) {
+            st = iteration(cs);
+            cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+            if (st == GBN_OK && e2 == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+            else if (st == GBN_OK) e = e2;
+            if (graph) cudaGraphDestroy(graph);
+        }
+        cudaStreamDestroy(cs);
+        if (st != GBN_OK || e != cudaSuccess) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g = gbn_plan::SolveGraph{};
+            cudaGetLastError();
+            return st != GBN_OK ? st : fail(GBN_ERR_CUDA, std::string("solver graph capture: ") + cudaGetErrorString(e));
+        }
+        g.sens = sens;
+        g.sl = sl;
+        g.dcf = dcf;
+        g.ws = p->solve_ws.p;
+        g.gen = p->points_gen;
+        g.cap = sv.cap;
+        g.level = level;
+        g.step = step;
+        g.th = th;
+    }
+    for (int i = 0; i < n; ++i) GBN_CUDA(cudaGraphLaunch(g.exec, s));
+    return GBN_OK;
+}
+
+int check_solve(const gbn_plan *p, const void *rhs, const void *x, int n_iter) {
+    GBN_TRY(check_plan(p, true));
+    if (!rhs || !x) return fail(GBN_ERR_ARG, "null buffer");
+    if (n_iter < 1) return fail(GBN_ERR_ARG, "n_iter must be >= 1");
+    return GBN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbn_cg_sense(gbn_plan *p, const void *sens, gbn_layout sl, const float *dcf, const void *rhs, void *x,
+                 int32_t n_iter, double *res_norms, int32_t flags, gbn_stream_t stream) {
+    GBN_TRY(check_solve(p, rhs, x, n_iter));
+    cudaStream_t s = (cudaStream_t)stream;
+    SolveVecs sv;
+    GBN_TRY(solve_setup(p, sens, n_iter, -1, sv));
+    float2 *xv = sv.v[0], *r = sv.v[1], *pv = sv.v[2], *q = sv.v[3];
+    const size_t bytes = sizeof(float2) * (size_t)sv.n;
+    GBN_CUDA(cudaMemsetAsync(sv.st, 0, sizeof(SolveState), s));
+    if (flags & GBN_SOLVE_X0) {
+        GBN_CUDA(cudaMemcpyAsync(xv, x, bytes, cudaMemcpyDeviceToDevice, s));
+        GBN_TRY(solve_normal(p, sv, sens, sl, dcf, xv, q, s));
+        GBN_CUDA(launch_cg_start((const float2 *)rhs, q, r, pv, sv.n, sv.partial, sv.st, s));
+    } else {
+        GBN_CUDA(cudaMemsetAsync(xv, 0, bytes, s));
+        GBN_CUDA(launch_cg_start((const float2 *)rhs, nullptr, r, pv, sv.n, sv.partial, sv.st, s));
+    }
+    auto iteration = [&](cudaStream_t cs) -> int {
+        GBN_TRY(solve_normal(p, sv, sens, sl, dcf, pv, q, cs));
+        GBN_CUDA(launch_cg_alpha(pv, q, sv.n, sv.partial, sv.st, cs));
+        GBN_CUDA(launch_cg_update(xv, r, pv, q, sv.n, sv.partial, sv.st, sv.norms, sv.cap, cs));
+        GBN_CUDA(launch_cg_direction(r, pv, sv.n, sv.st, cs));
+        return GBN_OK;
+    };
+    GBN_TRY(run_iterations(p, 0, sens, sl, dcf, sv, -1, 0.f, 0.f, n_iter, !(flags & GBN_SOLVE_NO_GRAPH), s,
+                           iteration));
+    GBN_CUDA(cudaMemcpyAsync(x, xv, bytes, cudaMemcpyDeviceToDevice, s));
+    if (res_norms)
+        GBN_CUDA(cudaMemcpyAsync(res_norms, sv.norms, sizeof(double) * n_iter, cudaMemcpyDeviceToDevice, s));
+    return GBN_OK;
+}
+
+int gbn_ista_haar(gbn_plan *p, const void *sens, gbn_layout sl, const float *dcf, const void *rhs, void *x,
+                  int32_t n_iter, float step, float th, int32_t level, int32_t flags, gbn_stream_t stream) {
+    GBN_TRY(check_solve(p, rhs, x, n_iter));
+    if (!std::isfinite(step) || !(th >= 0.f) || !std::isfinite(th))
+        return fail(GBN_ERR_ARG, "step must be finite and th finite and >= 0");
+    if (level < 0) return fail(GBN_ERR_ARG, "level must be >= 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    SolveVecs sv;
+    GBN_TRY(solve_setup(p, sens, n_iter, level, sv));
+    const size_t bytes = sizeof(float2) * (size_t)sv.n;
+    const bool fista = (flags & GBN_SOLVE_FISTA) != 0;
+    float2 *acc = sv.v[0], *xv = sv.v[1], *q = sv.v[2], *b = sv.v[3], *x_pre = sv.v[4];
+    GBN_CUDA(cudaMemsetAsync(sv.st, 0, sizeof(SolveState), s));
+    GBN_CUDA(cudaMemcpyAsync(b, rhs, bytes, cudaMemcpyDeviceToDevice, s));
+    HaarStepArgs a{};
+    a.h = sv.h;
+    a.acc = acc;
+    a.rhs = b;
+    a.step = step;
+    a.th = th;
+    a.st = sv.st;
+    if (fista) {
+        // y (the normal operator's input) lives in xv; x_pre carries x between iterations
+        GBN_CUDA(launch_fista_start(b, step, xv, acc, x_pre, sv.n, sv.st, s));
+        a.q = q;
+        a.x_pre = x_pre;
+        a.y = xv;
+    } else {
+        // IST_32: x_acc = step * rhs, x = prox(x_acc); then (normal, update + prox) n_iter - 1
+        // times: the reference's last normal-operator call only feeds an x_acc it never uses
+        GBN_CUDA(launch_scale(b, step, acc, sv.n, s));
+        a.x_out = xv;
+        GBN_CUDA(launch_haar_step(a, false, s));
+        a.q = q;
+    }
+    auto iteration = [&](cudaStream_t cs) -> int {
+        GBN_TRY(solve_normal(p, sv, sens, sl, dcf, xv, q, cs));
+        GBN_CUDA(launch_haar_step(a, fista, cs));
+        return GBN_OK;
+    };
+    GBN_TRY(run_iterations(p, fista ? 2 : 1, sens, sl, dcf, sv, level, step, th, fista ? n_iter : n_iter - 1,
+                           !(flags & GBN_SOLVE_NO_GRAPH), s, iteration));
+    GBN_CUDA(cudaMemcpyAsync(x, fista ? x_pre : xv, bytes, cudaMemcpyDeviceToDevice, s));
     return GBN_OK;
 }
 

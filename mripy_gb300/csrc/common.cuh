@@ -186,4 +186,59 @@ cudaError_t launch_pad_sense(const DeapodArgs &a, const float2 *x, gbn_layout XL
 cudaError_t launch_crop_sense(const DeapodArgs &a, const float2 *grid, const float2 *sens,
                               gbn_layout SL, float2 *x, gbn_layout XL, cudaStream_t s);
 
+// solver.cu: vector kernels of the CG and IST/FISTA solvers
+// Scalars of one solve, kept in device memory so no iteration waits on the host.
+struct SolveState {
+    double rs;       // <r, r> (CG)
+    double alpha;    // rs / Re<p, Ap>
+    double beta;     // rs_new / rs
+    double t;        // FISTA t_k
+    unsigned done;   // blocks of the running reduction that have finished (last-block test)
+    int it;          // CG iterations completed = residual norms written
+};
+constexpr int kRedBlocks = 304;  // upper bound on the blocks of one reduction (2 per SM)
+cudaError_t launch_cg_start(const float2 *rhs, const float2 *q, float2 *r, float2 *p, int64_t n,
+                            double *partial, SolveState *st, cudaStream_t s);
+cudaError_t launch_cg_alpha(const float2 *p, const float2 *q, int64_t n, double *partial, SolveState *st,
+                            cudaStream_t s);
+cudaError_t launch_cg_update(float2 *x, float2 *r, const float2 *p, const float2 *q, int64_t n,
+                             double *partial, SolveState *st, double *norms, int cap, cudaStream_t s);
+cudaError_t launch_cg_direction(const float2 *r, float2 *p, int64_t n, const SolveState *st,
+                                cudaStream_t s);
+cudaError_t launch_fista_start(const float2 *rhs, float step, float2 *y, float2 *y_acc, float2 *x_pre,
+                               int64_t n, SolveState *st, cudaStream_t s);
+cudaError_t launch_scale(const float2 *in, float a, float2 *out, int64_t n, cudaStream_t s);
+
+// Images as Haar tiles: (n_outer, s0[, s1[, s2]], n_inner) complex64, contiguous; a
+// level-L orthonormal Haar transform over the dim spatial axes acts on disjoint tiles of
+// 2^L cells per axis, so one thread block holds whole tiles in shared memory.
+struct HaarGeom {
+    int dim;             // 1, 2 or 3 spatial axes
+    int L;               // levels; tile edge T = 2^L
+    int s[3];            // spatial sizes (1 beyond dim), s[dim-1] fastest
+    int nt[3];           // tiles per axis = s >> L
+    int64_t tiles_img;   // tiles per image
+    int64_t n_img;       // n_outer * n_inner
+    int64_t inner;       // images interleaved element by element (trailing axis)
+    int64_t P;           // pixels per image
+    int tpb_log;         // log2 tiles per thread block
+};
+int haar_geom(int dim, const int32_t *shape, int level, int64_t n_outer, int64_t n_inner, HaarGeom &h);
+// one IST/FISTA step on Haar tiles (pics/CS_MRI_solvers_func.py:75-86, 207-224):
+//   update:    acc -= step * (q - rhs)            (skipped when q is null)
+//   prox:      x = H^-1 soft(H acc, th)           (proximal_func.py:20-24, 46-52)
+//   momentum:  y = x + c (x - x_pre), x_pre = x   (FISTA; st->t advanced on the device)
+//   else:      x_out = x
+struct HaarStepArgs {
+    HaarGeom h;
+    float2 *acc;
+    const float2 *q, *rhs;
+    float step, th;
+    float2 *x_out;             // IST
+    float2 *x_pre, *y;         // FISTA
+    SolveState *st;            // FISTA
+};
+cudaError_t launch_haar_step(const HaarStepArgs &a, bool momentum, cudaStream_t s);
+cudaError_t launch_haar_dwt(const HaarGeom &h, const float2 *in, float2 *out, bool inverse, cudaStream_t s);
+
 }  // namespace gbn

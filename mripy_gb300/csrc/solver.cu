@@ -1,0 +1,544 @@
+// Solver kernels: the vector work of linear CG (CG-SENSE) and of mripy's IST/FISTA with a
+// Haar-wavelet soft threshold, so that a whole solver iteration runs on the GPU with its
+// scalars in device memory (one CUDA graph per iteration, no host synchronisation).
+//
+//  * CG: r = rhs - A x, p = r; per iteration alpha = <r,r>/Re<p,Ap>, x += alpha p,
+//    r -= alpha Ap, beta = <r,r>_new/<r,r>, p = r + beta p.  Inner products are summed in
+//    FP64: per-block partials, then the last block to finish adds them in block order
+//    (deterministic for a given vector length) and writes the scalars.  The reference has
+//    no CG-SENSE routine (its linear CG on the normal equations, pics/proximal_func.py:
+//    379-406, is commented out); this is that algorithm with forward_backward as A.
+//  * IST/FISTA step (pics/CS_MRI_solvers_func.py:75-86 IST_32, :207-224 FIST_32): the
+//    gradient update acc -= step (A^H A x - A^H b), the prox x = invT(soft(T acc, th))
+//    (pics/proximal_func.py:46-52, soft threshold :20-24: v / (|v| + 1e-6) * max(|v| - th, 0))
+//    with T the orthonormal level-L Haar transform (DWTnd, pics/operators_class.py:394-416,
+//    wavelet 'haar'), and FISTA's momentum y = x + (t_k - 1)/t_{k+1} (x - x_pre).  A level-L
+//    Haar transform maps each tile of 2^L cells per axis onto itself, so one block loads
+//    whole tiles into shared memory, runs L forward levels, thresholds, runs L inverse
+//    levels and writes x: one read and one write of each vector per step.
+//  * gbn_haar_dwt: the same tile transform, writing (or reading) the coefficients in the
+//    layout of pywt.coeffs_to_array (approximation block first along every axis, then the
+//    detail blocks of the coarsest level, ..., the finest level's last).
+#include <cmath>
+#include <string>
+
+#include "common.cuh"
+
+namespace gbn {
+namespace {
+
+constexpr int kVecThreads = 256;
+constexpr int kHaarThreads = 256;
+constexpr int kHaarMaxElems = 4096;     // complex cells per block (32 KB of shared memory)
+constexpr int kHaarPairs = kHaarMaxElems / 2 / kHaarThreads;  // butterflies per thread per pass
+
+int vec_blocks(int64_t n) {
+    const int64_t b = (n + (int64_t)kVecThreads * 4 - 1) / ((int64_t)kVecThreads * 4);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, kRedBlocks));
+}
+
+// block-wide FP64 sum; the result is valid in thread 0.  Fixed order for a given blockDim.
+__device__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();  // sh may still be read by a previous call
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+
+// Adds this block's share v into the grid total.  Returns true in thread 0 of the last block
+// to finish, with *total set to the sum of the per-block partials taken in block order; the
+// done counter is reset for the next reduction.  No thread waits for another block.
+__device__ bool grid_sum(double v, double *partial, unsigned *done, double *total) {
+    __shared__ double sh[32];
+    __shared__ bool last;
+    const double b = block_sum(v, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += __ldcg(&partial[i]);
+    s = block_sum(s, sh);
+    if (threadIdx.x != 0) return false;
+    *done = 0;
+    *total = s;
+    return true;
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_cg_start(const float2 *__restrict__ rhs,
+                                                          const float2 *__restrict__ q, float2 *__restrict__ r,
+                                                          float2 *__restrict__ p, int64_t n, double *partial,
+                                                          SolveState *st) {
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float2 v = rhs[i];
+        if (q) {
+            const float2 w = q[i];
+            v.x -= w.x;
+            v.y -= w.y;
+        }
+        r[i] = v;
+        p[i] = v;
+        acc += (double)v.x * v.x + (double)v.y * v.y;
+    }
+    double tot;
+    if (grid_sum(acc, partial, &st->done, &tot)) {
+        st->rs = tot;
+        st->alpha = 0.0;
+        st->beta = 0.0;
+        st->t = 1.0;
+        st->it = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_cg_alpha(const float2 *__restrict__ p, const float2 *__restrict__ q,
+                                                          int64_t n, double *partial, SolveState *st) {
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 a = p[i], b = q[i];
+        acc += (double)a.x * b.x + (double)a.y * b.y;  // Re(conj(p) q)
+    }
+    double pq;
+    if (grid_sum(acc, partial, &st->done, &pq)) {
+        const double a = st->rs / pq;
+        // an exactly converged residual (rs = 0) or a vanishing curvature leaves x where it is
+        st->alpha = (st->rs > 0.0 && pq != 0.0 && isfinite(a)) ? a : 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_cg_update(float2 *__restrict__ x, float2 *__restrict__ r,
+                                                           const float2 *__restrict__ p,
+                                                           const float2 *__restrict__ q, int64_t n,
+                                                           double *partial, SolveState *st, double *norms,
+                                                           int cap) {
+    const float a = (float)st->alpha;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 pv = p[i], qv = q[i];
+        float2 xv = x[i], rv = r[i];
+        xv.x += a * pv.x;
+        xv.y += a * pv.y;
+        rv.x -= a * qv.x;
+        rv.y -= a * qv.y;
+        x[i] = xv;
+        r[i] = rv;
+        acc += (double)rv.x * rv.x + (double)rv.y * rv.y;
+    }
+    double rs_new;
+    if (grid_sum(acc, partial, &st->done, &rs_new)) {
+        const double b = rs_new / st->rs;
+        st->beta = (st->rs > 0.0 && isfinite(b)) ? b : 0.0;
+        st->rs = rs_new;
+        if (norms && st->it < cap) norms[st->it] = sqrt(rs_new);
+        st->it += 1;
+    }
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_cg_direction(const float2 *__restrict__ r, float2 *__restrict__ p,
+                                                              int64_t n, const SolveState *st) {
+    const float b = (float)st->beta;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 rv = r[i];
+        float2 pv = p[i];
+        pv.x = rv.x + b * pv.x;
+        pv.y = rv.y + b * pv.y;
+        p[i] = pv;
+    }
+}
+
+// FIST_32's start (CS_MRI_solvers_func.py:207-211): y = step * rhs, y_acc = 0, x_pre = y, t = 1
+__global__ void __launch_bounds__(kVecThreads) k_fista_start(const float2 *__restrict__ rhs, float step,
+                                                             float2 *__restrict__ y, float2 *__restrict__ y_acc,
+                                                             float2 *__restrict__ x_pre, int64_t n,
+                                                             SolveState *st) {
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i0 == 0) {
+        st->t = 1.0;
+        st->done = 0;
+        st->it = 0;
+    }
+    for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 b = rhs[i];
+        const float2 v = make_float2(step * b.x, step * b.y);
+        y[i] = v;
+        x_pre[i] = v;
+        y_acc[i] = make_float2(0.f, 0.f);
+    }
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_scale(const float2 *__restrict__ in, float a,
+                                                       float2 *__restrict__ out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = in[i];
+        out[i] = make_float2(a * v.x, a * v.y);
+    }
+}
+
+// ---- Haar tiles ------------------------------------------------------------------------
+// Element e of a block: tile (e >> (DIM*L)) of the block, in-tile cell c with c[DIM-1]
+// fastest, L bits per axis.  In-tile coefficients after the forward levels sit where
+// pywt's layout would put them for an image of one tile: level l acts on the leading
+// (T >> l)^DIM cube, approximations in the lower half of every axis.
+template <int DIM>
+__device__ __forceinline__ int64_t haar_addr(const HaarGeom &h, int64_t tile, int el, int cell[DIM], int tc[DIM]) {
+    const int64_t img = tile / h.tiles_img;
+    int64_t tr = tile - img * h.tiles_img;
+    const int T = 1 << h.L;
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; --d) {
+        tc[d] = (int)(tr % h.nt[d]);
+        tr /= h.nt[d];
+        cell[d] = (el >> (h.L * (DIM - 1 - d))) & (T - 1);
+    }
+    int64_t pix = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) pix = pix * h.s[d] + (int64_t)tc[d] * T + cell[d];
+    const int64_t outer = img / h.inner;
+    return outer * h.P * h.inner + (img - outer * h.inner) + pix * h.inner;
+}
+
+// position of in-tile coefficient `cell` of tile `tc` in pywt.coeffs_to_array's layout
+template <int DIM>
+__device__ __forceinline__ int64_t haar_coeff_addr(const HaarGeom &h, int64_t tile, const int cell[DIM],
+                                                   const int tc[DIM]) {
+    int m = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) m = max(m, cell[d]);
+    // band level j: T >> j <= m < T >> (j - 1); m = 0 is the level-L approximation
+    const int j = m == 0 ? h.L : h.L - (31 - __clz(m));
+    const int hj = 1 << (h.L - j);
+    int64_t pix = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const int g = cell[d] >= hj ? (h.s[d] >> j) + tc[d] * hj + (cell[d] - hj) : tc[d] * hj + cell[d];
+        pix = pix * h.s[d] + g;
+    }
+    const int64_t img = tile / h.tiles_img;
+    const int64_t outer = img / h.inner;
+    return outer * h.P * h.inner + (img - outer * h.inner) + pix * h.inner;
+}
+
+// One butterfly pass along axis `ax` over the leading n^DIM cube of every tile in the
+// block: forward  (c_ax = 2k, 2k+1) -> (k, n/2 + k) as ((e + o)/sqrt2, (e - o)/sqrt2);
+// inverse the transpose.  Pairs are read into registers, then written after a barrier.
+template <int DIM, bool INV>
+__device__ void haar_pass(float2 *sm, int L, int ln, int ax, int ntiles_blk) {
+    const int per_tile_log = DIM * ln - 1;
+    const int total = ntiles_blk << per_tile_log;
+    const float r2 = 0.70710678118654752440f;
+    float2 va[kHaarPairs], vb[kHaarPairs];
+    int ia[kHaarPairs], ib[kHaarPairs];
+#pragma unroll
+    for (int j = 0; j < kHaarPairs; ++j) {
+        const int q = threadIdx.x + j * kHaarThreads;
+        ia[j] = -1;
+        if (q >= total) continue;
+        const int tl = q >> per_tile_log;
+        int r = q & ((1 << per_tile_log) - 1);
+        int k = 0, base = tl << (DIM * L);
+#pragma unroll
+        for (int d = DIM - 1; d >= 0; --d) {
+            const int eb = d == ax ? ln - 1 : ln;
+            const int cd = r & ((1 << eb) - 1);
+            r >>= eb;
+            if (d == ax)
+                k = cd;
+            else
+                base += cd << (L * (DIM - 1 - d));
+        }
+        const int stride_ax = 1 << (L * (DIM - 1 - ax));
+        const int lo = base + (2 * k) * stride_ax, hi = base + (2 * k + 1) * stride_ax;
+        const int a_pos = base + k * stride_ax, d_pos = base + ((1 << (ln - 1)) + k) * stride_ax;
+        if (!INV) {
+            const float2 e = sm[lo], o = sm[hi];
+            va[j] = make_float2((e.x + o.x) * r2, (e.y + o.y) * r2);
+            vb[j] = make_float2((e.x - o.x) * r2, (e.y - o.y) * r2);
+            ia[j] = a_pos;
+            ib[j] = d_pos;
+        } else {
+            const float2 a = sm[a_pos], d = sm[d_pos];
+            va[j] = make_float2((a.x + d.x) * r2, (a.y + d.y) * r2);
+            vb[j] = make_float2((a.x - d.x) * r2, (a.y - d.y) * r2);
+            ia[j] = lo;
+            ib[j] = hi;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kHaarPairs; ++j) {
+        if (ia[j] < 0) continue;
+        sm[ia[j]] = va[j];
+        sm[ib[j]] = vb[j];
+    }
+    __syncthreads();
+}
+
+template <int DIM>
+__device__ void haar_forward(float2 *sm, int L, int ntiles_blk) {
+    for (int l = 0; l < L; ++l)
+        for (int ax = 0; ax < DIM; ++ax) haar_pass<DIM, false>(sm, L, L - l, ax, ntiles_blk);
+}
+template <int DIM>
+__device__ void haar_inverse(float2 *sm, int L, int ntiles_blk) {
+    for (int l = L - 1; l >= 0; --l)
+        for (int ax = 0; ax < DIM; ++ax) haar_pass<DIM, true>(sm, L, L - l, ax, ntiles_blk);
+}
+
+__device__ __forceinline__ float2 soft_thresh(float2 v, float th) {
+    const float a = sqrtf(v.x * v.x + v.y * v.y);
+    const float s = fmaxf(a - th, 0.f) / (a + 1e-6f);
+    return make_float2(v.x * s, v.y * s);
+}
+
+template <int DIM, bool MOM>
+__global__ void __launch_bounds__(kHaarThreads) k_haar_step(HaarStepArgs a) {
+    extern __shared__ float2 sm[];
+    const HaarGeom &h = a.h;
+    const int tile_log = DIM * h.L;
+    const int blk_elems = 1 << (tile_log + h.tpb_log);
+    const int64_t ntiles = h.tiles_img * h.n_img;
+    const int64_t tile0 = (int64_t)blockIdx.x << h.tpb_log;
+    const int64_t left = ntiles - tile0;
+    const int ntiles_blk = left < ((int64_t)1 << h.tpb_log) ? (int)left : (1 << h.tpb_log);
+    __shared__ float c_mom;
+    __shared__ double t_next;
+    if (MOM && threadIdx.x == 0) {
+        // t_{k+1} = (1 + sqrt(1 + 4 t_k^2)) / 2 (CS_MRI_solvers_func.py:219), in FP64 as numpy
+        const double t = a.st->t;
+        t_next = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
+        c_mom = (float)((t - 1.0) / t_next);
+    }
+    int cell[DIM], tc[DIM];
+    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
+        const int tl = e >> tile_log;
+        if (tl >= ntiles_blk) {
+            sm[e] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const int64_t g = haar_addr<DIM>(h, tile0 + tl, e & ((1 << tile_log) - 1), cell, tc);
+        float2 v = a.acc[g];
+        if (a.q) {
+            const float2 q = a.q[g], b = a.rhs[g];
+            v.x -= a.step * (q.x - b.x);
+            v.y -= a.step * (q.y - b.y);
+            a.acc[g] = v;
+        }
+        sm[e] = v;
+    }
+    __syncthreads();
+    haar_forward<DIM>(sm, h.L, ntiles_blk);
+    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) sm[e] = soft_thresh(sm[e], a.th);
+    __syncthreads();
+    haar_inverse<DIM>(sm, h.L, ntiles_blk);
+    const float c = MOM ? c_mom : 0.f;
+    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
+        const int tl = e >> tile_log;
+        if (tl >= ntiles_blk) continue;
+        const int64_t g = haar_addr<DIM>(h, tile0 + tl, e & ((1 << tile_log) - 1), cell, tc);
+        const float2 x = sm[e];
+        if (MOM) {
+            const float2 xp = a.x_pre[g];
+            a.y[g] = make_float2(x.x + c * (x.x - xp.x), x.y + c * (x.y - xp.y));
+            a.x_pre[g] = x;
+        } else {
+            a.x_out[g] = x;
+        }
+    }
+    if (MOM) {
+        // the last block to finish stores t_{k+1}; every block read t_k before its increment
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&a.st->done, 1u) == gridDim.x - 1) {
+                a.st->t = t_next;
+                a.st->done = 0;
+            }
+        }
+    }
+}
+
+template <int DIM, bool INV>
+__global__ void __launch_bounds__(kHaarThreads) k_haar_dwt(HaarGeom h, const float2 *__restrict__ in,
+                                                           float2 *__restrict__ out) {
+    extern __shared__ float2 sm[];
+    const int tile_log = DIM * h.L;
+    const int blk_elems = 1 << (tile_log + h.tpb_log);
+    const int64_t ntiles = h.tiles_img * h.n_img;
+    const int64_t tile0 = (int64_t)blockIdx.x << h.tpb_log;
+    const int64_t left = ntiles - tile0;
+    const int ntiles_blk = left < ((int64_t)1 << h.tpb_log) ? (int)left : (1 << h.tpb_log);
+    int cell[DIM], tc[DIM];
+    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
+        const int tl = e >> tile_log;
+        if (tl >= ntiles_blk) {
+            sm[e] = make_float2(0.f, 0.f);
+            continue;
+        }
+        int64_t g = haar_addr<DIM>(h, tile0 + tl, e & ((1 << tile_log) - 1), cell, tc);
+        if (INV) g = haar_coeff_addr<DIM>(h, tile0 + tl, cell, tc);
+        sm[e] = in[g];
+    }
+    __syncthreads();
+    if (INV)
+        haar_inverse<DIM>(sm, h.L, ntiles_blk);
+    else
+        haar_forward<DIM>(sm, h.L, ntiles_blk);
+    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
+        const int tl = e >> tile_log;
+        if (tl >= ntiles_blk) continue;
+        int64_t g = haar_addr<DIM>(h, tile0 + tl, e & ((1 << tile_log) - 1), cell, tc);
+        if (!INV) g = haar_coeff_addr<DIM>(h, tile0 + tl, cell, tc);
+        out[g] = sm[e];
+    }
+}
+
+int64_t haar_blocks(const HaarGeom &h) {
+    const int64_t ntiles = h.tiles_img * h.n_img;
+    return (ntiles + ((int64_t)1 << h.tpb_log) - 1) >> h.tpb_log;
+}
+size_t haar_smem(const HaarGeom &h) { return sizeof(float2) << (h.dim * h.L + h.tpb_log); }
+
+}  // namespace
+
+int haar_geom(int dim, const int32_t *shape, int level, int64_t n_outer, int64_t n_inner, HaarGeom &h) {
+    if (dim < 1 || dim > 3) return record_error(GBN_ERR_ARG, "Haar transform: dim must be 1, 2 or 3");
+    if (!shape || level < 0 || n_outer < 1 || n_inner < 1)
+        return record_error(GBN_ERR_ARG, "Haar transform: bad shape, level or image count");
+    if (dim * level > 12)
+        return record_error(GBN_ERR_CAPACITY, "Haar transform: tiles of 2^level cells per axis above 4096 cells");
+    h = HaarGeom{};
+    h.dim = dim;
+    h.L = level;
+    h.P = 1;
+    h.tiles_img = 1;
+    for (int d = 0; d < 3; ++d) {
+        h.s[d] = d < dim ? shape[d] : 1;
+        if (d < dim && (h.s[d] < 1 || (h.s[d] & ((1 << level) - 1))))
+            return record_error(GBN_ERR_ARG, "Haar transform: every axis size must be a multiple of 2^level");
+        h.nt[d] = d < dim ? h.s[d] >> level : 1;
+        h.P *= h.s[d];
+        h.tiles_img *= h.nt[d];
+    }
+    h.inner = n_inner;
+    h.n_img = n_outer * n_inner;
+    // tiles per block: at least 1024 cells per block, at most 4096
+    int tpb_log = 0;
+    while (((dim * level) + tpb_log) < 10) ++tpb_log;
+    h.tpb_log = tpb_log;
+    if (haar_blocks(h) > 0x7fffffff) return record_error(GBN_ERR_CAPACITY, "Haar transform: too many tiles");
+    return GBN_OK;
+}
+
+cudaError_t launch_cg_start(const float2 *rhs, const float2 *q, float2 *r, float2 *p, int64_t n, double *partial,
+                            SolveState *st, cudaStream_t s) {
+    k_cg_start<<<vec_blocks(n), kVecThreads, 0, s>>>(rhs, q, r, p, n, partial, st);
+    return cudaGetLastError();
+}
+cudaError_t launch_cg_alpha(const float2 *p, const float2 *q, int64_t n, double *partial, SolveState *st,
+                            cudaStream_t s) {
+    k_cg_alpha<<<vec_blocks(n), kVecThreads, 0, s>>>(p, q, n, partial, st);
+    return cudaGetLastError();
+}
+cudaError_t launch_cg_update(float2 *x, float2 *r, const float2 *p, const float2 *q, int64_t n, double *partial,
+                             SolveState *st, double *norms, int cap, cudaStream_t s) {
+    k_cg_update<<<vec_blocks(n), kVecThreads, 0, s>>>(x, r, p, q, n, partial, st, norms, cap);
+    return cudaGetLastError();
+}
+cudaError_t launch_cg_direction(const float2 *r, float2 *p, int64_t n, const SolveState *st, cudaStream_t s) {
+    k_cg_direction<<<vec_blocks(n), kVecThreads, 0, s>>>(r, p, n, st);
+    return cudaGetLastError();
+}
+cudaError_t launch_fista_start(const float2 *rhs, float step, float2 *y, float2 *y_acc, float2 *x_pre, int64_t n,
+                               SolveState *st, cudaStream_t s) {
+    k_fista_start<<<vec_blocks(n), kVecThreads, 0, s>>>(rhs, step, y, y_acc, x_pre, n, st);
+    return cudaGetLastError();
+}
+cudaError_t launch_scale(const float2 *in, float a, float2 *out, int64_t n, cudaStream_t s) {
+    k_scale<<<vec_blocks(n), kVecThreads, 0, s>>>(in, a, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_haar_step(const HaarStepArgs &a, bool momentum, cudaStream_t s) {
+    const int64_t nb = haar_blocks(a.h);
+    if (nb == 0) return cudaSuccess;
+    const size_t sm = haar_smem(a.h);
+#define GBN_HAAR_STEP(D)                                                                    \
+    do {                                                                                    \
+        if (momentum)                                                                       \
+            k_haar_step<D, true><<<(unsigned)nb, kHaarThreads, sm, s>>>(a);                 \
+        else                                                                                \
+            k_haar_step<D, false><<<(unsigned)nb, kHaarThreads, sm, s>>>(a);                \
+    } while (0)
+    if (a.h.dim == 1)
+        GBN_HAAR_STEP(1);
+    else if (a.h.dim == 2)
+        GBN_HAAR_STEP(2);
+    else
+        GBN_HAAR_STEP(3);
+#undef GBN_HAAR_STEP
+    return cudaGetLastError();
+}
+
+cudaError_t launch_haar_dwt(const HaarGeom &h, const float2 *in, float2 *out, bool inverse, cudaStream_t s) {
+    const int64_t nb = haar_blocks(h);
+    if (nb == 0) return cudaSuccess;
+    const size_t sm = haar_smem(h);
+#define GBN_HAAR_DWT(D)                                                                     \
+    do {                                                                                    \
+        if (inverse)                                                                        \
+            k_haar_dwt<D, true><<<(unsigned)nb, kHaarThreads, sm, s>>>(h, in, out);         \
+        else                                                                                \
+            k_haar_dwt<D, false><<<(unsigned)nb, kHaarThreads, sm, s>>>(h, in, out);        \
+    } while (0)
+    if (h.dim == 1)
+        GBN_HAAR_DWT(1);
+    else if (h.dim == 2)
+        GBN_HAAR_DWT(2);
+    else
+        GBN_HAAR_DWT(3);
+#undef GBN_HAAR_DWT
+    return cudaGetLastError();
+}
+
+}  // namespace gbn
+
+using namespace gbn;
+
+// ---- C ABI: standalone wavelet and soft threshold ---------------------------------------
+int gbn_haar_dwt(int32_t dim, const int32_t *shape, int32_t level, int64_t n_outer, int64_t n_inner,
+                 const void *in, void *out, int32_t inverse, gbn_stream_t stream) {
+    HaarGeom h;
+    if (int st = haar_geom(dim, shape, level, n_outer, n_inner, h)) return st;
+    if (!in || !out) return record_error(GBN_ERR_ARG, "Haar transform: null buffer");
+    if (in == out && level > 0)
+        return record_error(GBN_ERR_ARG, "Haar transform: input and output must be different buffers");
+    cudaError_t e = launch_haar_dwt(h, (const float2 *)in, (float2 *)out, inverse != 0, (cudaStream_t)stream);
+    if (e != cudaSuccess) return record_error(GBN_ERR_CUDA, (std::string("Haar transform: ") + cudaGetErrorString(e)).c_str());
+    return GBN_OK;
+}
+
+int gbn_prox_haar(int32_t dim, const int32_t *shape, int32_t level, int64_t n_outer, int64_t n_inner,
+                  const void *in, float th, void *out, gbn_stream_t stream) {
+    HaarGeom h;
+    if (int st = haar_geom(dim, shape, level, n_outer, n_inner, h)) return st;
+    if (!in || !out) return record_error(GBN_ERR_ARG, "Haar prox: null buffer");
+    if (!(th >= 0.f) || !std::isfinite(th)) return record_error(GBN_ERR_ARG, "Haar prox: threshold must be finite and >= 0");
+    HaarStepArgs a{};
+    a.h = h;
+    a.acc = (float2 *)in;  // read only: no gradient update (q == null)
+    a.th = th;
+    a.x_out = (float2 *)out;
+    cudaError_t e = launch_haar_step(a, false, (cudaStream_t)stream);
+    if (e != cudaSuccess) return record_error(GBN_ERR_CUDA, (std::string("Haar prox: ") + cudaGetErrorString(e)).c_str());
+    return GBN_OK;
+}

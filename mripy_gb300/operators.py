@@ -172,6 +172,11 @@ class _NUFFTnd:
         # density_weighting fused into the spread kernel (per-sample weight)
         return p.type1(c, weight=self.dcf_device())
 
+    def normal_solver(self, n_coil):
+        """(plan, None, dcf) of forward_backward on images with n_coil trailing channels,
+        for the native solvers."""
+        return self.plan(n_coil), None, (self.dcf_device() if self.dim == 3 else None)
+
     def forward_backward(self, im):
         t, trail, nc, was_np = self._split_image(im)
         p = self.plan(nc)
@@ -298,6 +303,14 @@ class joint2operators:
         dcf = self.Bopt.dcf_device() if self.Bopt.dim == 3 else None
         out = p.sense_normal(x, s, dcf=dcf).reshape(self.Bopt.im_shape + (1,))
         return _to_np(out) if was_np else out
+
+    def normal_solver(self):
+        """(plan, coil maps, dcf) of the fused normal operator for the native solvers, or
+        None when the pair is not espirit + NUFFT."""
+        if not self._fused():
+            return None
+        p, s = self._sense_plan()
+        return p, s, (self.Bopt.dcf_device() if self.Bopt.dim == 3 else None)
 
     def normal_graph(self, x_buf, out_buf):
         """CUDA graph of forward_backward on fixed (1, *im_shape) complex64 buffers."""

@@ -344,6 +344,45 @@ class NufftPlan:
                                            _stream(stream)))
         return out
 
+    # ------------------------------------------------------------------ solvers
+    def _solve_vec(self, t, sens, name):
+        want = (self.n_traj,) + self.shape + (() if sens is not None else (self.n_coil,))
+        _require_cuda(t, name, torch.complex64)
+        if tuple(t.shape) != want or not t.is_contiguous():
+            raise ValueError("%s must be a contiguous complex64 tensor of shape %s, got %s"
+                             % (name, want, tuple(t.shape)))
+
+    def cg(self, rhs, n_iter, sens=None, dcf=None, x0=None, use_graph=True, stream=None):
+        """Linear CG on N x = rhs with N = S^H type21(S .) (sens given; x, rhs: (n_traj,
+        *shape)) or type21 (x, rhs: (n_traj, *shape, n_coil)).  Returns (x, residual norms
+        after every iteration, float64 device tensor)."""
+        self._check_points()
+        self._solve_vec(rhs, sens, "rhs")
+        if x0 is not None:
+            self._solve_vec(x0, sens, "x0")
+            x = x0.clone()
+        else:
+            x = torch.empty_like(rhs)
+        norms = torch.empty(int(n_iter), dtype=torch.float64, device="cuda")
+        sl = self._sense_layout(sens) if sens is not None else N.Layout(0, 0, 0)
+        flags = (N.GBN_SOLVE_X0 if x0 is not None else 0) | (0 if use_graph else N.GBN_SOLVE_NO_GRAPH)
+        N.check(self._lib.gbn_cg_sense(self._h, _ptr(sens), sl, self._weight(dcf, self.n_samples), _ptr(rhs),
+                                       _ptr(x), int(n_iter), _ptr(norms), flags, _stream(stream)))
+        return x, norms
+
+    def ista(self, rhs, n_iter, step, th, level, sens=None, dcf=None, fista=True, use_graph=True, stream=None):
+        """IST_32 / FIST_32 with rhs = A^H b and the level-``level`` Haar soft-threshold prox
+        (level 0: plain soft threshold).  Vectors as in :meth:`cg`.  Returns x."""
+        self._check_points()
+        self._solve_vec(rhs, sens, "rhs")
+        x = torch.empty_like(rhs)
+        sl = self._sense_layout(sens) if sens is not None else N.Layout(0, 0, 0)
+        flags = (N.GBN_SOLVE_FISTA if fista else 0) | (0 if use_graph else N.GBN_SOLVE_NO_GRAPH)
+        N.check(self._lib.gbn_ista_haar(self._h, _ptr(sens), sl, self._weight(dcf, self.n_samples), _ptr(rhs),
+                                        _ptr(x), int(n_iter), float(step), float(th), int(level), flags,
+                                        _stream(stream)))
+        return x
+
     # ------------------------------------------------------------------ gradient
     def interp_grad_coords(self, grid, grad_c, out=None, stream=None):
         """(M_total, dim) float32: df * Re(sum_coil conj(grad_c) dc/dx) for c = interp(grid)."""
@@ -367,6 +406,45 @@ class NufftPlan:
                                                    self._weight(dcf, self.n_samples), _ptr(out), ol,
                                                    ctypes.byref(h)))
         return Graph(h, (x, out, sens, dcf, self))
+
+
+def _haar_layout(x, axes):
+    axes = tuple(int(a) % x.dim() for a in axes)
+    d = len(axes)
+    if d < 1 or d > 3 or axes != tuple(range(axes[0], axes[0] + d)):
+        raise NotImplementedError("the Haar kernels take 1 to 3 consecutive, increasing axes, got %s" % (axes,))
+    _require_cuda(x, "x", torch.complex64)
+    if not x.is_contiguous():
+        raise ValueError("x must be contiguous")
+    outer, inner = 1, 1
+    for s in x.shape[:axes[0]]:
+        outer *= int(s)
+    for s in x.shape[axes[0] + d:]:
+        inner *= int(s)
+    shape = (ctypes.c_int32 * 3)(*([int(x.shape[a]) for a in axes] + [1] * (3 - d)))
+    return d, shape, outer, inner
+
+
+def haar_dwt(x, level, axes, inverse=False, out=None, stream=None):
+    """Orthonormal level-``level`` Haar transform over ``axes`` of a complex64 CUDA tensor:
+    image -> coefficients in pywt.coeffs_to_array's layout (inverse=False), or back."""
+    d, shape, outer, inner = _haar_layout(x, axes)
+    out = torch.empty_like(x) if out is None else out
+    if out.shape != x.shape or out.data_ptr() == x.data_ptr():
+        raise ValueError("out must be a separate tensor of the input's shape")
+    N.check(N.lib().gbn_haar_dwt(d, shape, int(level), outer, inner, _ptr(x), _ptr(out), 1 if inverse else 0,
+                                 _stream(stream)))
+    return out
+
+
+def prox_haar(x, th, level, axes, out=None, stream=None):
+    """H^-1 soft(H x, th) with the level-``level`` Haar transform over ``axes`` (level 0:
+    the plain soft threshold x / (|x| + 1e-6) * max(|x| - th, 0))."""
+    d, shape, outer, inner = _haar_layout(x, axes)
+    out = torch.empty_like(x) if out is None else out
+    N.check(N.lib().gbn_prox_haar(d, shape, int(level), outer, inner, _ptr(x), float(th), _ptr(out),
+                                  _stream(stream)))
+    return out
 
 
 def _from_ptr(ptr, n):

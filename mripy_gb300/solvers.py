@@ -1,18 +1,25 @@
 """Solvers that call the NUFFT operators: CG-SENSE and mripy's IST/FISTA with a
-wavelet soft-threshold (pics/CS_MRI_solvers_func.py, pics/proximal_func.py), on the GPU.
+wavelet soft-threshold (pics/CS_MRI_solvers_func.py, pics/proximal_func.py).
 
-* ``cg_sense``      linear conjugate gradient on S^H A^H D A S x = S^H A^H D y; the normal
-                    operator is the SENSE-fused type-21 pipeline, optionally replayed from a
-                    CUDA graph; all scalars stay on the device (no host sync per iteration)
-* ``IST_32``, ``FIST_32``, ``IST_wrap``, ``FIST_wrap``   mripy's iterations
-                    (CS_MRI_solvers_func.py:75-86, 207-247) on torch CUDA tensors
-* ``prox_l1_Tf_soft_thresh2``  soft threshold in a transform domain (proximal_func.py:46-52)
-* ``DWTnd``         orthonormal multi-level Haar wavelet with the DWTnd interface
-                    (pics/operators_class.py:394-416; backward = image -> coefficients)
+* ``cg_sense``      linear CG on S^H A^H D A S x = S^H A^H D y.  With A a NUFFT operator or
+                    joint2operators(espirit, NUFFT) the whole solve runs in the library
+                    (gbn_cg_sense): per iteration the fused normal operator and three vector
+                    kernels (FP64 inner products kept on the device) replayed as one CUDA
+                    graph, no host synchronisation.  Other operators: the same algorithm
+                    with torch vector ops around ``forward_backward``.
+* ``IST_wrap``, ``FIST_wrap``   mripy's wrappers (CS_MRI_solvers_func.py:89-110, 227-247).
+                    NUFFT / SENSE operators with T = DWTnd('haar') (or no T) run natively
+                    (gbn_ista_haar: normal operator + one fused gradient-step / Haar prox /
+                    momentum kernel per iteration, one graph); any other operator runs
+                    ``IST_32`` / ``FIST_32`` (:75-86, 207-224) on its callables.
+* ``prox_l1_soft_thresh2``, ``prox_l1_Tf_soft_thresh2``   proximal_func.py:20-24, 46-52
+* ``DWTnd``         DWTnd with the Haar wavelet (pics/operators_class.py:394-416; pywt's
+                    wavedecn + coeffs_to_array layout, dwt/dwt_func.py:15-23) on the GPU
 """
-import math
-
+import numpy as np
 import torch
+
+from . import plan as _plan
 
 __all__ = ["cg_sense", "IST_32", "FIST_32", "IST_wrap", "FIST_wrap", "prox_l1_Tf_soft_thresh2",
            "prox_l1_soft_thresh2", "DWTnd"]
@@ -22,34 +29,50 @@ def _vdot(a, b):
     return torch.sum(a.conj() * b)
 
 
+def _native_normal(A, rhs):
+    """(plan, sens, dcf, vector shape) when A's normal operator runs in the library."""
+    if hasattr(A, "normal_solver") and hasattr(A, "Bopt"):
+        ns = A.normal_solver()
+        if ns is None:
+            return None
+        p, s, dcf = ns
+        return p, s, dcf, (1,) + tuple(A.Bopt.im_shape)
+    if hasattr(A, "normal_solver") and hasattr(A, "im_shape"):
+        trail = tuple(rhs.shape[A.dim:])
+        nc = int(np.prod(trail)) if trail else 1
+        p, s, dcf = A.normal_solver(nc)
+        return p, s, dcf, (1,) + tuple(A.im_shape) + (nc,)
+    return None
+
+
+def _to_cuda(b):
+    if isinstance(b, torch.Tensor):
+        return b.to("cuda", torch.complex64), False
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(b).astype(np.complex64))).to("cuda"), True
+
+
 def cg_sense(A, y, n_iter=20, x0=None, use_graph=True):
-    """Solve (A^H A) x = A^H y for A = joint2operators(espirit, NUFFT) with ``n_iter``
-    CG iterations.  ``A.forward_backward`` is the normal operator and ``A.backward(y)`` the
-    right-hand side (both carry mripy's 1/M, which cancels).  Returns (x, residual norms)."""
+    """Solve (A^H A) x = A^H y with ``n_iter`` CG iterations; ``A.forward_backward`` is the
+    normal operator and ``A.backward(y)`` the right-hand side (both carry mripy's 1/M,
+    which cancels).  Returns (x, residual norms after every iteration)."""
     b = A.backward(y)
     if not isinstance(b, torch.Tensor):
         raise TypeError("cg_sense runs on torch CUDA tensors")
-    shape = b.shape
+    nat = _native_normal(A, b)
+    if nat is not None:
+        p, s, dcf, vshape = nat
+        rhs = b.reshape(vshape).contiguous()
+        xs = None if x0 is None else x0.to("cuda", torch.complex64).reshape(vshape).contiguous()
+        x, norms = p.cg(rhs, n_iter, sens=s, dcf=dcf, x0=xs, use_graph=use_graph)
+        return x.reshape(b.shape), norms
+    # any other operator: the same iteration around its forward_backward
     x = torch.zeros_like(b) if x0 is None else x0.clone()
-    xin = torch.empty_like(b)
-    Ap = torch.empty_like(b)
-    graph = None
-    if use_graph:
-        graph = A.normal_graph(xin.view((1,) + tuple(A.Bopt.im_shape)), Ap.view((1,) + tuple(A.Bopt.im_shape)))
-
-    def normal(v):
-        if graph is not None:
-            xin.copy_(v)
-            graph.launch()
-            return Ap
-        return A.forward_backward(v).reshape(shape)
-
-    r = b - normal(x) if x0 is not None else b.clone()
+    r = b - A.forward_backward(x) if x0 is not None else b.clone()
     p = r.clone()
     rs = _vdot(r, r).real
     norms = []
     for _ in range(n_iter):
-        q = normal(p)
+        q = A.forward_backward(p)
         alpha = rs / _vdot(p, q).real
         x.add_(alpha * p)
         r.sub_(alpha * q)
@@ -57,15 +80,20 @@ def cg_sense(A, y, n_iter=20, x0=None, use_graph=True):
         p.mul_(rs_new / rs).add_(r)
         rs = rs_new
         norms.append(rs)
-    if graph is not None:
-        graph.close()
     return x, torch.stack(norms).sqrt()
 
 
 # ---------------------------------------------------------------- proximal operators
 def prox_l1_soft_thresh2(x0, th):
-    a = x0.abs()
-    return x0 / (a + 1e-6) * torch.clamp(a - th, min=0.0)
+    """x0 / (|x0| + 1e-6) * max(|x0| - th, 0) (proximal_func.py:20-24); CUDA complex64
+    tensors go through the library's kernel."""
+    if isinstance(x0, torch.Tensor) and x0.is_cuda and x0.dtype == torch.complex64 and x0.is_contiguous():
+        return _plan.prox_haar(x0.reshape(-1), th, 0, (0,)).reshape(x0.shape)
+    if isinstance(x0, torch.Tensor):
+        a = x0.abs()
+        return x0 / (a + 1e-6) * torch.clamp(a - th, min=0.0)
+    a = np.abs(x0)
+    return x0 / (a + 1e-6) * np.maximum(a - th, 0.0)
 
 
 def prox_l1_Tf_soft_thresh2(Tfunc, invTfunc, x0, th):
@@ -83,14 +111,14 @@ def IST_32(Afunc, invAAfunc, invAfunc, Tfunc, invTfunc, b, Nite, step, th, verbo
         r = invAAfunc(x) - invAb
         x_acc = x_acc - step * r
         if verbose:
-            print(float(torch.linalg.vector_norm(r)))
+            print(float(np.linalg.norm(np.asarray(r.cpu() if isinstance(r, torch.Tensor) else r))))
     return x
 
 
 def FIST_32(Afunc, invAAfunc, invAfunc, Tfunc, invTfunc, b, Nite, step, th, verbose=False):
     invAb = invAfunc(b)
     y = step * invAb
-    y_acc = torch.zeros_like(y)
+    y_acc = y * 0
     x_pre = y
     t = [1.0] * (Nite + 1)
     x = y
@@ -102,14 +130,39 @@ def FIST_32(Afunc, invAAfunc, invAfunc, Tfunc, invTfunc, b, Nite, step, th, verb
         y = x + ((t[k] - 1) / t[k + 1]) * (x - x_pre)
         x_pre = x
         if verbose:
-            print(float(torch.linalg.vector_norm(r)))
+            print(float(np.linalg.norm(np.asarray(r.cpu() if isinstance(r, torch.Tensor) else r))))
     return x
 
 
-def _wrap(solver, Aopt, Topt, b, Nite, step, th):
+def _haar_level(Topt, dim_axes):
+    """Level of a Haar DWTnd over exactly the image axes, 0 for no transform, else None."""
+    if Topt is None:
+        return 0
+    if isinstance(Topt, DWTnd) and tuple(a for a in Topt.axes) == tuple(dim_axes):
+        return int(Topt.level)
+    return None
+
+
+def _wrap(fista, Aopt, Topt, b, Nite, step, th):
     Nite = 20 if Nite is None else Nite
     step = 0.1 if step is None else step
     th = 0.04 if th is None else th
+    if not hasattr(Aopt, "forward_backward"):
+        raise TypeError("the operator needs forward_backward (the *_32 solver forms)")
+    dim = getattr(getattr(Aopt, "Bopt", Aopt), "dim", None)
+    native = (hasattr(Aopt, "normal_solver") and dim is not None and Nite >= 1
+              and _haar_level(Topt, tuple(range(dim))) is not None
+              and (isinstance(b, np.ndarray) or (isinstance(b, torch.Tensor) and b.is_cuda)))
+    if native:
+        bt, was_np = _to_cuda(b)
+        invAb = Aopt.backward(bt)
+        nat = _native_normal(Aopt, invAb)
+        if nat is not None:
+            p, s, dcf, vshape = nat
+            level = _haar_level(Topt, tuple(range(dim)))
+            x = p.ista(invAb.reshape(vshape).contiguous(), Nite, step, th, level, sens=s, dcf=dcf, fista=fista)
+            x = x.reshape(invAb.shape)
+            return x.cpu().numpy().astype(np.complex128) if was_np else x
     if Topt is None:
         class _Id:
             def forward(self, v):
@@ -118,27 +171,29 @@ def _wrap(solver, Aopt, Topt, b, Nite, step, th):
             def backward(self, v):
                 return v
         Topt = _Id()
-    if not hasattr(Aopt, "forward_backward"):
-        raise TypeError("the operator needs forward_backward (the *_32 solver forms)")
+    solver = FIST_32 if fista else IST_32
     return solver(Aopt.forward, Aopt.forward_backward, Aopt.backward, Topt.backward, Topt.forward, b, Nite, step,
                   th)
 
 
 def IST_wrap(Aopt, Topt=None, b=None, Nite=None, step=None, th=None):
-    return _wrap(IST_32, Aopt, Topt, b, Nite, step, th)
+    return _wrap(False, Aopt, Topt, b, Nite, step, th)
 
 
 def FIST_wrap(Aopt, Topt=None, b=None, Nite=None, step=None, th=None):
-    return _wrap(FIST_32, Aopt, Topt, b, Nite, step, th)
+    return _wrap(True, Aopt, Topt, b, Nite, step, th)
 
 
 # ---------------------------------------------------------------- Haar wavelet
 class DWTnd:
-    """Orthonormal multi-level Haar transform over ``axes`` (sizes divisible by 2^level).
+    """Orthonormal multi-level Haar transform over ``axes`` (1 to 3 consecutive axes,
+    sizes divisible by 2^level), computed by the library's tile kernel.
 
-    backward(im) -> coefficient array of the same shape (approximation block first along
-    every axis, details after, recursively: the layout of pywt.coeffs_to_array for Haar);
-    forward(coeffs) -> image.  Any other wavelet name raises: only Haar is built."""
+    backward(im) -> coefficient array of the same shape (pywt.coeffs_to_array layout:
+    approximation block first along every axis, then the detail blocks of each level,
+    coarsest first); forward(coeffs) -> image.  CUDA tensors stay on the GPU; numpy arrays
+    and CPU tensors are copied to it and back.  Any other wavelet name raises: only Haar
+    is built."""
 
     def __init__(self, wavelet="haar", level=2, axes=(0, 1, 2)):
         if wavelet not in ("haar", "db1"):
@@ -148,55 +203,19 @@ class DWTnd:
         self.axes = tuple(axes)
         self.shape = None
 
-    @staticmethod
-    def _fwd_axis(x, ax, n):
-        idx_e = torch.arange(0, n, 2, device=x.device)
-        sl = x.narrow(ax, 0, n)
-        e = sl.index_select(ax, idx_e)
-        o = sl.index_select(ax, idx_e + 1)
-        s = 1.0 / math.sqrt(2.0)
-        return torch.cat([(e + o) * s, (e - o) * s], dim=ax)
-
-    @staticmethod
-    def _inv_axis(x, ax, n):
-        h = n // 2
-        a = x.narrow(ax, 0, h)
-        d = x.narrow(ax, h, h)
-        s = 1.0 / math.sqrt(2.0)
-        e, o = (a + d) * s, (a - d) * s
-        st = torch.stack([e, o], dim=ax + 1)
-        shp = list(a.shape)
-        shp[ax] = n
-        return st.reshape(shp)
+    def _run(self, x, inverse):
+        if isinstance(x, torch.Tensor):
+            dev = x.device
+            t = x.to("cuda", torch.complex64).contiguous()
+            out = _plan.haar_dwt(t, self.level, self.axes, inverse=inverse)
+            return out if dev.type == "cuda" else out.to(dev)
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(x).astype(np.complex64))).to("cuda")
+        return _plan.haar_dwt(t, self.level, self.axes, inverse=inverse).cpu().numpy().astype(np.complex128)
 
     def backward(self, im):
         if self.shape is None:
             self.shape = tuple(im.shape)
-        x = im.clone()
-        sizes = [im.shape[a] for a in self.axes]
-        for lv in range(self.level):
-            n = [s >> lv for s in sizes]
-            if any(v % 2 for v in n):
-                raise ValueError("axis sizes must be divisible by 2^level")
-            block = x
-            for a, na in zip(self.axes, n):
-                block = block.narrow(a, 0, na)
-            y = block.clone()
-            for a, na in zip(self.axes, n):
-                y = self._fwd_axis(y, a, na)
-            block.copy_(y)
-        return x
+        return self._run(im, False)
 
     def forward(self, coeffs):
-        x = coeffs.clone()
-        sizes = [coeffs.shape[a] for a in self.axes]
-        for lv in reversed(range(self.level)):
-            n = [s >> lv for s in sizes]
-            block = x
-            for a, na in zip(self.axes, n):
-                block = block.narrow(a, 0, na)
-            y = block.clone()
-            for a, na in zip(self.axes, n):
-                y = self._inv_axis(y, a, na)
-            block.copy_(y)
-        return x
+        return self._run(coeffs, True)

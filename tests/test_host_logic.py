@@ -1,6 +1,7 @@
-"""Host-side logic that needs no GPU: Haar wavelet, proximal operators, the IST/FISTA
-iterations (checked against a numpy restatement of mripy's loops), synthetic workloads,
-and the multi-rank timing reduction of bench.py on two gloo processes."""
+"""Host-side logic that needs no GPU: the wavelet class's argument check, proximal
+operators, the IST/FISTA iterations on caller-supplied operators (checked against a numpy
+restatement of mripy's loops), synthetic workloads, and the multi-rank timing reduction
+of bench.py on two gloo processes."""
 import math
 import os
 import socket
@@ -12,28 +13,9 @@ import torch
 from mripy_gb300 import solvers, synth
 
 
-def test_haar_perfect_reconstruction_and_orthonormality():
-    torch.manual_seed(0)
-    x = torch.randn(16, 8, 32, dtype=torch.complex64)
-    w = solvers.DWTnd("haar", level=3, axes=(0, 1, 2))
-    c = w.backward(x)
-    assert c.shape == x.shape
-    assert torch.allclose(torch.linalg.vector_norm(c), torch.linalg.vector_norm(x), rtol=1e-5)
-    assert torch.allclose(w.forward(c), x, atol=1e-5)
-
-
-def test_haar_level1_known_values():
-    x = torch.tensor([[1.0, 3.0], [5.0, 7.0]])
-    c = solvers.DWTnd("haar", level=1, axes=(0, 1)).backward(x)
-    # approximation = sum/2, details = differences/2
-    assert torch.allclose(c, torch.tensor([[8.0, -2.0], [-4.0, 0.0]]))
-
-
-def test_haar_rejects_other_wavelets_and_odd_sizes():
+def test_haar_rejects_other_wavelets():
     with pytest.raises(NotImplementedError):
         solvers.DWTnd("db2")
-    with pytest.raises(ValueError):
-        solvers.DWTnd("haar", level=2, axes=(0,)).backward(torch.zeros(6))
 
 
 def test_soft_threshold_matches_reference_formula():
