@@ -234,6 +234,15 @@ int gbn_ista_haar(gbn_plan *plan, const void *sens, gbn_layout sens_layout, cons
                   const void *rhs, void *x, int32_t n_iter, float step, float th, int32_t level,
                   int32_t flags, gbn_stream_t stream);
 
+/* Density compensation by Pipe-Menon iteration (J. G. Pipe, P. Menon, MRM 41:179, 1999):
+ * w = 1, then n_iter times w <- w / |C w| with C w = interp(spread(w)) on the plan's own
+ * Gaussian kernel and grid (no FFT); dcf (device float[M_total]) receives w scaled to mean
+ * 1 in every trajectory group, so the normal operator's diagonal ((1/M) sum_j dcf_j) stays
+ * 1 as without dcf.  The reference reads its dcf from files (examples/
+ * pics_IST_3dute_wavelet_L1.py:31); this computes one for a trajectory.  The plan must have
+ * n_coil == 1.  Uses the plan's grid. */
+int gbn_dcf_pipe_menon(gbn_plan *plan, int32_t n_iter, float *dcf, gbn_stream_t stream);
+
 /* ---- wavelet and proximal operators (no plan) ------------------------------------- */
 /* Orthonormal level-`level` Haar transform of complex64 arrays (n_outer, s0[, s1[, s2]],
  * n_inner) over the dim spatial axes (contiguous, device): DWTnd('haar', level, axes)

@@ -115,6 +115,7 @@ struct gbn_plan {
     // solvers: workspace (state, partial sums, residual norms, vectors) and the captured
     // iteration graph of the last solve of each kind (CG, IST, FISTA)
     DevBuf solve_ws;
+    DevBuf dcf_ws;  // Pipe-Menon weights (complex samples) while gbn_dcf_pipe_menon runs
     struct SolveGraph {
         cudaGraphExec_t exec = nullptr;
         const void *sens = nullptr;
@@ -743,7 +744,7 @@ int gbn_plan_destroy(gbn_plan *p) {
                       &p->dup_keys, &p->dup_vals, &p->dup_keys_sorted, &p->dup_idx, &p->dup_pts,
                       &p->spread_count, &p->spread_tile_off, &p->home_tile_off, &p->nsub, &p->sub_off,
                       &p->spread_subs, &p->interp_subs, &p->cub_tmp, &p->scratch, &p->stage_in,
-                      &p->stage_out, &p->stage_w, &p->split_tiles, &p->solve_ws};
+                      &p->stage_out, &p->stage_w, &p->split_tiles, &p->solve_ws, &p->dcf_ws};
     for (gbn_plan::SolveGraph &sg : p->solve_graph)
         if (sg.exec) cudaGraphExecDestroy(sg.exec);
     for (DevBuf *b : bufs) release(*b);
@@ -1118,6 +1119,26 @@ int gbn_cg_sense(gbn_plan *p, const void *sens, gbn_layout sl, const float *dcf,
     GBN_CUDA(cudaMemcpyAsync(x, xv, bytes, cudaMemcpyDeviceToDevice, s));
     if (res_norms)
         GBN_CUDA(cudaMemcpyAsync(res_norms, sv.norms, sizeof(double) * n_iter, cudaMemcpyDeviceToDevice, s));
+    return GBN_OK;
+}
+
+int gbn_dcf_pipe_menon(gbn_plan *p, int32_t n_iter, float *dcf, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, true));
+    if (n_iter < 1) return fail(GBN_ERR_ARG, "n_iter must be >= 1");
+    if (p->desc.n_coil != 1) return fail(GBN_ERR_ARG, "density estimation takes a plan with n_coil == 1");
+    if (p->M == 0) return GBN_OK;
+    if (!dcf) return fail(GBN_ERR_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    GBN_TRY(ensure(p, p->dcf_ws, sizeof(float2) * (size_t)p->M));
+    float2 *w = p->dcf_ws.as<float2>(), *cw = p->scratch.as<float2>();  // scratch: M x n_coil from set_points
+    const gbn_layout cl = {0, 1, 1};
+    GBN_CUDA(launch_dcf_fill(w, p->M, s));
+    for (int it = 0; it < n_iter; ++it) {
+        GBN_TRY(run_spread(p, w, cl, nullptr, p->grid, s));
+        GBN_TRY(run_interp(p, p->grid, cw, cl, nullptr, s));
+        GBN_CUDA(launch_dcf_update(w, cw, p->M, s));
+    }
+    GBN_CUDA(launch_dcf_finish(w, p->traj_off_d.as<int64_t>(), p->desc.n_traj, dcf, s));
     return GBN_OK;
 }
 

@@ -208,6 +208,11 @@ cudaError_t launch_cg_direction(const float2 *r, float2 *p, int64_t n, const Sol
 cudaError_t launch_fista_start(const float2 *rhs, float step, float2 *y, float2 *y_acc, float2 *x_pre,
                                int64_t n, SolveState *st, cudaStream_t s);
 cudaError_t launch_scale(const float2 *in, float a, float2 *out, int64_t n, cudaStream_t s);
+// Pipe-Menon density compensation: w = 1; w /= |interp(spread(w))|; dcf = w scaled to
+// mean 1 per trajectory group
+cudaError_t launch_dcf_fill(float2 *w, int64_t n, cudaStream_t s);
+cudaError_t launch_dcf_update(float2 *w, const float2 *cw, int64_t n, cudaStream_t s);
+cudaError_t launch_dcf_finish(const float2 *w, const int64_t *d_traj_off, int n_traj, float *dcf, cudaStream_t s);
 
 // Images as Haar tiles: (n_outer, s0[, s1[, s2]], n_inner) complex64, contiguous; a
 // level-L orthonormal Haar transform over the dim spatial axes acts on disjoint tiles of

@@ -184,6 +184,40 @@ __global__ void __launch_bounds__(kVecThreads) k_scale(const float2 *__restrict_
     }
 }
 
+// ---- Pipe-Menon density compensation --------------------------------------------------
+// w <- w / |C w| with C w = interp(spread(w)) on the plan's Gaussian kernel; w is held as
+// complex samples (imaginary part 0) so the plan's spread reads it directly.
+__global__ void __launch_bounds__(kVecThreads) k_dcf_fill(float2 *__restrict__ w, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        w[i] = make_float2(1.f, 0.f);
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_dcf_update(float2 *__restrict__ w, const float2 *__restrict__ cw,
+                                                            int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 c = cw[i];
+        const float a = sqrtf(c.x * c.x + c.y * c.y);
+        // every sample's own stencil contributes w_j * sum_m g^2 > 0, so a > 0 unless w underflowed
+        w[i] = make_float2(a > 0.f ? w[i].x / a : 0.f, 0.f);
+    }
+}
+
+// one block per trajectory group: dcf = w * M_g / sum_g(w) (mean 1 over the group), the sum
+// in FP64 and in a fixed order
+__global__ void __launch_bounds__(kVecThreads) k_dcf_finish(const float2 *__restrict__ w, const int64_t *off,
+                                                            float *__restrict__ dcf) {
+    __shared__ double sh[32];
+    __shared__ double scale;
+    const int64_t a = off[blockIdx.x], b = off[blockIdx.x + 1];
+    double s = 0.0;
+    for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) s += (double)w[i].x;
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) scale = s > 0.0 ? (double)(b - a) / s : 0.0;
+    __syncthreads();
+    const float f = (float)scale;
+    for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) dcf[i] = w[i].x * f;
+}
+
 // ---- Haar tiles ------------------------------------------------------------------------
 // Element e of a block: tile (e >> (DIM*L)) of the block, in-tile cell c with c[DIM-1]
 // fastest, L bits per axis.  In-tile coefficients after the forward levels sit where
@@ -465,6 +499,19 @@ cudaError_t launch_fista_start(const float2 *rhs, float step, float2 *y, float2 
 }
 cudaError_t launch_scale(const float2 *in, float a, float2 *out, int64_t n, cudaStream_t s) {
     k_scale<<<vec_blocks(n), kVecThreads, 0, s>>>(in, a, out, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_dcf_fill(float2 *w, int64_t n, cudaStream_t s) {
+    k_dcf_fill<<<vec_blocks(n), kVecThreads, 0, s>>>(w, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_dcf_update(float2 *w, const float2 *cw, int64_t n, cudaStream_t s) {
+    k_dcf_update<<<vec_blocks(n), kVecThreads, 0, s>>>(w, cw, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_dcf_finish(const float2 *w, const int64_t *d_traj_off, int n_traj, float *dcf, cudaStream_t s) {
+    if (n_traj < 1) return cudaSuccess;
+    k_dcf_finish<<<n_traj, kVecThreads, 0, s>>>(w, d_traj_off, dcf);
     return cudaGetLastError();
 }
 

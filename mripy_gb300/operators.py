@@ -94,6 +94,16 @@ class _NUFFTnd:
             self.dcf = self._flat(dcf)
         self._invalidate()
 
+    def pipe_menon_dcf(self, n_iter=20):
+        """Estimate a density compensation for the current trajectory (Pipe-Menon iteration
+        on this operator's Gaussian kernel, mean 1), make it this operator's dcf and return
+        it as a (M,) float32 CUDA tensor.  The reference reads dcf from files; this is for
+        trajectories that come without one."""
+        d = self.plan(1).pipe_menon_dcf(n_iter)
+        self.dcf = d
+        self._dcf_dev = None
+        return d
+
     def _invalidate(self):
         for p in self._plans.values():
             p.close()

@@ -383,6 +383,18 @@ class NufftPlan:
                                         _stream(stream)))
         return x
 
+    def pipe_menon_dcf(self, n_iter=20, out=None, stream=None):
+        """Density compensation of this plan's trajectory by Pipe-Menon iteration on the
+        plan's Gaussian kernel: (M_total,) float32, mean 1 per trajectory group.  Needs a
+        plan with n_coil == 1; overwrites the plan's grid."""
+        self._check_points()
+        out = torch.empty(self.n_samples, dtype=torch.float32, device="cuda") if out is None else out
+        _require_cuda(out, "out", torch.float32)
+        if out.numel() != self.n_samples or not out.is_contiguous():
+            raise ValueError("out must be a contiguous float32 tensor of %d elements" % self.n_samples)
+        N.check(self._lib.gbn_dcf_pipe_menon(self._h, int(n_iter), _ptr(out), _stream(stream)))
+        return out
+
     # ------------------------------------------------------------------ gradient
     def interp_grad_coords(self, grid, grad_c, out=None, stream=None):
         """(M_total, dim) float32: df * Re(sum_coil conj(grad_c) dc/dx) for c = interp(grid)."""

@@ -18,14 +18,20 @@ Only ``tests/`` may import this module, as the checker.  It restates in FP64 num
                                  (the reference file is Python 2 syntax and cannot be imported)
 * ``cg``                         linear CG on the normal equations, the algorithm of the
                                  commented-out block pics/proximal_func.py:379-406
+* ``pipe_menon_dcf``             density compensation by Pipe-Menon iteration with the
+                                 oracle's FP64 Gaussian spread/interp (gridding.c); the
+                                 reference reads dcf from files (examples/
+                                 pics_IST_3dute_wavelet_L1.py:31) and has no estimator
 
 Parity of the Haar restatement is pinned by known answers of the published transform
 (``tests/test_solver_oracle.py``): the level-2 Haar of [1..8] is [5, 13, -2, -2, -1/sqrt2 x 4],
-and the 2-D / 3-D block layout of coeffs_to_array on hand-checked inputs.
+and the 2-D / 3-D block layout of coeffs_to_array on hand-checked inputs.  The Pipe-Menon
+restatement is pinned by its defining property: at the fixed point every sample's
+gridded-and-interpolated weight is equal.
 """
 import numpy as np
 
-__all__ = ["haar_dwt", "haar_idwt", "soft_thresh", "prox_haar", "ist", "fista", "cg"]
+__all__ = ["haar_dwt", "haar_idwt", "soft_thresh", "prox_haar", "ist", "fista", "cg", "pipe_menon_dcf"]
 
 _R2 = 1.0 / np.sqrt(2.0)
 
@@ -117,6 +123,29 @@ def fista(normal, rhs, n_iter, step, th, level, axes):
         y = x + ((t[k] - 1) / t[k + 1]) * (x - x_pre)
         x_pre = x
     return x
+
+
+def pipe_menon_dcf(coords, shape, n_iter, eps=1e-5, offsets=None):
+    """Pipe-Menon density compensation (J. G. Pipe, P. Menon, MRM 41:179, 1999) with the
+    Gaussian gridding kernel of the NUFFT at ``eps``: w = 1, w <- w / |interp(spread(w))|,
+    then w scaled to mean 1 in every trajectory group (``offsets``: group boundaries)."""
+    from . import nufft_oracle as NO
+    dim = len(shape)
+    ns, nf, tau = NO._params_for(dim, tuple(shape), eps)
+    xs = [np.asarray(v, dtype=np.float64) for v in coords]
+    M = len(xs[0])
+    offsets = [0, M] if offsets is None else list(offsets)
+    w = np.ones(M)
+    for _ in range(n_iter):
+        cw = np.zeros(M, dtype=np.complex128)
+        for a, b in zip(offsets[:-1], offsets[1:]):
+            sub = [v[a:b] for v in xs]
+            G = NO.spread(sub, w[None, a:b].astype(np.complex128), tau, ns, nf)
+            cw[a:b] = NO.interp(sub, G, tau, ns)[0]
+        w = w / np.abs(cw)
+    for a, b in zip(offsets[:-1], offsets[1:]):
+        w[a:b] *= (b - a) / w[a:b].sum()
+    return w
 
 
 def cg(normal, rhs, n_iter, x0=None):

@@ -227,3 +227,36 @@ def test_fista_sense_numpy_in_numpy_out():
     b = np.sum(np.conj(S) * O.nufft_type1(coords, y, shape, eps=EPS_OP), axis=-1, keepdims=True)
     ref = SO.fista(normal, b, 5, 0.5, 2e-4, 3, (0, 1))
     assert rel(xr, ref) < 1e-4
+
+
+# ---------------------------------------------------------------- density compensation
+def test_pipe_menon_dcf_2d_ragged_groups_match_oracle():
+    kx, ky = synth.golden_radial_2d(60, 64)
+    coords = (2 * np.pi * kx, 2 * np.pi * ky)
+    offsets = [0, 40 * 64, 60 * 64]                  # two frames: 40 and 20 spokes
+    plan = P.NufftPlan(2, (32, 32), n_coil=1, n_traj=2, eps=EPS_OP)
+    plan.set_points([torch.tensor(c, device="cuda") for c in coords], traj_offsets=offsets)
+    w = plan.pipe_menon_dcf(12)
+    ref = SO.pipe_menon_dcf(coords, (32, 32), 12, eps=EPS_OP, offsets=offsets)
+    assert rel(w, ref) < 1e-4
+    wn = w.cpu().numpy()
+    assert np.isclose(wn[:offsets[1]].mean(), 1.0, rtol=1e-5) and np.isclose(wn[offsets[1]:].mean(), 1.0, rtol=1e-5)
+
+
+def test_pipe_menon_dcf_3d_operator():
+    kk = synth.centre_out_radial_3d(300, 16)
+    nft = ops.NUFFT3d((16, 16, 16))
+    nft.normalize_set_ktraj(np.stack(kk))
+    coords = tuple(np.asarray(k.cpu() if isinstance(k, torch.Tensor) else k, dtype=np.float64)
+                   for k in nft._k[:3])
+    w = nft.pipe_menon_dcf(10)
+    ref = SO.pipe_menon_dcf(coords, (16, 16, 16), 10, eps=EPS_OP)
+    assert rel(w, ref) < 1e-4
+    assert nft.dcf is w
+
+
+def test_pipe_menon_dcf_needs_one_coil():
+    plan = P.NufftPlan(2, (16, 16), n_coil=2, eps=EPS_OP)
+    plan.set_points([torch.zeros(10, dtype=torch.float64, device="cuda")] * 2)
+    with pytest.raises(RuntimeError):
+        plan.pipe_menon_dcf(3)

@@ -76,3 +76,21 @@ def test_ist_fista_first_iterate_is_the_prox_of_the_gradient_step():
     ref = SO.prox_haar(rhs, 0.3, 2, (0, 1))
     assert np.allclose(SO.ist(lambda v: 0 * v, rhs, 1, 1.0, 0.3, 2, (0, 1)), ref, atol=1e-13)
     assert np.allclose(SO.fista(lambda v: 0 * v, rhs, 1, 1.0, 0.3, 2, (0, 1)), ref, atol=1e-13)
+
+
+def test_pipe_menon_fixed_point_and_radial_density():
+    from mripy_gb300 import synth
+    import oracle as O
+    kx, ky = synth.radial_2d(32, 64)
+    coords = (2 * np.pi * kx, 2 * np.pi * ky)
+    shape = (32, 32)
+    w = SO.pipe_menon_dcf(coords, shape, 30)
+    assert np.isclose(w.mean(), 1.0)
+    # fixed point: interp(spread(w)) is the same at every sample
+    ns, nf, tau = O.grid_params(2, 32, 32, eps=1e-5)
+    cw = np.abs(O.interp(coords, O.spread(coords, w[None].astype(np.complex128), tau, ns, nf), tau, ns)[0])
+    assert np.std(cw) / np.mean(cw) < 0.05
+    # radial sampling density falls as 1/|k|: away from the centre the weights grow with |k|
+    r = np.hypot(kx, ky)
+    mid = (r > 0.1) & (r < 0.4)
+    assert np.corrcoef(r[mid], w[mid])[0, 1] > 0.95
