@@ -608,6 +608,18 @@ def run_reference(args, wl):
             "wall_s_timed": round(wall, 2)}
 
 
+def run_solver_only(args, wl):
+    import torch
+    coords = [torch.from_numpy(c).cuda() for c in wl.coords]
+    tuning = None
+    if args.tune == "auto":
+        from mripy_gb300.tune import autotune
+        tuning = autotune(wl.dim, wl.shape, coords, n_coil=wl.n_coil, n_traj=wl.n_traj, traj_offsets=wl.offsets,
+                          eps=wl.eps, cache_file=args.tune_cache)
+    res = cg_sense_time(torch, wl, coords) if wl.name == "c2" else ist_time(torch, wl, tuning)
+    return {"workload": wl.description, "part": "solver", "solver": res}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -621,7 +633,17 @@ def main():
     ap.add_argument("--tune-cache", default=None,
                     help="JSON file of autotuner results: read if it holds this workload's key, else "
                          "written; lets a profiler run reuse the tiling of an earlier run")
+    ap.add_argument("--part", default="all", choices=["all", "solver"],
+                    help="solver: only the solver timing of c2 (CG-SENSE) or c4 (IST), one JSON line "
+                         "with its figures (for profiling the solver kernels)")
     args = ap.parse_args()
+    if args.part == "solver":
+        if args.workload not in ("c2", "c4") or args.impl != "gb300":
+            ap.error("--part solver takes --workload c2 or c4 with the gb300 arm")
+        from mripy_gb300 import build
+        build.build()
+        print(json.dumps(run_solver_only(args, make_workload(args.workload))))
+        return
     if args.impl == "gb300":
         args.warmup = max(args.warmup, 3)
     import oracle

@@ -1129,8 +1129,10 @@ int gbn_dcf_pipe_menon(gbn_plan *p, int32_t n_iter, float *dcf, gbn_stream_t str
     if (p->M == 0) return GBN_OK;
     if (!dcf) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
-    GBN_TRY(ensure(p, p->dcf_ws, sizeof(float2) * (size_t)p->M));
+    const size_t w_bytes = align256(sizeof(float2) * (size_t)p->M);
+    GBN_TRY(ensure(p, p->dcf_ws, w_bytes + sizeof(double) * kDcfPartials * (size_t)p->desc.n_traj));
     float2 *w = p->dcf_ws.as<float2>(), *cw = p->scratch.as<float2>();  // scratch: M x n_coil from set_points
+    double *partial = (double *)(p->dcf_ws.as<char>() + w_bytes);
     const gbn_layout cl = {0, 1, 1};
     GBN_CUDA(launch_dcf_fill(w, p->M, s));
     for (int it = 0; it < n_iter; ++it) {
@@ -1138,7 +1140,7 @@ int gbn_dcf_pipe_menon(gbn_plan *p, int32_t n_iter, float *dcf, gbn_stream_t str
         GBN_TRY(run_interp(p, p->grid, cw, cl, nullptr, s));
         GBN_CUDA(launch_dcf_update(w, cw, p->M, s));
     }
-    GBN_CUDA(launch_dcf_finish(w, p->traj_off_d.as<int64_t>(), p->desc.n_traj, dcf, s));
+    GBN_CUDA(launch_dcf_finish(w, p->traj_off_d.as<int64_t>(), p->desc.n_traj, partial, dcf, s));
     return GBN_OK;
 }
 

@@ -196,7 +196,7 @@ struct SolveState {
     unsigned done;   // blocks of the running reduction that have finished (last-block test)
     int it;          // CG iterations completed = residual norms written
 };
-constexpr int kRedBlocks = 304;  // upper bound on the blocks of one reduction (2 per SM)
+constexpr int kRedBlocks = 1216;  // upper bound on the blocks of one reduction (8 per SM)
 cudaError_t launch_cg_start(const float2 *rhs, const float2 *q, float2 *r, float2 *p, int64_t n,
                             double *partial, SolveState *st, cudaStream_t s);
 cudaError_t launch_cg_alpha(const float2 *p, const float2 *q, int64_t n, double *partial, SolveState *st,
@@ -212,7 +212,9 @@ cudaError_t launch_scale(const float2 *in, float a, float2 *out, int64_t n, cuda
 // mean 1 per trajectory group
 cudaError_t launch_dcf_fill(float2 *w, int64_t n, cudaStream_t s);
 cudaError_t launch_dcf_update(float2 *w, const float2 *cw, int64_t n, cudaStream_t s);
-cudaError_t launch_dcf_finish(const float2 *w, const int64_t *d_traj_off, int n_traj, float *dcf, cudaStream_t s);
+constexpr int kDcfPartials = 64;  // FP64 partial sums per trajectory group (launch_dcf_finish)
+cudaError_t launch_dcf_finish(const float2 *w, const int64_t *d_traj_off, int n_traj, double *partial, float *dcf,
+                              cudaStream_t s);
 
 // Images as Haar tiles: (n_outer, s0[, s1[, s2]], n_inner) complex64, contiguous; a
 // level-L orthonormal Haar transform over the dim spatial axes acts on disjoint tiles of

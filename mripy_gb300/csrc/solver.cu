@@ -33,7 +33,7 @@ constexpr int kHaarMaxElems = 4096;     // complex cells per block (32 KB of sha
 constexpr int kHaarPairs = kHaarMaxElems / 2 / kHaarThreads;  // butterflies per thread per pass
 
 int vec_blocks(int64_t n) {
-    const int64_t b = (n + (int64_t)kVecThreads * 4 - 1) / ((int64_t)kVecThreads * 4);
+    const int64_t b = (n + kVecThreads - 1) / kVecThreads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, kRedBlocks));
 }
 
@@ -202,20 +202,43 @@ __global__ void __launch_bounds__(kVecThreads) k_dcf_update(float2 *__restrict__
     }
 }
 
-// one block per trajectory group: dcf = w * M_g / sum_g(w) (mean 1 over the group), the sum
-// in FP64 and in a fixed order
-__global__ void __launch_bounds__(kVecThreads) k_dcf_finish(const float2 *__restrict__ w, const int64_t *off,
-                                                            float *__restrict__ dcf) {
+// dcf = w * M_g / sum_g(w) (mean 1 over each trajectory group).  Grid (kDcfBlocks, n_traj):
+// block b of group g sums chunk b of the group in FP64, then every block adds the group's
+// kDcfBlocks partials in block order (deterministic) and scales its chunk.
+constexpr int kDcfBlocks = kDcfPartials;
+
+__device__ __forceinline__ void dcf_chunk(const int64_t *off, int64_t &lo, int64_t &hi) {
+    const int64_t a = off[blockIdx.y], b = off[blockIdx.y + 1];
+    const int64_t chunk = (b - a + kDcfBlocks - 1) / kDcfBlocks;
+    lo = min(b, a + chunk * blockIdx.x);
+    hi = min(b, lo + chunk);
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_dcf_partial(const float2 *__restrict__ w, const int64_t *off,
+                                                             double *partial) {
     __shared__ double sh[32];
-    __shared__ double scale;
-    const int64_t a = off[blockIdx.x], b = off[blockIdx.x + 1];
+    int64_t lo, hi;
+    dcf_chunk(off, lo, hi);
     double s = 0.0;
-    for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) s += (double)w[i].x;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) s += (double)w[i].x;
     s = block_sum(s, sh);
-    if (threadIdx.x == 0) scale = s > 0.0 ? (double)(b - a) / s : 0.0;
+    if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * kDcfBlocks + blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_dcf_scale(const float2 *__restrict__ w, const int64_t *off,
+                                                           const double *partial, float *__restrict__ dcf) {
+    __shared__ float scale;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < kDcfBlocks; ++i) s += partial[(int64_t)blockIdx.y * kDcfBlocks + i];
+        const double n = (double)(off[blockIdx.y + 1] - off[blockIdx.y]);
+        scale = s > 0.0 ? (float)(n / s) : 0.f;
+    }
     __syncthreads();
-    const float f = (float)scale;
-    for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) dcf[i] = w[i].x * f;
+    int64_t lo, hi;
+    dcf_chunk(off, lo, hi);
+    const float f = scale;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) dcf[i] = w[i].x * f;
 }
 
 // ---- Haar tiles ------------------------------------------------------------------------
@@ -223,43 +246,65 @@ __global__ void __launch_bounds__(kVecThreads) k_dcf_finish(const float2 *__rest
 // fastest, L bits per axis.  In-tile coefficients after the forward levels sit where
 // pywt's layout would put them for an image of one tile: level l acts on the leading
 // (T >> l)^DIM cube, approximations in the lower half of every axis.
+// A tile decoded once per block: the base element of its image and its tile coordinates
+// along each axis (21 bits each), so the per-element addresses need no division.
+struct TileRef {
+    int64_t img_base;
+    int64_t tcp;
+};
+constexpr int kHaarMaxTiles = 512;  // tiles per block (blocks hold at least 512 cells)
+
 template <int DIM>
-__device__ __forceinline__ int64_t haar_addr(const HaarGeom &h, int64_t tile, int el, int cell[DIM], int tc[DIM]) {
+__device__ __forceinline__ TileRef haar_tile(const HaarGeom &h, int64_t tile) {
     const int64_t img = tile / h.tiles_img;
     int64_t tr = tile - img * h.tiles_img;
-    const int T = 1 << h.L;
+    int64_t packed = 0;
 #pragma unroll
     for (int d = DIM - 1; d >= 0; --d) {
-        tc[d] = (int)(tr % h.nt[d]);
+        packed |= (tr % h.nt[d]) << (21 * d);
         tr /= h.nt[d];
-        cell[d] = (el >> (h.L * (DIM - 1 - d))) & (T - 1);
     }
-    int64_t pix = 0;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) pix = pix * h.s[d] + (int64_t)tc[d] * T + cell[d];
     const int64_t outer = img / h.inner;
-    return outer * h.P * h.inner + (img - outer * h.inner) + pix * h.inner;
+    return TileRef{outer * h.P * h.inner + (img - outer * h.inner), packed};
 }
 
-// position of in-tile coefficient `cell` of tile `tc` in pywt.coeffs_to_array's layout
+__device__ __forceinline__ int tile_coord(int64_t packed, int d) { return (int)((packed >> (21 * d)) & 0x1FFFFF); }
+
+// image element of in-tile cell `el` (c[DIM-1] fastest, L bits per axis)
 template <int DIM>
-__device__ __forceinline__ int64_t haar_coeff_addr(const HaarGeom &h, int64_t tile, const int cell[DIM],
-                                                   const int tc[DIM]) {
+__device__ __forceinline__ int64_t haar_pix_addr(const HaarGeom &h, const TileRef &t, int el) {
+    const int T = 1 << h.L;
+    int64_t pix = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const int c = (el >> (h.L * (DIM - 1 - d))) & (T - 1);
+        pix = pix * h.s[d] + (int64_t)tile_coord(t.tcp, d) * T + c;
+    }
+    return t.img_base + pix * h.inner;
+}
+
+// position of in-tile coefficient `el` in pywt.coeffs_to_array's layout
+template <int DIM>
+__device__ __forceinline__ int64_t haar_coeff_addr(const HaarGeom &h, const TileRef &t, int el) {
+    const int T = 1 << h.L;
+    int cell[DIM];
     int m = 0;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) m = max(m, cell[d]);
+    for (int d = 0; d < DIM; ++d) {
+        cell[d] = (el >> (h.L * (DIM - 1 - d))) & (T - 1);
+        m = max(m, cell[d]);
+    }
     // band level j: T >> j <= m < T >> (j - 1); m = 0 is the level-L approximation
     const int j = m == 0 ? h.L : h.L - (31 - __clz(m));
     const int hj = 1 << (h.L - j);
     int64_t pix = 0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        const int g = cell[d] >= hj ? (h.s[d] >> j) + tc[d] * hj + (cell[d] - hj) : tc[d] * hj + cell[d];
+        const int tc = tile_coord(t.tcp, d);
+        const int g = cell[d] >= hj ? (h.s[d] >> j) + tc * hj + (cell[d] - hj) : tc * hj + cell[d];
         pix = pix * h.s[d] + g;
     }
-    const int64_t img = tile / h.tiles_img;
-    const int64_t outer = img / h.inner;
-    return outer * h.P * h.inner + (img - outer * h.inner) + pix * h.inner;
+    return t.img_base + pix * h.inner;
 }
 
 // One butterfly pass along axis `ax` over the leading n^DIM cube of every tile in the
@@ -352,14 +397,17 @@ __global__ void __launch_bounds__(kHaarThreads) k_haar_step(HaarStepArgs a) {
         t_next = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
         c_mom = (float)((t - 1.0) / t_next);
     }
-    int cell[DIM], tc[DIM];
+    __shared__ TileRef tiles[kHaarMaxTiles];
+    for (int t = threadIdx.x; t < ntiles_blk; t += kHaarThreads) tiles[t] = haar_tile<DIM>(h, tile0 + t);
+    __syncthreads();
+    const int el_mask = (1 << tile_log) - 1;
     for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
         const int tl = e >> tile_log;
         if (tl >= ntiles_blk) {
             sm[e] = make_float2(0.f, 0.f);
             continue;
         }
-        const int64_t g = haar_addr<DIM>(h, tile0 + tl, e & ((1 << tile_log) - 1), cell, tc);
+        const int64_t g = haar_pix_addr<DIM>(h, tiles[tl], e & el_mask);
         float2 v = a.acc[g];
         if (a.q) {
             const float2 q = a.q[g], b = a.rhs[g];
@@ -378,7 +426,7 @@ __global__ void __launch_bounds__(kHaarThreads) k_haar_step(HaarStepArgs a) {
     for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
         const int tl = e >> tile_log;
         if (tl >= ntiles_blk) continue;
-        const int64_t g = haar_addr<DIM>(h, tile0 + tl, e & ((1 << tile_log) - 1), cell, tc);
+        const int64_t g = haar_pix_addr<DIM>(h, tiles[tl], e & el_mask);
         const float2 x = sm[e];
         if (MOM) {
             const float2 xp = a.x_pre[g];
@@ -411,15 +459,18 @@ __global__ void __launch_bounds__(kHaarThreads) k_haar_dwt(HaarGeom h, const flo
     const int64_t tile0 = (int64_t)blockIdx.x << h.tpb_log;
     const int64_t left = ntiles - tile0;
     const int ntiles_blk = left < ((int64_t)1 << h.tpb_log) ? (int)left : (1 << h.tpb_log);
-    int cell[DIM], tc[DIM];
+    __shared__ TileRef tiles[kHaarMaxTiles];
+    for (int t = threadIdx.x; t < ntiles_blk; t += kHaarThreads) tiles[t] = haar_tile<DIM>(h, tile0 + t);
+    __syncthreads();
+    const int el_mask = (1 << tile_log) - 1;
     for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
         const int tl = e >> tile_log;
         if (tl >= ntiles_blk) {
             sm[e] = make_float2(0.f, 0.f);
             continue;
         }
-        int64_t g = haar_addr<DIM>(h, tile0 + tl, e & ((1 << tile_log) - 1), cell, tc);
-        if (INV) g = haar_coeff_addr<DIM>(h, tile0 + tl, cell, tc);
+        const int64_t g = INV ? haar_coeff_addr<DIM>(h, tiles[tl], e & el_mask)
+                              : haar_pix_addr<DIM>(h, tiles[tl], e & el_mask);
         sm[e] = in[g];
     }
     __syncthreads();
@@ -430,8 +481,8 @@ __global__ void __launch_bounds__(kHaarThreads) k_haar_dwt(HaarGeom h, const flo
     for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
         const int tl = e >> tile_log;
         if (tl >= ntiles_blk) continue;
-        int64_t g = haar_addr<DIM>(h, tile0 + tl, e & ((1 << tile_log) - 1), cell, tc);
-        if (!INV) g = haar_coeff_addr<DIM>(h, tile0 + tl, cell, tc);
+        const int64_t g = INV ? haar_pix_addr<DIM>(h, tiles[tl], e & el_mask)
+                              : haar_coeff_addr<DIM>(h, tiles[tl], e & el_mask);
         out[g] = sm[e];
     }
 }
@@ -460,14 +511,15 @@ int haar_geom(int dim, const int32_t *shape, int level, int64_t n_outer, int64_t
         if (d < dim && (h.s[d] < 1 || (h.s[d] & ((1 << level) - 1))))
             return record_error(GBN_ERR_ARG, "Haar transform: every axis size must be a multiple of 2^level");
         h.nt[d] = d < dim ? h.s[d] >> level : 1;
+        if (h.nt[d] >= (1 << 21)) return record_error(GBN_ERR_CAPACITY, "Haar transform: more than 2^21 tiles along an axis");
         h.P *= h.s[d];
         h.tiles_img *= h.nt[d];
     }
     h.inner = n_inner;
     h.n_img = n_outer * n_inner;
-    // tiles per block: at least 1024 cells per block, at most 4096
+    // tiles per block: at least 512 cells per block (so at most kHaarMaxTiles tiles), at most 4096
     int tpb_log = 0;
-    while (((dim * level) + tpb_log) < 10) ++tpb_log;
+    while (((dim * level) + tpb_log) < 9) ++tpb_log;
     h.tpb_log = tpb_log;
     if (haar_blocks(h) > 0x7fffffff) return record_error(GBN_ERR_CAPACITY, "Haar transform: too many tiles");
     return GBN_OK;
@@ -509,9 +561,13 @@ cudaError_t launch_dcf_update(float2 *w, const float2 *cw, int64_t n, cudaStream
     k_dcf_update<<<vec_blocks(n), kVecThreads, 0, s>>>(w, cw, n);
     return cudaGetLastError();
 }
-cudaError_t launch_dcf_finish(const float2 *w, const int64_t *d_traj_off, int n_traj, float *dcf, cudaStream_t s) {
+cudaError_t launch_dcf_finish(const float2 *w, const int64_t *d_traj_off, int n_traj, double *partial, float *dcf,
+                              cudaStream_t s) {
     if (n_traj < 1) return cudaSuccess;
-    k_dcf_finish<<<n_traj, kVecThreads, 0, s>>>(w, d_traj_off, dcf);
+    if (n_traj > 65535) return cudaErrorInvalidConfiguration;
+    const dim3 grid(kDcfBlocks, n_traj);
+    k_dcf_partial<<<grid, kVecThreads, 0, s>>>(w, d_traj_off, partial);
+    k_dcf_scale<<<grid, kVecThreads, 0, s>>>(w, d_traj_off, partial, dcf);
     return cudaGetLastError();
 }
 
