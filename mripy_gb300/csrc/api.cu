@@ -275,6 +275,11 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
 int interp_cg(const gbn_plan *p) {
     const int n = std::max(1, (int)p->desc.n_coil);
     int cg = p->interp_coil_group;
+    // a caller's group larger than the coil count only pads (e.g. a tuning chosen for 8
+    // coils applied to a one-coil plan): cap it at the smallest power of two >= n
+    int n_pow2 = 1;
+    while (n_pow2 < n) n_pow2 *= 2;
+    if (cg > n_pow2) cg = n_pow2;
     if (cg <= 0) {
         int best = 1 << 30;
         for (int cand : {8, 4, 2, 1}) {
