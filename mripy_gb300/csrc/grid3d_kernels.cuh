@@ -153,8 +153,12 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
 // s mod warps); a sample whose x stencil covers the plane adds wx * sum_y wy sum_z wz G over
 // the plane's W x W taps: lanes = (coil, z slot) as in k_interp3d, per-slot sums applied
 // with wz once, a shuffle reduction over the slots, and one lane per coil adding the result
-// to the sample's accumulator (no other warp touches it).
-constexpr int kPlaneMaxElems = 4096;  // plane elements (cell x coil) the kernel accepts
+// to the sample's accumulator (no other warp touches it).  A plane is stored coil-major,
+// [coil][y][z] with a padded coil stride (plane_coil_stride), so the copies run along z
+// (contiguous in the grid) and the lanes' reads stay conflict-free.  (With coil-fastest
+// planes each 8-byte copy of a warp came from a different coil volume and cost its own
+// shared-memory wavefront: 40 % of the shared pipe of the c4 launch went to staging.)
+constexpr int kPlaneMaxElems = 4096;  // plane elements (coil stride x coils) the kernel accepts
 
 // 8-byte asynchronous copy global -> shared (cp.async); src_bytes 0 writes zeros
 __device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_bytes) {
@@ -164,19 +168,33 @@ __device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_by
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// issue the copies of plane gx (periodic y/z indices, coil fastest) into dst; the caller
-// waits (cp_async_wait_all) and synchronises before reading it
+// Coil stride (float2) of a staged plane [coil][y][z]: at least the plane's y*z cells and
+// such that a half-warp's 8-byte reads (CG coils x 16/CG consecutive z cells) fall on 32
+// distinct banks: 8 coils -> stride 2 mod 4 (coil c starts 4c words apart, mod 32), 4 coils ->
+// 4 mod 8 (8c words apart).
+__host__ __device__ inline int plane_coil_stride(int cells, int cg) {
+    const int m = cg == 8 ? 4 : 8, r = cg == 8 ? 2 : 4;
+    int s = cells;
+    while (s % m != r) ++s;
+    return s;
+}
+
+// issue the copies of plane gx (periodic y/z indices) into dst, [coil][y][z] with coil
+// stride CSP; consecutive threads take consecutive z cells of one coil, so a warp's sources
+// are contiguous runs in the grid and its shared-memory writes consecutive words.  The
+// caller waits (cp_async_wait_all) and synchronises before reading it.
 template <int CG>
 __device__ __forceinline__ void plane_copy(float2 *dst, const float2 *__restrict__ base, const Geom &g, int cg0,
-                                           int gx, int ws1, int ws2, int WZ, int PC, float rWZ) {
+                                           int gx, int ws1, int ws2, int WZ, int cells, int CSP, float rWZ,
+                                           float rcells) {
     const float2 *pb = base + (int64_t)gx * g.nf[1] * g.nf[2];
-    for (int el = threadIdx.x; el < PC; el += blockDim.x) {
-        const int cc = el % CG, cell = el / CG;  // coil fastest: consecutive shared words
+    for (int el = threadIdx.x; el < CG * cells; el += blockDim.x) {
+        const int cc = div_small(el, rcells), cell = el - cc * cells;
         const int wy = div_small(cell, rWZ), wz = cell - wy * WZ;
         const int gy = wrap_fast(ws1 + wy, g.nf[1]), gz = wrap_fast(ws2 + wz, g.nf[2]);
         const bool ok = cg0 + cc < g.n_coil;
         const float2 *src = ok ? pb + (int64_t)cc * g.G + (int64_t)gy * g.nf[2] + gz : pb;
-        cp_async8(dst + el, src, ok ? 8 : 0);
+        cp_async8(dst + cc * CSP + cell, src, ok ? 8 : 0);
     }
 }
 
@@ -189,8 +207,10 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
     const int W = WT ? WT : g.W;
     const int ns = g.ns;
     const int WX = g.tile[0] + W - 1, WY = g.tile[1] + W - 1, WZ = g.tile[2] + W - 1;
-    const int PC = WY * WZ * CG;                                   // float2 per plane
-    float2 *planes = reinterpret_cast<float2 *>(smem_p3);          // [2][PC], [y][z][coil]
+    const int cells = WY * WZ;
+    const int CSP = plane_coil_stride(cells, CG);                  // coil stride in a plane
+    const int PC = CSP * CG;                                       // float2 per plane
+    float2 *planes = reinterpret_cast<float2 *>(smem_p3);          // [2][PC], [coil][y][z]
     float *st_w = reinterpret_cast<float *>(planes + 2 * PC);      // [NS][48]: wx, wy, wz
     int4 *st_r = reinterpret_cast<int4 *>(st_w + NS * 48);         // [NS]: rel0, rel1, rel2, sample
     float2 *st_acc = reinterpret_cast<float2 *>(st_r + NS);        // [NS][CG]
@@ -204,7 +224,7 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
     const float2 *base = a.grid + ((int64_t)grp * g.n_coil + cg0) * g.G;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int c = lane % CG, q = lane / CG;
-    const float rWZ = 1.f / (float)WZ;
+    const float rWZ = 1.f / (float)WZ, rcells = 1.f / (float)cells;
 
     for (int base_s = 0; base_s < sub.z; base_s += NS) {
         const int n = min(NS, sub.z - base_s);
@@ -229,7 +249,7 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
             }
         }
         for (int i = threadIdx.x; i < n * CG; i += blockDim.x) st_acc[i] = make_float2(0.f, 0.f);
-        plane_copy<CG>(planes, base, g, cg0, wrap_fast(ws0, g.nf[0]), ws1, ws2, WZ, PC, rWZ);
+        plane_copy<CG>(planes, base, g, cg0, wrap_fast(ws0, g.nf[0]), ws1, ws2, WZ, cells, CSP, rWZ, rcells);
         cp_async_wait_all();
         __syncthreads();
 
@@ -239,7 +259,7 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
             // before the previous barrier)
             if (px + 1 < WX)
                 plane_copy<CG>(planes + ((px + 1) & 1) * PC, base, g, cg0, wrap_fast(ws0 + px + 1, g.nf[0]), ws1, ws2,
-                               WZ, PC, rWZ);
+                               WZ, cells, CSP, rWZ, rcells);
             for (int s = warp; s < n; s += nw) {
                 const int4 r = st_r[s];
                 const int kx = px - r.x;
@@ -248,7 +268,7 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
                 float2 at[L::KT];
 #pragma unroll
                 for (int t = 0; t < L::KT; ++t) at[t] = make_float2(0.f, 0.f);
-                const float2 *rowbase = cur + ((size_t)r.y * WZ + r.z) * CG + c;
+                const float2 *rowbase = cur + c * CSP + r.y * WZ + r.z;
                 float wys[(L::WMAX + 3) & ~3];  // y weights by 16-byte broadcast loads
 #pragma unroll
                 for (int k4 = 0; k4 < (L::WMAX + 3) / 4; ++k4) {
@@ -263,11 +283,11 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
                     if (WT == 0 && ky >= W) break;
                     const float wy = wys[ky];
                     const float2 wy2 = make_float2(wy, wy);
-                    const float2 *row = rowbase + (size_t)ky * WZ * CG;
+                    const float2 *row = rowbase + ky * WZ;
 #pragma unroll
                     for (int t = 0; t < L::KT; ++t) {
                         const int kz = q + t * L::NQ;
-                        if (kz < W) at[t] = __ffma2_rn(wy2, row[kz * CG], at[t]);
+                        if (kz < W) at[t] = __ffma2_rn(wy2, row[kz], at[t]);
                     }
                 }
                 float ax = 0.f, ay = 0.f;
@@ -312,7 +332,8 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
 
 // shared memory of k_interp3d_planes, or 0 when a plane does not fit the register prefetch
 inline size_t interp3d_planes_smem_bytes(const Geom &g, int cg, int threads) {
-    const int PC = (g.tile[1] + g.W - 1) * (g.tile[2] + g.W - 1) * cg;
+    if (cg != 4 && cg != 8) return 0;
+    const int PC = plane_coil_stride((g.tile[1] + g.W - 1) * (g.tile[2] + g.W - 1), cg) * cg;
     (void)threads;
     if (g.dim != 3 || g.W > 16 || (cg != 4 && cg != 8) || PC > kPlaneMaxElems) return 0;
     return 2 * (size_t)PC * sizeof(float2) + kPlaneSamples * (48 * sizeof(float) + sizeof(int4)) +
