@@ -338,6 +338,32 @@ bool grid_tensor_map(gbn_plan *p, const float2 *grid, int cg, const TmaWin &t) {
     return true;
 }
 
+// 3-D: the grid as a 4-D tensor (z innermost, y, x, instance) of 8-byte cells with the
+// plane box BZ x BY x 1 x cg of the plane-streaming interp
+bool grid_tensor_map3d(gbn_plan *p, const float2 *grid, int cg, int BY, int BZ) {
+    if (p->tmap_grid == grid && p->tmap_cg == cg && p->tmap_bx == BY && p->tmap_by == BZ) return true;
+    p->tmap_grid = nullptr;
+    if ((reinterpret_cast<uintptr_t>(grid) & 15) || (p->nf[2] & 1)) return false;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)p->nf[2], (cuuint64_t)p->nf[1], (cuuint64_t)p->nf[0],
+                                (cuuint64_t)p->n_inst};
+    const cuuint64_t strides[3] = {(cuuint64_t)p->nf[2] * sizeof(float2),
+                                   (cuuint64_t)p->nf[1] * p->nf[2] * sizeof(float2),
+                                   (cuuint64_t)p->G * sizeof(float2)};
+    const cuuint32_t box[4] = {(cuuint32_t)BZ, (cuuint32_t)BY, 1u, (cuuint32_t)cg};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<float2 *>(grid), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    p->tmap_grid = grid;
+    p->tmap_cg = cg;
+    p->tmap_bx = BY;
+    p->tmap_by = BZ;
+    return true;
+}
+
 int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const float *weight, cudaStream_t s) {
     InterpArgs a;
     a.g = p->gi;
@@ -359,6 +385,14 @@ int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const flo
     }
     if (interp_smem_bytes(p->gi, cg, p->interp_threads) > (size_t)p->smem_optin)
         return fail(GBN_ERR_CAPACITY, "interp window does not fit in shared memory");
+    // 3-D, 4 or 8 coils per block: planes staged by tensor copies when the grid admits a map
+    int BY = 0, BZ = 0;
+    if (p->dim == 3 && interp3d_plane_box(p->gi, cg, BY, BZ)) {
+        const bool tma = p->interp_staging == 0 && grid_tensor_map3d(p, grid, cg, BY, BZ);
+        GBN_CUDA(launch_interp3d_planes(a, p->n_interp_sub, cg, p->interp_threads, tma ? &p->tmap : nullptr,
+                                        tma ? p->kstatus : nullptr, s));
+        return GBN_OK;
+    }
     GBN_CUDA(launch_interp(a, p->n_interp_sub, cg, p->interp_threads, s));
     return GBN_OK;
 }

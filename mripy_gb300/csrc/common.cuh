@@ -151,6 +151,12 @@ size_t interp_smem_bytes(const Geom &g, int coil_group, int threads);
 // shared memory of the plane-streaming 3-D interp, 0 where it does not apply
 size_t interp3d_planes_smem(const Geom &g, int coil_group, int threads);
 constexpr int kPlaneSamples = 64;  // samples per chunk of the plane-streaming 3-D interp
+// plane box (y rows, z cells per coil) of the plane-streaming 3-D interp: the tensor copy's
+// box over a grid tensor map (z, y, x, instance); false where the kernel does not apply
+bool interp3d_plane_box(const Geom &g, int coil_group, int &BY, int &BZ);
+// the plane-streaming 3-D interp; map (with status) may be null: the threads copy every plane
+cudaError_t launch_interp3d_planes(const InterpArgs &a, int64_t n_sub, int coil_group, int threads,
+                                   const CUtensorMap *map, uint32_t *status, cudaStream_t s);
 
 // TMA-staged 2-D interp (interp2d_tma.cuh): window box geometry and launcher
 struct TmaWin {

@@ -19,6 +19,7 @@
 
 #include "grid2d_kernels.cuh"
 #include "grid_kernels.cuh"
+#include "tma.cuh"
 
 namespace gbn {
 
@@ -146,15 +147,18 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
 // ------------------------------------------------------------------ interp, plane streaming
 // For 4 or 8 coils per block.  A bin's (TX+W-1) x (TY+W-1) x (TZ+W-1) window does not fit in
 // shared memory at 8 coils (439 KB for 8^3 bins), so it is streamed one x plane at a time:
-// two plane buffers, the next plane's cells copied by cp.async while the current one is
-// used.  Up to kPlaneSamples samples of the bin are processed together; their weights
+// two plane buffers, the next plane copied while the current one is used -- by one tensor
+// copy (cp.async.bulk.tensor.4d, completing on an mbarrier; the copy writes shared memory
+// outside the load/store pipe the sample loop is bound by) when the window lies inside the
+// grid in y and z, else by the threads with cp.async (periodic wrap at the grid edge).  Up
+// to kPlaneSamples samples of the bin are processed together; their weights
 // (16 slots per dimension), home-relative first taps and per-coil accumulators live in
 // shared memory.  For each plane every warp walks its samples (sample s belongs to warp
 // s mod warps); a sample whose x stencil covers the plane adds wx * sum_y wy sum_z wz G over
 // the plane's W x W taps: lanes = (coil, z slot) as in k_interp3d, per-slot sums applied
 // with wz once, a shuffle reduction over the slots, and one lane per coil adding the result
 // to the sample's accumulator (no other warp touches it).  A plane is stored coil-major,
-// [coil][y][z] with a padded coil stride (plane_coil_stride), so the copies run along z
+// [coil][y][z] in the copy box's layout (plane_box), so the threads' copies run along z
 // (contiguous in the grid) and the lanes' reads stay conflict-free.  (With coil-fastest
 // planes each 8-byte copy of a warp came from a different coil volume and cost its own
 // shared-memory wavefront: 40 % of the shared pipe of the c4 launch went to staging.)
@@ -168,24 +172,34 @@ __device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_by
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Coil stride (float2) of a staged plane [coil][y][z]: at least the plane's y*z cells and
-// such that a half-warp's 8-byte reads (CG coils x 16/CG consecutive z cells) fall on 32
-// distinct banks: 8 coils -> stride 2 mod 4 (coil c starts 4c words apart, mod 32), 4 coils ->
-// 4 mod 8 (8c words apart).
-__host__ __device__ inline int plane_coil_stride(int cells, int cg) {
+// Staged plane [coil][y][z]: BY rows of BZ cells per coil, coil stride BY * BZ.  This is
+// the box of the plane's tensor copy (z innermost): BZ is even and covers the window's z
+// extent plus one cell, because the copy starts on an even z cell (16-byte boundary); BY
+// covers the y extent.  BY * BZ is chosen so that a half-warp's 8-byte reads (CG coils x
+// 16/CG consecutive z cells) fall on 32 distinct banks: 8 coils -> 2 mod 4 (coil c starts
+// 4c words apart, mod 32), 4 coils -> 4 mod 8 (8c words apart).  The threads' copies (windows
+// that wrap at the periodic grid edge) use the same layout.
+struct PlaneBox {
+    int BY, BZ;
+};
+__host__ __device__ inline PlaneBox plane_box(const Geom &g, int cg) {
+    const int WY = g.tile[1] + g.W - 1, WZ = g.tile[2] + g.W - 1;
     const int m = cg == 8 ? 4 : 8, r = cg == 8 ? 2 : 4;
-    int s = cells;
-    while (s % m != r) ++s;
-    return s;
+    for (int bz = (WZ + 2) & ~1; bz < WZ + 18; bz += 2)
+        for (int by = WY; by < WY + 4; ++by)
+            if ((by * bz) % m == r) return PlaneBox{by, bz};
+    return PlaneBox{0, 0};
 }
+// float2 per plane buffer, rounded to 128 bytes (tensor-copy destinations)
+__host__ __device__ inline int plane_elems(const PlaneBox &b, int cg) { return (b.BY * b.BZ * cg + 15) & ~15; }
 
-// issue the copies of plane gx (periodic y/z indices) into dst, [coil][y][z] with coil
-// stride CSP; consecutive threads take consecutive z cells of one coil, so a warp's sources
-// are contiguous runs in the grid and its shared-memory writes consecutive words.  The
-// caller waits (cp_async_wait_all) and synchronises before reading it.
+// the threads' copy of plane gx (periodic y/z indices) into dst: consecutive threads take
+// consecutive z cells of one coil, so a warp's sources are contiguous runs in the grid and
+// its shared-memory writes consecutive words.  The caller waits (cp_async_wait_all) and
+// synchronises before reading it.
 template <int CG>
 __device__ __forceinline__ void plane_copy(float2 *dst, const float2 *__restrict__ base, const Geom &g, int cg0,
-                                           int gx, int ws1, int ws2, int WZ, int cells, int CSP, float rWZ,
+                                           int gx, int ws1, int ws2, int WZ, int cells, int BZ, int CSP, float rWZ,
                                            float rcells) {
     const float2 *pb = base + (int64_t)gx * g.nf[1] * g.nf[2];
     for (int el = threadIdx.x; el < CG * cells; el += blockDim.x) {
@@ -194,22 +208,27 @@ __device__ __forceinline__ void plane_copy(float2 *dst, const float2 *__restrict
         const int gy = wrap_fast(ws1 + wy, g.nf[1]), gz = wrap_fast(ws2 + wz, g.nf[2]);
         const bool ok = cg0 + cc < g.n_coil;
         const float2 *src = ok ? pb + (int64_t)cc * g.G + (int64_t)gy * g.nf[2] + gz : pb;
-        cp_async8(dst + cc * CSP + cell, src, ok ? 8 : 0);
+        cp_async8(dst + cc * CSP + wy * BZ + wz, src, ok ? 8 : 0);
     }
 }
 
+// use_tma: the caller passed a tensor map of the grid (z, y, x, instance; 8-byte cells,
+// box BZ x BY x 1 x CG); windows inside the grid in y and z then arrive one plane per copy
+// on an mbarrier (x planes wrap freely: each is its own copy).
 template <int WT, int CG>
-__global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
+__global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a, const __grid_constant__ CUtensorMap map,
+                                                         PlaneBox pb, int use_tma, uint32_t *status) {
     using L = Lanes2D<WT, CG>;
     constexpr int NS = kPlaneSamples;
-    extern __shared__ float4 smem_p3[];
+    extern __shared__ __align__(128) float4 smem_p3[];
+    __shared__ __align__(8) uint64_t bar[2];
     const Geom &g = a.g;
     const int W = WT ? WT : g.W;
     const int ns = g.ns;
     const int WX = g.tile[0] + W - 1, WY = g.tile[1] + W - 1, WZ = g.tile[2] + W - 1;
     const int cells = WY * WZ;
-    const int CSP = plane_coil_stride(cells, CG);                  // coil stride in a plane
-    const int PC = CSP * CG;                                       // float2 per plane
+    const int BZ = pb.BZ, CSP = pb.BY * pb.BZ;                     // row pitch, coil stride
+    const int PC = plane_elems(pb, CG);                            // float2 per plane buffer
     float2 *planes = reinterpret_cast<float2 *>(smem_p3);          // [2][PC], [coil][y][z]
     float *st_w = reinterpret_cast<float *>(planes + 2 * PC);      // [NS][48]: wx, wy, wz
     int4 *st_r = reinterpret_cast<int4 *>(st_w + NS * 48);         // [NS]: rel0, rel1, rel2, sample
@@ -225,10 +244,37 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int c = lane % CG, q = lane / CG;
     const float rWZ = 1.f / (float)WZ, rcells = 1.f / (float)cells;
+    // tensor copies for windows inside the grid in y and z; the copy starts on an even z
+    const int zs = ws2 - (ws2 & 1);
+    const bool tma = use_tma && ws1 >= 0 && ws1 + pb.BY <= g.nf[1] && ws2 >= 0 && zs + BZ <= g.nf[2];
+    const int offz = tma ? ws2 - zs : 0;
+    const uint32_t box_bytes = (uint32_t)(CSP * CG * sizeof(float2));
+    if (tma && threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    uint32_t parity = 0u;  // bit b: phase parity expected next on buffer b's barrier
+
+    // start the copy of plane px into buffer b (tensor copy by one thread, or the threads')
+    auto stage = [&](int px, int b) {
+        float2 *dst = planes + b * PC;
+        const int gx = wrap_fast(ws0 + px, g.nf[0]);
+        if (tma) {
+            if (threadIdx.x == 0) {
+                fence_proxy_async_smem();  // the buffer's previous readers come first
+                mbar_arrive_expect_tx(&bar[b], box_bytes);
+                tma_load_4d(dst, &map, zs, ws1, gx, grp * g.n_coil + cg0, &bar[b]);
+            }
+        } else {
+            plane_copy<CG>(dst, base, g, cg0, gx, ws1, ws2, WZ, cells, BZ, CSP, rWZ, rcells);
+        }
+    };
 
     for (int base_s = 0; base_s < sub.z; base_s += NS) {
         const int n = min(NS, sub.z - base_s);
-        __syncthreads();  // the previous chunk's state and planes are consumed
+        __syncthreads();  // the previous chunk's state and planes are consumed (and the barriers set up)
+        stage(0, 0);
         for (int i = threadIdx.x; i < n * 48; i += blockDim.x) {
             const int s = i / 48, k = i - s * 48, d = k >> 4, kq = k & 15;
             const float4 p = a.pts[(int64_t)sub.y + base_s + s];
@@ -249,17 +295,19 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
             }
         }
         for (int i = threadIdx.x; i < n * CG; i += blockDim.x) st_acc[i] = make_float2(0.f, 0.f);
-        plane_copy<CG>(planes, base, g, cg0, wrap_fast(ws0, g.nf[0]), ws1, ws2, WZ, cells, CSP, rWZ, rcells);
-        cp_async_wait_all();
+        if (!tma) cp_async_wait_all();
         __syncthreads();
 
         for (int px = 0; px < WX; ++px) {
-            const float2 *cur = planes + (px & 1) * PC;
-            // the next plane's copies run while this one is used (its buffer was last read
+            const int b = px & 1;
+            if (tma) {
+                if (!mbar_wait_bounded(&bar[b], (parity >> b) & 1u) && lane == 0) atomicOr(status, kStatusTmaTimeout);
+                parity ^= 1u << b;
+            }
+            const float2 *cur = planes + b * PC;
+            // the next plane's copy runs while this one is used (its buffer was last read
             // before the previous barrier)
-            if (px + 1 < WX)
-                plane_copy<CG>(planes + ((px + 1) & 1) * PC, base, g, cg0, wrap_fast(ws0 + px + 1, g.nf[0]), ws1, ws2,
-                               WZ, cells, CSP, rWZ, rcells);
+            if (px + 1 < WX) stage(px + 1, b ^ 1);
             for (int s = warp; s < n; s += nw) {
                 const int4 r = st_r[s];
                 const int kx = px - r.x;
@@ -268,7 +316,7 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
                 float2 at[L::KT];
 #pragma unroll
                 for (int t = 0; t < L::KT; ++t) at[t] = make_float2(0.f, 0.f);
-                const float2 *rowbase = cur + c * CSP + r.y * WZ + r.z;
+                const float2 *rowbase = cur + c * CSP + r.y * BZ + r.z + offz;
                 float wys[(L::WMAX + 3) & ~3];  // y weights by 16-byte broadcast loads
 #pragma unroll
                 for (int k4 = 0; k4 < (L::WMAX + 3) / 4; ++k4) {
@@ -283,7 +331,7 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
                     if (WT == 0 && ky >= W) break;
                     const float wy = wys[ky];
                     const float2 wy2 = make_float2(wy, wy);
-                    const float2 *row = rowbase + ky * WZ;
+                    const float2 *row = rowbase + ky * BZ;
 #pragma unroll
                     for (int t = 0; t < L::KT; ++t) {
                         const int kz = q + t * L::NQ;
@@ -310,7 +358,7 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
                     acc.y = fmaf(wx, ay, acc.y);
                 }
             }
-            cp_async_wait_all();
+            if (!tma) cp_async_wait_all();
             __syncthreads();
         }
 
@@ -330,12 +378,13 @@ __global__ void __launch_bounds__(256) k_interp3d_planes(InterpArgs a) {
     }
 }
 
-// shared memory of k_interp3d_planes, or 0 when a plane does not fit the register prefetch
+// shared memory of k_interp3d_planes, or 0 when the plane kernel does not apply
 inline size_t interp3d_planes_smem_bytes(const Geom &g, int cg, int threads) {
-    if (cg != 4 && cg != 8) return 0;
-    const int PC = plane_coil_stride((g.tile[1] + g.W - 1) * (g.tile[2] + g.W - 1), cg) * cg;
     (void)threads;
-    if (g.dim != 3 || g.W > 16 || (cg != 4 && cg != 8) || PC > kPlaneMaxElems) return 0;
+    if (g.dim != 3 || g.W > 16 || (cg != 4 && cg != 8)) return 0;
+    const PlaneBox pb = plane_box(g, cg);
+    const int PC = plane_elems(pb, cg);
+    if (pb.BY == 0 || PC > kPlaneMaxElems) return 0;
     return 2 * (size_t)PC * sizeof(float2) + kPlaneSamples * (48 * sizeof(float) + sizeof(int4)) +
            (size_t)kPlaneSamples * cg * sizeof(float2);
 }

@@ -6,6 +6,7 @@
 // k_interp3d_planes (4 or 8 coils per block, window streamed by x planes) or k_interp3d.
 // Otherwise (1-D, wide stencils): k_interp (one thread per sample).
 #include <algorithm>
+#include <cstring>
 
 #include "dispatch.cuh"
 #include "grid2d_kernels.cuh"
@@ -36,6 +37,37 @@ static size_t grad_smem_bytes(const Geom &g, int coil_group) {
     return cells * (size_t)coil_group * sizeof(float2);
 }
 
+bool interp3d_plane_box(const Geom &g, int coil_group, int &BY, int &BZ) {
+    if (!interp3d_planes_smem_bytes(g, coil_group, 256)) return false;
+    const PlaneBox pb = plane_box(g, coil_group);
+    BY = pb.BY;
+    BZ = pb.BZ;
+    return true;
+}
+
+cudaError_t launch_interp3d_planes(const InterpArgs &a, int64_t n_sub, int coil_group, int threads,
+                                   const CUtensorMap *map, uint32_t *status, cudaStream_t s) {
+    if (n_sub == 0) return cudaSuccess;
+    const int th = threads > 256 ? 256 : threads;
+    const size_t smem = interp3d_planes_smem_bytes(a.g, coil_group, th);
+    if (!smem) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)n_sub, (unsigned)((a.g.n_coil + coil_group - 1) / coil_group));
+    const PlaneBox pb = plane_box(a.g, coil_group);
+    CUtensorMap none;
+    memset(&none, 0, sizeof(none));
+    const int use_tma = map != nullptr && status != nullptr;
+    cudaError_t err = cudaSuccess;
+    GBN_DISPATCH_W(a.g.W, {
+        auto kern = coil_group == 8 ? k_interp3d_planes<WT, 8> : k_interp3d_planes<WT, 4>;
+        err = set_smem(kern, smem);
+        if (err == cudaSuccess) {
+            kern<<<grid, th, smem, s>>>(a, use_tma ? *map : none, pb, use_tma, status);
+            err = cudaGetLastError();
+        }
+    });
+    return err;
+}
+
 cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, int threads, cudaStream_t s) {
     if (n_sub == 0) return cudaSuccess;
     const size_t smem = interp_smem_bytes(a.g, coil_group, threads);
@@ -54,18 +86,8 @@ cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, in
     }
     if (a.g.dim == 3 && a.g.W <= 16) {
         const int th = threads > 256 ? 256 : threads;
-        const size_t psmem = interp3d_planes_smem_bytes(a.g, coil_group, th);
-        if (psmem) {  // 4 or 8 coils per block: stream the window plane by plane
-            GBN_DISPATCH_W(a.g.W, {
-                auto kern = coil_group == 8 ? k_interp3d_planes<WT, 8> : k_interp3d_planes<WT, 4>;
-                err = set_smem(kern, psmem);
-                if (err == cudaSuccess) {
-                    kern<<<grid, th, psmem, s>>>(a);
-                    err = cudaGetLastError();
-                }
-            });
-            return err;
-        }
+        if (interp3d_planes_smem_bytes(a.g, coil_group, th))  // 4 or 8 coils: stream plane by plane
+            return launch_interp3d_planes(a, n_sub, coil_group, th, nullptr, nullptr, s);
         const size_t wsmem = interp3d_smem_bytes(a.g, coil_group);  // the whole staged window
         GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
             auto kern = k_interp3d<WT, CG>;

@@ -27,65 +27,11 @@
 #include <cuda.h>
 
 #include "grid2d_kernels.cuh"
+#include "tma.cuh"
 
 namespace gbn {
 
-constexpr uint32_t kTmaWaitLimit = 1u << 21;  // mbarrier probes before a wait gives up
-constexpr uint32_t kTmaSuspendNs = 1000;      // suspend-time hint of one probe
 constexpr int kTmaMaxStages = 4;              // window buffers per block (ring)
-constexpr uint32_t kStatusTmaTimeout = 2u;    // status-word bit: a bounded wait gave up
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-
-// potentially blocking probe: the thread is suspended until the phase with the given
-// parity completes or about kTmaSuspendNs nanoseconds pass (it issues nothing meanwhile)
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity), "r"(kTmaSuspendNs)
-        : "memory");
-    return ok != 0;
-}
-
-// bounded wait for the phase with the given parity to complete: at most kTmaWaitLimit
-// suspended probes of ~kTmaSuspendNs each (about two seconds in all)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kTmaWaitLimit; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void fence_barrier_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-// order this thread's earlier generic-proxy shared-memory accesses before async-proxy ones
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
-        : "memory");
-}
 
 struct TmaItem {
     int4 sub;

@@ -347,6 +347,31 @@ def test_tma_interp_matches_thread_staging(shape, nc, eps, tile, icg):
     assert rel(k[:counts[0]], ref) < TOL_REF
 
 
+@pytest.mark.parametrize("nc,icg,tile", [(8, 8, (8, 8, 8)), (4, 4, (8, 4, 8)), (12, 4, (4, 8, 8))])
+def test_tma_planes_3d_match_thread_staging(nc, icg, tile):
+    """3-D plane-streaming interp: planes staged by tensor copies (windows inside the grid in
+    y and z) and by the threads (every window) feed the same arithmetic: equal bit for bit.
+    A 48^3 grid puts most 19-cell windows at an edge, so one launch mixes both paths."""
+    rng = np.random.default_rng(25)
+    shape, M = (24, 24, 24), 30000
+    xs = rng.uniform(-np.pi, np.pi, (3, M))
+    xs[:, :12000] *= 0.2
+    plans = [NufftPlan(3, shape, n_coil=nc, eps=1e-6, max_nspread=6,
+                       tuning=Tuning(interp_tile=tile, interp_coil_group=icg, interp_staging=st))
+             .set_points([cuda(v) for v in xs]) for st in (0, 1)]
+    g = plans[0].grid()
+    g.copy_(torch.randn(g.shape, dtype=torch.complex64, device="cuda"))
+    c_tma = plans[0].interp(g)
+    c_thr = plans[1].interp(g)
+    plans[0].status()
+    assert torch.equal(c_tma, c_thr)
+    img = cvec(rng, (1,) + shape + (nc,))
+    k = plans[0].type2(cuda(img))
+    plans[0].status()
+    ref = O.nufft_type2(tuple(xs), img[0].astype(np.complex128), shape, eps=1e-6)
+    assert rel(k, ref) < TOL_REF
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 def test_host_entry_points_pinned_and_pageable(dim):
     """gbn_type{1,2,21}_host give the device path's results whether the caller's arrays are
