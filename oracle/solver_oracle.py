@@ -137,14 +137,17 @@ def pipe_menon_dcf(coords, shape, n_iter, eps=1e-5, offsets=None):
     offsets = [0, M] if offsets is None else list(offsets)
     w = np.ones(M)
     for _ in range(n_iter):
-        cw = np.zeros(M, dtype=np.complex128)
+        cw = np.ones(M, dtype=np.complex128)
         for a, b in zip(offsets[:-1], offsets[1:]):
+            if b == a:
+                continue
             sub = [v[a:b] for v in xs]
             G = NO.spread(sub, w[None, a:b].astype(np.complex128), tau, ns, nf)
             cw[a:b] = NO.interp(sub, G, tau, ns)[0]
         w = w / np.abs(cw)
     for a, b in zip(offsets[:-1], offsets[1:]):
-        w[a:b] *= (b - a) / w[a:b].sum()
+        if b > a:
+            w[a:b] *= (b - a) / w[a:b].sum()
     return w
 
 

@@ -233,14 +233,14 @@ def test_fista_sense_numpy_in_numpy_out():
 def test_pipe_menon_dcf_2d_ragged_groups_match_oracle():
     kx, ky = synth.golden_radial_2d(60, 64)
     coords = (2 * np.pi * kx, 2 * np.pi * ky)
-    offsets = [0, 40 * 64, 60 * 64]                  # two frames: 40 and 20 spokes
-    plan = P.NufftPlan(2, (32, 32), n_coil=1, n_traj=2, eps=EPS_OP)
+    offsets = [0, 40 * 64, 40 * 64, 60 * 64]         # three frames: 40, 0 and 20 spokes
+    plan = P.NufftPlan(2, (32, 32), n_coil=1, n_traj=3, eps=EPS_OP)
     plan.set_points([torch.tensor(c, device="cuda") for c in coords], traj_offsets=offsets)
     w = plan.pipe_menon_dcf(12)
     ref = SO.pipe_menon_dcf(coords, (32, 32), 12, eps=EPS_OP, offsets=offsets)
     assert rel(w, ref) < 1e-4
     wn = w.cpu().numpy()
-    assert np.isclose(wn[:offsets[1]].mean(), 1.0, rtol=1e-5) and np.isclose(wn[offsets[1]:].mean(), 1.0, rtol=1e-5)
+    assert np.isclose(wn[:offsets[1]].mean(), 1.0, rtol=1e-5) and np.isclose(wn[offsets[2]:].mean(), 1.0, rtol=1e-5)
 
 
 def test_pipe_menon_dcf_3d_operator():
