@@ -243,6 +243,17 @@ int gbn_ista_haar(gbn_plan *plan, const void *sens, gbn_layout sens_layout, cons
  * n_coil == 1.  Uses the plan's grid. */
 int gbn_dcf_pipe_menon(gbn_plan *plan, int32_t n_iter, float *dcf, gbn_stream_t stream);
 
+/* ---- ESPIRiT coil maps (espirit/espirit_func.py) ---------------------------------- */
+/* The pixel-wise eigen step of espirit_2d / espirit_3d (espirit_func.py:72-81, 186-196):
+ * a (device, complex64, (n_pix, nsv, nc)) holds each pixel's nsv image-space ESPIRiT
+ * kernels; for vvH = A^T conj(A) (nc x nc) the largest eigenvalue goes to smap (device
+ * float[n_pix]) and its unit eigenvector to vmap (device complex64 (n_pix, nc)), by n_iter
+ * power iterations from the column of the largest diagonal entry.  The reference takes the
+ * SVD of vvH, whose eigenvector phase is arbitrary per pixel; here coil 0's component (the
+ * first non-zero coil's) is real and non-negative.  nc <= 32. */
+int gbn_espirit_eigen(const void *a, int64_t n_pix, int32_t nsv, int32_t nc, int32_t n_iter, void *vmap,
+                      float *smap, gbn_stream_t stream);
+
 /* ---- wavelet and proximal operators (no plan) ------------------------------------- */
 /* Orthonormal level-`level` Haar transform of complex64 arrays (n_outer, s0[, s1[, s2]],
  * n_inner) over the dim spatial axes (contiguous, device): DWTnd('haar', level, axes)

@@ -25,7 +25,7 @@ EXPORTED = (
     "gbn_sense_forward", "gbn_sense_adjoint", "gbn_sense_normal",
     "gbn_interp_grad_coords",
     "gbn_graph_capture_normal", "gbn_graph_launch", "gbn_graph_destroy",
-    "gbn_cg_sense", "gbn_ista_haar", "gbn_dcf_pipe_menon", "gbn_haar_dwt", "gbn_prox_haar",
+    "gbn_cg_sense", "gbn_ista_haar", "gbn_dcf_pipe_menon", "gbn_espirit_eigen", "gbn_haar_dwt", "gbn_prox_haar",
     "gbn_spread2d_noalloc",
     "gbn_type1_host", "gbn_type2_host", "gbn_type21_host",
     "gbn_nufft2d1_gaussker", "gbn_nufft2d2_gaussker", "gbn_nufft2d21_gaussker",
@@ -113,6 +113,7 @@ def _declare(lib):
         "gbn_cg_sense": ([_vp, _vp, Layout, _vp, _vp, _vp, _i32, _vp, _i32, _vp], _i32),
         "gbn_ista_haar": ([_vp, _vp, Layout, _vp, _vp, _vp, _i32, _f32, _f32, _i32, _i32, _vp], _i32),
         "gbn_dcf_pipe_menon": ([_vp, _i32, _vp, _vp], _i32),
+        "gbn_espirit_eigen": ([_vp, _i64, _i32, _i32, _i32, _vp, _vp, _vp], _i32),
         "gbn_haar_dwt": ([_i32, P(_i32), _i32, _i64, _i64, _vp, _vp, _i32, _vp], _i32),
         "gbn_prox_haar": ([_i32, P(_i32), _i32, _i64, _i64, _vp, _f32, _vp, _vp], _i32),
         "gbn_spread2d_noalloc": ([_i32, _vp, _vp, _i64, _vp, Layout, _i32, _i32, _i32, _f64, _f64, _vp, _vp], _i32),
