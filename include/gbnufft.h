@@ -124,7 +124,8 @@ int gbn_plan_create(const gbn_plan_desc *desc, gbn_plan **out);
 int gbn_plan_destroy(gbn_plan *plan);
 int gbn_plan_get_info(const gbn_plan *plan, gbn_plan_info *out);
 /* Synchronises the stream and reads the plan's device status word: GBN_ERR_TIMEOUT if
- * a kernel's bounded wait (the TMA window copies of the 2-D interp) gave up since the
+ * a kernel's bounded wait (the tensor copies of the 2-D interp windows and of the 3-D
+ * interp planes) gave up since the
  * last call, which also clears it; else GBN_OK.  No counterpart in the reference (its
  * kernels have no waits). */
 int gbn_plan_status(gbn_plan *plan, gbn_stream_t stream);
