@@ -73,8 +73,9 @@ typedef struct {
     int32_t interp_threads; /* threads per interp block: 128, 256 or 512 */
     int32_t interp_coil_group; /* coils per interp thread block: 1, 2, 4 or 8 (0: the
                                   group that pads the coil count least) */
-    int32_t interp_staging;    /* 2-D interp windows: 0 = tensor-memory-access copies
-                                  where the grid allows (default), 1 = thread loads */
+    int32_t interp_staging;    /* 2-D interp windows and 3-D interp planes: 0 = tensor-
+                                  memory-access copies where the grid allows (default),
+                                  1 = thread loads */
     int32_t dense_tile_samples; /* 3-D spread: tiles with at least this many samples (the
                                    k-space centre of radial data) accumulate with Kahan-
                                    compensated FP32 sums; 0 = 32768, negative = never */
@@ -123,11 +124,10 @@ int gbn_grid_params(int dim, int ms, int mt, int mu, double eps, int max_nspread
 int gbn_plan_create(const gbn_plan_desc *desc, gbn_plan **out);
 int gbn_plan_destroy(gbn_plan *plan);
 int gbn_plan_get_info(const gbn_plan *plan, gbn_plan_info *out);
-/* Synchronises the stream and reads the plan's device status word: GBN_ERR_TIMEOUT if
- * a kernel's bounded wait (the tensor copies of the 2-D interp windows and of the 3-D
- * interp planes) gave up since the
- * last call, which also clears it; else GBN_OK.  No counterpart in the reference (its
- * kernels have no waits). */
+/* Synchronises the stream and reads the plan's device status word: GBN_ERR_TIMEOUT if a
+ * kernel's bounded wait (the tensor copies of the 2-D interp windows and of the 3-D interp
+ * planes) gave up since the last call, which also clears it; else GBN_OK.  No counterpart
+ * in the reference (its kernels have no waits). */
 int gbn_plan_status(gbn_plan *plan, gbn_stream_t stream);
 
 /* Sorts the samples into spatial bins (device coordinates, float32 or float64,
