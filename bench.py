@@ -392,7 +392,11 @@ def run_gpu(args, wl):
                      "measured max SM clock"}
     result["kernels_ms"] = {"interp": round(t_interp, 4), "spread": round(t_spread, 4), "pad_deapod": round(t_pad, 4),
                             "fft": round(t_fft, 4), "crop_deapod": round(t_crop, 4)}
-    result["gpu_launches"] = 5 * args.steps  # pad, interp, zero-split, spread, crop per step (cuFFT not counted)
+    # this library's kernels per step (cuFFT and memsets not counted): pad, interp, crop and
+    # what the spread launched in the eager step before capture (split-tile zeroing unless the
+    # grid is cleared by a memset; the 3-D compensated instance for dense tiles)
+    per_step = 2 + (1 if info["interp_subproblems"] else 0) + plan.info()["spread_kernels"]
+    result["gpu_launches"] = per_step * args.steps
 
     # --- plain per-instance path: single-coil plan per group, eager, instance by instance
     plans = []

@@ -100,6 +100,7 @@ typedef struct {
     int64_t device_bytes;   /* device memory held by the plan */
     int32_t interp_coil_group;
     int64_t dense_subproblems; /* spread subproblems with compensated accumulation */
+    int32_t spread_kernels;    /* kernels the plan's last spread launched (0 before one) */
 } gbn_plan_info;
 
 /* element strides (in complex64 elements) of a strided complex array */

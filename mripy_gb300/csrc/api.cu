@@ -110,6 +110,7 @@ struct gbn_plan {
         spread_tile_off, home_tile_off, nsub, sub_off, spread_subs, interp_subs, cub_tmp, scratch,
         stage_in, stage_out, stage_w, split_tiles;
     int64_t n_dup = 0, n_spread_sub = 0, n_interp_sub = 0;
+    int spread_kernels = 0;   // kernels the last spread launched (split-tile zeroing included)
     uint64_t points_gen = 0;  // bumped by every gbn_set_points: captured graphs hold its buffers
 
     // solvers: workspace (state, partial sums, residual norms, vectors) and the captured
@@ -246,7 +247,8 @@ int dir_type2(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_INVERSE : 
 int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, float2 *grid, cudaStream_t s) {
     // tiles covered by several work items start from zero; when they are most of the grid
     // (dense trajectories), one memset of the whole grid is cheaper than per-tile blocks
-    if (2 * p->n_split > (int64_t)p->gs.ntiles * p->gs.n_traj)
+    const bool memset_grid = 2 * p->n_split > (int64_t)p->gs.ntiles * p->gs.n_traj;
+    if (memset_grid)
         GBN_CUDA(cudaMemsetAsync(grid, 0, sizeof(float2) * (size_t)p->G * (size_t)p->n_inst, s));
     else
         GBN_CUDA(launch_zero_split(p->gs, p->split_tiles.as<uint32_t>(), p->n_split, grid, s));
@@ -266,6 +268,7 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
     if (spread_smem_bytes(p->gs, cg) > (size_t)p->smem_optin)
         return fail(GBN_ERR_CAPACITY, "spread tile does not fit in shared memory");
     GBN_CUDA(launch_spread(a, p->n_spread_sub, cg, p->threads, s));
+    p->spread_kernels = (!memset_grid && p->n_split > 0 ? 1 : 0) + spread_kernel_count(a, p->n_spread_sub, cg, p->threads);
     return GBN_OK;
 }
 
@@ -824,6 +827,7 @@ int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     o->max_subproblem = p->max_sub;
     o->interp_coil_group = interp_cg(p);
     o->dense_subproblems = p->n_dense_sub;
+    o->spread_kernels = p->spread_kernels;
     o->device_bytes = (int64_t)p->device_bytes;
     return GBN_OK;
 }

@@ -142,6 +142,8 @@ cudaError_t launch_zero_split(const Geom &g, const uint32_t *split_tiles, int64_
                               cudaStream_t s);
 cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads,
                           cudaStream_t s);
+// kernels launch_spread runs for these arguments (the 3-D register path adds a Kahan instance)
+int spread_kernel_count(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads);
 cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, int threads,
                           cudaStream_t s);
 cudaError_t launch_interp_grad(const GradArgs &a, int64_t n_sub, int coil_group, int threads,

@@ -34,6 +34,17 @@ cudaError_t launch_zero_split(const Geom &g, const uint32_t *split_tiles, int64_
     return cudaGetLastError();
 }
 
+// the 3-D register-tile kernel applies: (x, y) rows of 4 per warp, z run of 4 * 32/coils cells
+static bool reg3d_path(const Geom &g, int coil_group, int threads) {
+    return grid3d_applies(g) && (coil_group == 4 || coil_group == 8) && threads <= 256 && g.tile[1] % kRegRows == 0 &&
+           g.tile[0] * g.tile[1] == kRegRows * (threads / 32) && g.tile[2] == kRegCols * (32 / coil_group);
+}
+
+int spread_kernel_count(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads) {
+    if (n_sub == 0) return 0;
+    return (reg3d_path(a.g, coil_group, threads) && a.any_dense) ? 2 : 1;
+}
+
 cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads, cudaStream_t s) {
     if (n_sub == 0) return cudaSuccess;
     const size_t smem = spread_smem_bytes(a.g, coil_group);
@@ -65,10 +76,8 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
         }));
         return err;
     }
-    // 3-D register-tile kernel: (x, y) rows of 4 per warp, z run of 4 * 32/coils cells
-    if (grid3d_applies(a.g) && (coil_group == 4 || coil_group == 8) && threads <= 256 &&
-        a.g.tile[1] % kRegRows == 0 && a.g.tile[0] * a.g.tile[1] == kRegRows * (threads / 32) &&
-        a.g.tile[2] == kRegCols * (32 / coil_group)) {
+    // 3-D register-tile kernel
+    if (reg3d_path(a.g, coil_group, threads)) {
         // plain sums for ordinary tiles, then (if any) Kahan-compensated sums for dense ones
         const size_t rsmem = spread3d_reg_smem_bytes(a.g, coil_group);
         GBN_DISPATCH_W(a.g.W, {

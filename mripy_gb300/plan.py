@@ -59,7 +59,7 @@ class Tuning:
         self.threads = threads
         self.interp_threads = interp_threads
         self.interp_coil_group = interp_coil_group
-        self.interp_staging = interp_staging  # 2-D: 0 tensor copies (TMA) where possible, 1 thread loads
+        self.interp_staging = interp_staging  # 0 tensor copies (TMA) where possible, 1 thread loads
 
     def key(self):
         return (self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
@@ -162,6 +162,7 @@ class NufftPlan:
             "threads": inf.threads, "interp_threads": inf.interp_threads, "max_subproblem": inf.max_subproblem,
             "device_bytes": inf.device_bytes, "interp_coil_group": inf.interp_coil_group,
             "dense_subproblems": inf.dense_subproblems,
+            "spread_kernels": inf.spread_kernels,
         }
 
     def status(self, stream=None):

@@ -574,3 +574,20 @@ def test_empty_trajectory():
     assert out.shape == (1, 16, 16, 1) and torch.count_nonzero(out) == 0
     k = p.type2(torch.ones((1, 16, 16, 1), dtype=torch.complex64, device="cuda"))
     assert k.shape == (0, 1)
+
+
+def test_spread_kernel_count_reported():
+    """plan.info()['spread_kernels'] counts the kernels the last spread launched: the 3-D
+    compensated instance appears when dense tiles exist, the split-tile zeroing when the grid
+    is not cleared by a memset."""
+    rng = np.random.default_rng(26)
+    xs = rng.uniform(-np.pi, np.pi, (3, 20000)) * 0.1          # everything in the centre
+    p3 = NufftPlan(3, (16, 16, 16), n_coil=8, eps=1e-6, max_nspread=6, dense_tile_samples=64)
+    p3.set_points([cuda(v) for v in xs])
+    assert p3.info()["spread_kernels"] == 0
+    p3.type1(cuda(cvec(rng, (20000, 8))))
+    assert p3.info()["dense_subproblems"] > 0 and p3.info()["spread_kernels"] >= 2
+    p3n = NufftPlan(3, (16, 16, 16), n_coil=8, eps=1e-6, max_nspread=6, dense_tile_samples=-1)
+    p3n.set_points([cuda(v) for v in xs])
+    p3n.type1(cuda(cvec(rng, (20000, 8))))
+    assert p3n.info()["spread_kernels"] == p3.info()["spread_kernels"] - 1
