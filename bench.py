@@ -20,7 +20,9 @@ replayed from one CUDA graph; value = (samples x coils) / step time.  Also repor
                workload's trajectory before the timed region (--tune off: library defaults)
   cpu_baseline the FP64 C restatement of mripy's CPU NUFFT on the host cores
   accuracy     relative L2 error vs the FP64 NUDFT on a subset
-  solver       c2: 20 CG-SENSE iterations through the graph-captured normal operator
+  solver       c2: 20 CG-SENSE iterations; c4: Pipe-Menon dcf + 30 IST iterations with a
+               level-4 Haar L1 prox (each iteration one CUDA graph)
+  autograd     c5: loss ||A(x; k) - y||^2 and its gradients with respect to image and trajectory
 
 --impl reference times mripy's CPU NUFFT algorithm (the oracle port; mripy itself is
 Python + numba and is not installed on the GPU host) on the same workload.
@@ -478,6 +480,8 @@ def run_gpu(args, wl):
         result["solver"] = cg_sense_time(torch, wl, coords)
     if wl.name == "c4":
         result["solver"] = ist_time(torch, wl, tuning)
+    if wl.name == "c5":
+        result["autograd"] = autograd_time(torch, wl, tuning)
 
     # --- CPU baseline: FP64 port of mripy's CPU NUFFT on the host cores (bounded sample)
     result["cpu_baseline"] = cpu_baseline(wl, reps=1)
@@ -559,6 +563,47 @@ def ist_time(torch, wl, tuning):
             "noise": "complex Gaussian, 30 dB SNR"}
 
 
+def autograd_time(torch, wl, tuning, steps=20):
+    """Differentiable NUFFT (the 16-coil spiral with perturbed float32 coordinates): loss =
+    ||A(x; k) - y||^2 with y simulated on the unperturbed trajectory.  One step = forward (bin
+    sort of the current trajectory, type-2) and backward (image gradient by the adjoint
+    pipeline, trajectory gradient by pad + FFT + the weight-derivative interp kernel)."""
+    from mripy_gb300 import autograd as AG
+    from mripy_gb300 import synth
+    from mripy_gb300.plan import NufftPlan
+    cfg = synth.config5()
+    plan = NufftPlan(2, wl.shape, n_coil=wl.n_coil, eps=wl.eps, tuning=tuning)
+    img = torch.from_numpy(np.ascontiguousarray(cfg["image"])).cuda()[None]
+    k_true = [torch.from_numpy(2 * np.pi * np.asarray(v, dtype=np.float64)).cuda() for v in cfg["k"]]
+    y = plan.set_points(k_true).type2(img).detach()
+    k = torch.from_numpy(np.stack([np.asarray(c, dtype=np.float32) for c in wl.coords])).cuda().requires_grad_(True)
+    x = (img * 0.9).requires_grad_(True)
+
+    def step():
+        x.grad = None
+        k.grad = None
+        c = AG.nufft_forward(x, k, plan)
+        loss = (c - y).abs().pow(2).sum()
+        loss.backward()
+        return loss
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        loss = step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    M, nc = wl.M, wl.n_coil
+    return {"steps": steps, "ms_per_step": round(ms, 4), "value": round(M * nc / (ms * 1e-3) / 1e6, 2),
+            "unit": UNIT, "loss": float(loss), "grad_k_rms": float(k.grad.pow(2).mean().sqrt()),
+            "includes": "bin sort of the perturbed trajectory, type-2, loss, backward: image gradient "
+                        "(type-1) and trajectory gradient (pad, FFT, weight-derivative interp)"}
+
+
 def cpu_baseline(wl, reps=1):
     """The FP64 C restatement of mripy's CPU NUFFT (oracle/) on the host cores: fwd + adj
     of group 0.  2-D: every coil, all samples; 3-D: 1 coil and the first 400,000 samples
@@ -620,6 +665,8 @@ def run_solver_only(args, wl):
         from mripy_gb300.tune import autotune
         tuning = autotune(wl.dim, wl.shape, coords, n_coil=wl.n_coil, n_traj=wl.n_traj, traj_offsets=wl.offsets,
                           eps=wl.eps, cache_file=args.tune_cache)
+    if args.part == "autograd":
+        return {"workload": wl.description, "part": "autograd", "autograd": autograd_time(torch, wl, tuning)}
     res = cg_sense_time(torch, wl, coords) if wl.name == "c2" else ist_time(torch, wl, tuning)
     return {"workload": wl.description, "part": "solver", "solver": res}
 
@@ -637,13 +684,14 @@ def main():
     ap.add_argument("--tune-cache", default=None,
                     help="JSON file of autotuner results: read if it holds this workload's key, else "
                          "written; lets a profiler run reuse the tiling of an earlier run")
-    ap.add_argument("--part", default="all", choices=["all", "solver"],
-                    help="solver: only the solver timing of c2 (CG-SENSE) or c4 (IST), one JSON line "
-                         "with its figures (for profiling the solver kernels)")
+    ap.add_argument("--part", default="all", choices=["all", "solver", "autograd"],
+                    help="solver: only the solver timing of c2 (CG-SENSE) or c4 (IST); autograd: only "
+                         "the differentiable step of c5; one JSON line with its figures (for profiling)")
     args = ap.parse_args()
-    if args.part == "solver":
-        if args.workload not in ("c2", "c4") or args.impl != "gb300":
-            ap.error("--part solver takes --workload c2 or c4 with the gb300 arm")
+    if args.part != "all":
+        ok = {"solver": ("c2", "c4"), "autograd": ("c5",)}[args.part]
+        if args.workload not in ok or args.impl != "gb300":
+            ap.error("--part %s takes --workload %s with the gb300 arm" % (args.part, " or ".join(ok)))
         from mripy_gb300 import build
         build.build()
         print(json.dumps(run_solver_only(args, make_workload(args.workload))))

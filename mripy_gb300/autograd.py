@@ -30,12 +30,25 @@ def _set_points(plan, coords):
                     plan.traj_offsets[-1] == cs[0].numel() else None)
 
 
+def _points_for_backward(ctx, coords):
+    """The backward pass reuses the forward pass's bin sort when nothing re-sorted the plan
+    in between (the plan's points generation is unchanged); otherwise it sorts again."""
+    if ctx.plan.points_generation != ctx.points_generation:
+        _set_points(ctx.plan, coords)
+
+
 def _group_scale(plan, img, inverse):
-    """Multiply each trajectory group's image by M_g (inverse=True) to undo type-1's 1/M_g."""
-    off = plan.traj_offsets
-    counts = torch.tensor([off[g + 1] - off[g] for g in range(plan.n_traj)], dtype=torch.float32,
-                          device=img.device)
-    s = counts if inverse else torch.where(counts > 0, 1.0 / counts, torch.zeros_like(counts))
+    """Multiply each trajectory group's image by M_g (inverse=True) to undo type-1's 1/M_g.
+    The per-group factors are built once per set of points (no host copy per call)."""
+    cache = getattr(plan, "_group_scale_cache", None)
+    if cache is None or cache[0] != plan.points_generation or cache[1] != img.device:
+        off = plan.traj_offsets
+        counts = torch.tensor([off[g + 1] - off[g] for g in range(plan.n_traj)], dtype=torch.float32,
+                              device=img.device)
+        inv = torch.where(counts > 0, 1.0 / counts.clamp(min=1.0), torch.zeros_like(counts))
+        cache = (plan.points_generation, img.device, counts, inv)
+        plan._group_scale_cache = cache
+    s = cache[2] if inverse else cache[3]
     return img * s.view((-1,) + (1,) * (img.dim() - 1))
 
 
@@ -46,6 +59,7 @@ class _Type2(torch.autograd.Function):
         img = image.detach().contiguous()
         out = plan.type2(img)
         ctx.plan = plan
+        ctx.points_generation = plan.points_generation
         ctx.save_for_backward(img, coords)
         return out
 
@@ -53,7 +67,7 @@ class _Type2(torch.autograd.Function):
     def backward(ctx, grad_out):
         img, coords = ctx.saved_tensors
         plan = ctx.plan
-        _set_points(plan, coords)
+        _points_for_backward(ctx, coords)
         g = grad_out.contiguous().to(torch.complex64)
         grad_img = grad_coords = None
         if ctx.needs_input_grad[0]:
@@ -72,6 +86,7 @@ class _Type1(torch.autograd.Function):
         _set_points(plan, coords)
         out = plan.type1(samples.detach().contiguous())
         ctx.plan = plan
+        ctx.points_generation = plan.points_generation
         ctx.save_for_backward(coords)
         return out
 
@@ -79,7 +94,7 @@ class _Type1(torch.autograd.Function):
     def backward(ctx, grad_out):
         (coords,) = ctx.saved_tensors
         plan = ctx.plan
-        _set_points(plan, coords)
+        _points_for_backward(ctx, coords)
         grad_c = None
         if ctx.needs_input_grad[0]:
             g = _group_scale(plan, grad_out.contiguous().to(torch.complex64), inverse=False)

@@ -967,7 +967,7 @@ int gbn_interp_grad_coords(gbn_plan *p, const void *grid, const void *grad_c, gb
     a.out = grad_xyz;
     a.scale = (float)p->desc.df;
     const int cg = interp_cg(p);
-    GBN_CUDA(launch_interp_grad(a, p->n_interp_sub, cg, p->threads, s));
+    GBN_CUDA(launch_interp_grad(a, p->n_interp_sub, cg, p->interp_threads, s));
     return GBN_OK;
 }
 

@@ -475,4 +475,128 @@ inline size_t interp2d_smem_bytes(const Geom &g, int cg) {
     return (size_t)(g.tile[0] + g.W - 1) * (g.tile[1] + g.W - 1) * cg * sizeof(float2);
 }
 
+// ----------------------------------------------------------------- trajectory gradient, 2-D
+// grad_x[j, d] += scale * Re( sum_coil conj(gc[j, coil]) dc_j/dx_d ) with
+// dc/dx_0 = sum dwx[kx] wy[ky] G and dc/dx_1 = sum wx[kx] dwy[ky] G, dw = w * dsc * dist
+// (the analytic derivative of the Gaussian weight at tap distance dist, in cells).  The
+// k_interp2d sample loop with two sums per tap slot: b += dwx G and a += wx G; the y weights
+// and their derivatives are applied once per slot, then the slots, and after weighting with
+// the upstream gradient the coils, are reduced by shuffles.  The window is staged as in
+// k_interp2d ([x][y][coil]).
+template <int WT, int CG>
+__global__ void __launch_bounds__(512) k_interp_grad2d(GradArgs a, float dsc0, float dsc1) {
+    using L = Lanes2D<WT, CG>;
+    extern __shared__ float4 smem_g2[];
+    float2 *win = reinterpret_cast<float2 *>(smem_g2);  // [WX][WY][CG]
+    const Geom &g = a.g;
+    const int4 sub = a.subs[blockIdx.x];
+    const int cg0 = blockIdx.y * CG;
+    const int grp = sub.x / g.ntiles;
+    const int tile = sub.x % g.ntiles;
+    const int o0 = (tile / g.ntile[1]) * g.tile[0];
+    const int o1 = (tile % g.ntile[1]) * g.tile[1];
+    const int W = WT ? WT : g.W;
+    const int ns = g.ns;
+    const int WX = g.tile[0] + W - 1, WY = g.tile[1] + W - 1;
+    const int nf0 = g.nf[0], nf1 = g.nf[1];
+    {
+        const int ws0 = o0 - (ns - 1), ws1 = o1 - (ns - 1);
+        const float2 *base = a.grid + ((int64_t)grp * g.n_coil + cg0) * g.G;
+        const int nitem = WX * WY * CG;
+        const float rWY = 1.f / (float)WY;
+        for (int i = threadIdx.x; i < nitem; i += blockDim.x) {
+            const int c = i % CG, cell = i / CG;
+            const int wx = div_small(cell, rWY), wy = cell - wx * WY;
+            const int gx = wrap_fast(ws0 + wx, nf0), gy = wrap_fast(ws1 + wy, nf1);
+            win[i] = (cg0 + c < g.n_coil) ? base[(int64_t)c * g.G + (int64_t)gx * nf1 + gy] : make_float2(0.f, 0.f);
+        }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int c = lane % CG, q = lane / CG;
+    const int kk = lane & 15;
+    const float beta = lane < 16 ? g.beta2[0] : g.beta2[1];
+    const float dsc = lane < 16 ? dsc0 : dsc1;
+    for (int s = warp; s < sub.z; s += nw) {
+        const float4 p = a.pts[(int64_t)sub.y + s];
+        const uint32_t j = a.idx[(int64_t)sub.y + s];
+        int c0x, c0y, c0z;
+        unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
+        int ccx = c0x + ns - 1, ccy = c0y + ns - 1;
+        ccx -= ccx >= nf0 ? nf0 : 0;
+        ccy -= ccy >= nf1 ? nf1 : 0;
+        const int rel0 = ccx - o0, rel1 = ccy - o1;
+        float myw = 0.f, mydw = 0.f;
+        if (kk < W) {
+            const float d = (lane < 16 ? p.x : p.y) + (float)(ns - 1 - kk);
+            myw = exp2f(-beta * d * d);
+            mydw = myw * dsc * d;
+        }
+        float wy[L::KT], dwy[L::KT];
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) {
+            const int ky = q + t * L::NQ;
+            const int src = 16 + (ky < 16 ? ky : 15);
+            const float v = __shfl_sync(0xffffffffu, myw, src), dv = __shfl_sync(0xffffffffu, mydw, src);
+            wy[t] = ky < W ? v : 0.f;
+            dwy[t] = ky < W ? dv : 0.f;
+        }
+        float2 sa[L::KT], sb[L::KT];
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) {
+            sa[t] = make_float2(0.f, 0.f);
+            sb[t] = make_float2(0.f, 0.f);
+        }
+        const float2 *rowbase = win + ((size_t)rel0 * WY + rel1) * CG + c;
+#pragma unroll
+        for (int kx = 0; kx < L::WMAX; ++kx) {
+            if (WT == 0 && kx >= W) break;
+            const float wx = __shfl_sync(0xffffffffu, myw, kx), dwx = __shfl_sync(0xffffffffu, mydw, kx);
+            const float2 wx2 = make_float2(wx, wx), dwx2 = make_float2(dwx, dwx);
+            const float2 *row = rowbase + (size_t)kx * WY * CG;
+#pragma unroll
+            for (int t = 0; t < L::KT; ++t) {
+                const int ky = q + t * L::NQ;
+                if (ky < W) {
+                    const float2 G = row[ky * CG];
+                    sa[t] = __ffma2_rn(wx2, G, sa[t]);
+                    sb[t] = __ffma2_rn(dwx2, G, sb[t]);
+                }
+            }
+        }
+        float gx_re = 0.f, gx_im = 0.f, gy_re = 0.f, gy_im = 0.f;
+#pragma unroll
+        for (int t = 0; t < L::KT; ++t) {
+            gx_re = fmaf(wy[t], sb[t].x, gx_re);
+            gx_im = fmaf(wy[t], sb[t].y, gx_im);
+            gy_re = fmaf(dwy[t], sa[t].x, gy_re);
+            gy_im = fmaf(dwy[t], sa[t].y, gy_im);
+        }
+#pragma unroll
+        for (int off = CG; off < 32; off <<= 1) {
+            gx_re += __shfl_xor_sync(0xffffffffu, gx_re, off);
+            gx_im += __shfl_xor_sync(0xffffffffu, gx_im, off);
+            gy_re += __shfl_xor_sync(0xffffffffu, gy_re, off);
+            gy_im += __shfl_xor_sync(0xffffffffu, gy_im, off);
+        }
+        // Re(conj(gc) * dc/dx) per coil (slot-0 lanes), then summed over the coils
+        float g0 = 0.f, g1 = 0.f;
+        if (q == 0 && cg0 + c < g.n_coil) {
+            const float2 gc = a.gc[(int64_t)j * a.c_elem + (int64_t)(cg0 + c) * a.c_coil];
+            g0 = gc.x * gx_re + gc.y * gx_im;
+            g1 = gc.x * gy_re + gc.y * gy_im;
+        }
+#pragma unroll
+        for (int off = 1; off < CG; off <<= 1) {
+            g0 += __shfl_xor_sync(0xffffffffu, g0, off);
+            g1 += __shfl_xor_sync(0xffffffffu, g1, off);
+        }
+        if (lane == 0) {
+            atomicAdd(&a.out[(int64_t)j * 2], g0 * a.scale);
+            atomicAdd(&a.out[(int64_t)j * 2 + 1], g1 * a.scale);
+        }
+    }
+}
+
 }  // namespace gbn

@@ -200,6 +200,17 @@ cudaError_t launch_interp_grad(const GradArgs &a, int64_t n_sub, int coil_group,
         dsc[d] = (float)(-2.0 * beta / h);
     }
     cudaError_t err = cudaSuccess;
+    if (use_2d_path(a.g)) {  // warp per sample, lanes = coils x tap slots
+        GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
+            auto kern = k_interp_grad2d<WT, CG>;
+            err = set_smem(kern, smem);
+            if (err == cudaSuccess) {
+                kern<<<grid, threads, smem, s>>>(a, dsc[0], dsc[1]);
+                err = cudaGetLastError();
+            }
+        }));
+        return err;
+    }
     GBN_DISPATCH_D(a.g.dim, GBN_DISPATCH_W(a.g.W, GBN_DISPATCH_CG(coil_group, {
         auto kern = k_interp_grad<D, WT, CG>;
         err = set_smem(kern, smem);

@@ -137,6 +137,7 @@ class NufftPlan:
         self._h = h
         self.traj_offsets = None
         self.n_samples = 0
+        self.points_generation = 0  # bumped by every set_points
 
     # ------------------------------------------------------------------ lifetime
     def close(self):
@@ -203,6 +204,7 @@ class NufftPlan:
                                          ptrs[0], ptrs[1], ptrs[2], arr, _stream(stream)))
         self.traj_offsets = off
         self.n_samples = M
+        self.points_generation += 1
         return self
 
     # ------------------------------------------------------------------ layouts

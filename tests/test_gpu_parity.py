@@ -541,6 +541,24 @@ def test_interp_grad_coords_against_fp64_gradients():
             assert abs(gk[j, d] - fd) <= 1e-3 * np.abs(exact).max()
 
 
+@pytest.mark.parametrize("nc,eps", [(12, 1e-5), (3, 5e-6)])
+def test_interp_grad_coords_multicoil(nc, eps):
+    """The warp-per-sample 2-D gradient kernel over several coil groups (12 coils: a full
+    group and a half-masked one) against the FP64 NUDFT gradient summed over the coils."""
+    rng = np.random.default_rng(21)
+    shape, M = (32, 28), 2500
+    xs = rng.uniform(-np.pi, np.pi, (2, M))
+    xs[:, :800] *= 0.2
+    F = cvec(rng, shape + (nc,)).astype(np.complex128)
+    gc = cvec(rng, (M, nc)).astype(np.complex128)
+    p = NufftPlan(2, shape, n_coil=nc, eps=eps).set_points([cuda(xs[0]), cuda(xs[1])])
+    grid = p.pad_deapod(cuda(F.astype(np.complex64))[None])
+    p.fft(grid, -1)
+    gk = p.interp_grad_coords(grid, cuda(gc.astype(np.complex64))).cpu().numpy()
+    exact = O.nudft_type2_coord_grad((xs[0], xs[1]), F, shape, gc)            # summed over the coils
+    assert rel(gk, exact) < 1e-3
+
+
 # ------------------------------------------------------------------ failure paths
 def test_non_finite_coordinate_is_rejected():
     x = torch.zeros(100, dtype=torch.float64, device="cuda")
