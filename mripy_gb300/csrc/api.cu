@@ -107,7 +107,7 @@ struct gbn_plan {
     std::vector<int64_t> traj_off;
     DevBuf traj_off_d, grp_scale, pts, home_key, home_keys_sorted, touch_count, touch_off, home_count,
         iota, home_idx, home_pts, dup_keys, dup_vals, dup_keys_sorted, dup_idx, dup_pts, spread_count,
-        spread_tile_off, home_tile_off, nsub, sub_off, spread_subs, interp_subs, cub_tmp, scratch,
+        spread_tile_off, home_tile_off, nsub, sub_off, nsub_i, sub_off_i, spread_subs, interp_subs, cub_tmp, scratch,
         stage_in, stage_out, stage_w, split_tiles;
     int64_t n_dup = 0, n_spread_sub = 0, n_interp_sub = 0;
     int spread_kernels = 0;   // kernels the last spread launched (split-tile zeroing included)
@@ -417,32 +417,48 @@ int key_bits(uint64_t max_key) {
 }
 
 // count -> tile offsets (exclusive), subproblem table
-int build_subs(gbn_plan *p, const Geom &g, uint32_t *count, DevBuf &tile_off, DevBuf &subs, int every_tile,
-               int max_sub, uint32_t dense_min, uint32_t *n_dense, uint32_t *split_list, uint32_t *n_split,
-               int64_t *n_sub_out, cudaStream_t s) {
-    const int64_t T = (int64_t)g.ntiles * g.n_traj;
-    GBN_TRY(ensure(p, tile_off, sizeof(uint32_t) * T));
-    GBN_TRY(ensure(p, p->nsub, sizeof(uint32_t) * T));
-    GBN_TRY(ensure(p, p->sub_off, sizeof(uint32_t) * (T + 1)));
-    uint32_t *toff = tile_off.as<uint32_t>();
+// Work items of one bin geometry, in two phases so that the spread's and the interp's
+// totals (and the dense / split counts) come back to the host in one synchronisation.
+struct SubsJob {
+    const Geom *g;
+    uint32_t *count;      // samples per tile
+    DevBuf *tile_off;     // their exclusive scan
+    DevBuf *nsub;         // work items per tile
+    DevBuf *sub_off;      // their exclusive scan
+    int every_tile, max_sub;
+    uint32_t dense_min;
+    uint32_t *n_dense, *n_split;  // device counters (may be null)
+    int64_t T = 0;
+};
+
+// scans and per-tile item counts; the last tile's offset and count are copied into last[2]
+int subs_count(gbn_plan *p, SubsJob &j, uint32_t last[2], cudaStream_t s) {
+    j.T = (int64_t)j.g->ntiles * j.g->n_traj;
+    const int64_t T = j.T;
+    GBN_TRY(ensure(p, *j.tile_off, sizeof(uint32_t) * T));
+    GBN_TRY(ensure(p, *j.nsub, sizeof(uint32_t) * T));
+    GBN_TRY(ensure(p, *j.sub_off, sizeof(uint32_t) * (T + 1)));
+    uint32_t *toff = j.tile_off->as<uint32_t>(), *ns_ = j.nsub->as<uint32_t>(), *soff = j.sub_off->as<uint32_t>();
     GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
-        return cub::DeviceScan::ExclusiveSum(tmp, bytes, count, toff, (int)T, s);
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, j.count, toff, (int)T, s);
     }));
-    GBN_CUDA(launch_count_subs(count, T, max_sub, every_tile, p->nsub.as<uint32_t>(), s));
-    uint32_t *soff = p->sub_off.as<uint32_t>();
-    uint32_t *ns_ = p->nsub.as<uint32_t>();
+    GBN_CUDA(launch_count_subs(j.count, T, j.max_sub, j.every_tile, j.dense_min, ns_, j.n_dense, j.n_split, s));
     GBN_TRY(cub_call(p, [&](void *tmp, size_t &bytes) {
         return cub::DeviceScan::ExclusiveSum(tmp, bytes, ns_, soff, (int)T, s);
     }));
-    uint32_t last[2] = {0, 0};
     GBN_CUDA(cudaMemcpyAsync(&last[0], soff + (T - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     GBN_CUDA(cudaMemcpyAsync(&last[1], ns_ + (T - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    GBN_CUDA(cudaStreamSynchronize(s));
+    return GBN_OK;
+}
+
+// after the synchronisation: allocate and fill the work items
+int subs_build(gbn_plan *p, const SubsJob &j, const uint32_t last[2], DevBuf &subs, uint32_t *split_list,
+               uint32_t *split_cursor, int64_t *n_sub_out, cudaStream_t s) {
     const int64_t n_sub = (int64_t)last[0] + last[1];
     if (n_sub > 0x7FFFFFFF) return fail(GBN_ERR_CAPACITY, "too many subproblems");
     GBN_TRY(ensure(p, subs, sizeof(int4) * (size_t)std::max<int64_t>(n_sub, 1)));
-    GBN_CUDA(launch_build_subs(count, toff, soff, T, max_sub, every_tile, dense_min, n_dense, split_list, n_split,
-                               subs.as<int4>(), s));
+    GBN_CUDA(launch_build_subs(j.count, j.tile_off->as<uint32_t>(), j.sub_off->as<uint32_t>(), j.T, j.max_sub,
+                               j.every_tile, j.dense_min, split_list, split_cursor, subs.as<int4>(), s));
     *n_sub_out = n_sub;
     return GBN_OK;
 }
@@ -549,25 +565,29 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
         GBN_CUDA(launch_gather_pts(p->pts.as<float4>(), vout, M, p->home_pts.as<float4>(), s));
     }
     // 3-D: spread tiles with at least dense_min samples (the k-space centre of radial
-    // trajectories) accumulate with compensated sums; their subproblem count lands in
-    // the second status word
+    // trajectories) accumulate with compensated sums; status word 1 counts their work items,
+    // word 2 the split tiles (zeroed before each spread), word 3 is the split list's cursor
     const uint32_t dense_min = p->dim == 3 && p->dense_min > 0 ? (uint32_t)p->dense_min : 0u;
-    // the list of split spread tiles (zeroed before each spread) and its length in the
-    // third status word
     GBN_TRY(ensure(p, p->split_tiles, sizeof(uint32_t) * (size_t)std::max<int64_t>(Ts, 1)));
-    GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, 2 * sizeof(uint32_t), s));
-    GBN_TRY(build_subs(p, p->gs, scount, p->spread_tile_off, p->spread_subs, 1, p->max_sub, dense_min,
-                       p->kstatus + 1, p->split_tiles.as<uint32_t>(), p->kstatus + 2, &p->n_spread_sub, s));
+    GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, 3 * sizeof(uint32_t), s));
     // the plane-streaming 3-D interp holds a chunk of kPlaneSamples samples' state; work
     // items of at most that size stream each window once
     const int interp_max_sub = interp3d_planes_smem(p->gi, interp_cg(p), p->interp_threads) > 0
                                    ? std::min(p->max_sub, kPlaneSamples)
                                    : p->max_sub;
-    GBN_TRY(build_subs(p, p->gi, home_count, p->home_tile_off, p->interp_subs, 0, interp_max_sub, 0u, nullptr,
-                       nullptr, nullptr, &p->n_interp_sub, s));
-    uint32_t counts[2] = {0, 0};
-    GBN_CUDA(cudaMemcpyAsync(counts, p->kstatus + 1, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SubsJob js{&p->gs, scount, &p->spread_tile_off, &p->nsub, &p->sub_off, 1, p->max_sub, dense_min,
+               p->kstatus + 1, p->kstatus + 2};
+    SubsJob ji{&p->gi, home_count, &p->home_tile_off, &p->nsub_i, &p->sub_off_i, 0, interp_max_sub, 0u, nullptr,
+               nullptr};
+    uint32_t sizes[6] = {0, 0, 0, 0, 0, 0};  // spread last offset / count, interp ditto, dense, split
+    GBN_TRY(subs_count(p, js, sizes, s));
+    GBN_TRY(subs_count(p, ji, sizes + 2, s));
+    GBN_CUDA(cudaMemcpyAsync(sizes + 4, p->kstatus + 1, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     GBN_CUDA(cudaStreamSynchronize(s));
+    GBN_TRY(subs_build(p, js, sizes, p->spread_subs, p->split_tiles.as<uint32_t>(), p->kstatus + 3,
+                       &p->n_spread_sub, s));
+    GBN_TRY(subs_build(p, ji, sizes + 2, p->interp_subs, nullptr, nullptr, &p->n_interp_sub, s));
+    const uint32_t counts[2] = {sizes[4], sizes[5]};
     p->n_dense_sub = counts[0];
     p->n_split = counts[1];
     p->points_gen += 1;
@@ -707,13 +727,13 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     }
     // word 0: kernel status bits; words 1, 2: dense spread subproblems and split spread
     // tiles (counted by set_points)
-    e = cudaMalloc((void **)&p->kstatus, 3 * sizeof(uint32_t));
+    e = cudaMalloc((void **)&p->kstatus, 4 * sizeof(uint32_t));
     if (e != cudaSuccess) {
         cudaGetLastError();
         p->kstatus = nullptr;
         return bail(fail(GBN_ERR_ALLOC, "status word allocation failed"));
     }
-    e = cudaMemset(p->kstatus, 0, 3 * sizeof(uint32_t));
+    e = cudaMemset(p->kstatus, 0, 4 * sizeof(uint32_t));
     if (e == cudaSuccess) e = launch_build_tables(p->dim, p->m, p->nf, p->tau, p->tab[0], p->tab[1], p->tab[2], 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return bail(fail(GBN_ERR_CUDA, std::string("table build: ") + cudaGetErrorString(e)));
@@ -784,7 +804,7 @@ int gbn_plan_destroy(gbn_plan *p) {
     DevBuf *bufs[] = {&p->traj_off_d, &p->grp_scale, &p->pts, &p->home_key, &p->home_keys_sorted,
                       &p->touch_count, &p->touch_off, &p->home_count, &p->iota, &p->home_idx, &p->home_pts,
                       &p->dup_keys, &p->dup_vals, &p->dup_keys_sorted, &p->dup_idx, &p->dup_pts,
-                      &p->spread_count, &p->spread_tile_off, &p->home_tile_off, &p->nsub, &p->sub_off,
+                      &p->spread_count, &p->spread_tile_off, &p->home_tile_off, &p->nsub, &p->sub_off, &p->nsub_i, &p->sub_off_i,
                       &p->spread_subs, &p->interp_subs, &p->cub_tmp, &p->scratch, &p->stage_in,
                       &p->stage_out, &p->stage_w, &p->split_tiles, &p->solve_ws, &p->dcf_ws};
     for (gbn_plan::SolveGraph &sg : p->solve_graph)

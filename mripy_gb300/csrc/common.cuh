@@ -95,15 +95,16 @@ cudaError_t launch_dup_keys(const float4 *pts, int64_t M, const int64_t *d_traj_
                             uint32_t *tile_count, cudaStream_t s);
 cudaError_t launch_gather_pts(const float4 *pts, const uint32_t *idx, int64_t n, float4 *out,
                               cudaStream_t s);
-// dense_min > 0: subproblems of tiles with at least dense_min samples get kDenseFlag and
-// are counted into *n_dense (may be null).  split_list (may be null): the indices of the
-// tiles covered by more than one subproblem are appended, counted in *n_split.
+// dense_min > 0: subproblems of tiles with at least dense_min samples get kDenseFlag.
+// split_list (may be null): the indices of the tiles covered by more than one subproblem
+// are appended at *split_cursor (zeroed by the caller).
 cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
                               int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min,
-                              uint32_t *n_dense, uint32_t *split_list, uint32_t *n_split, int4 *subs,
-                              cudaStream_t s);
-cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int every_tile,
-                              uint32_t *n_sub, cudaStream_t s);
+                              uint32_t *split_list, uint32_t *split_cursor, int4 *subs, cudaStream_t s);
+// work items per tile; n_dense (may be null) accumulates the items of tiles with at least
+// dense_min samples, n_split (may be null) the tiles split over several items
+cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int every_tile, uint32_t dense_min,
+                              uint32_t *n_sub, uint32_t *n_dense, uint32_t *n_split, cudaStream_t s);
 
 // grid.cu
 struct SpreadArgs {

@@ -131,20 +131,25 @@ __global__ void k_gather_pts(const float4 *__restrict__ pts, const uint32_t *__r
     if (i < n) out[i] = pts[idx[i]];
 }
 
+// per tile: its number of work items; optionally counts the work items of dense tiles
+// (n_dense) and the tiles split over several items (n_split)
 __global__ void k_count_subs(const uint32_t *__restrict__ count, int64_t n, int max_sub, int every_tile,
-                             uint32_t *__restrict__ n_sub) {
+                             uint32_t dense_min, uint32_t *__restrict__ n_sub, uint32_t *n_dense,
+                             uint32_t *n_split) {
     int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= n) return;
     uint32_t c = count[t];
     uint32_t s = (c + (uint32_t)max_sub - 1) / (uint32_t)max_sub;
     if (every_tile && s == 0) s = 1;
     n_sub[t] = s;
+    if (n_dense && dense_min > 0 && c >= dense_min) atomicAdd(n_dense, s);
+    if (n_split && s > 1) atomicAdd(n_split, 1u);
 }
 
 __global__ void k_build_subs(const uint32_t *__restrict__ count, const uint32_t *__restrict__ tile_off,
                              const uint32_t *__restrict__ sub_off, int64_t n, int max_sub, int every_tile,
-                             uint32_t dense_min, uint32_t *__restrict__ n_dense, uint32_t *__restrict__ split_list,
-                             uint32_t *__restrict__ n_split, int4 *__restrict__ subs) {
+                             uint32_t dense_min, uint32_t *__restrict__ split_list,
+                             uint32_t *__restrict__ split_cursor, int4 *__restrict__ subs) {
     int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= n) return;
     uint32_t c = count[t];
@@ -152,8 +157,7 @@ __global__ void k_build_subs(const uint32_t *__restrict__ count, const uint32_t 
     if (every_tile && s == 0) s = 1;
     uint32_t o = sub_off[t];
     const bool dense = dense_min > 0 && c >= dense_min;
-    if (dense && n_dense) atomicAdd(n_dense, s);
-    if (s > 1 && split_list) split_list[atomicAdd(n_split, 1u)] = (uint32_t)t;  // order is irrelevant
+    if (s > 1 && split_list) split_list[atomicAdd(split_cursor, 1u)] = (uint32_t)t;  // order is irrelevant
     for (uint32_t k = 0; k < s; ++k) {
         uint32_t start = k * (uint32_t)max_sub;
         uint32_t len = c > start ? min((uint32_t)max_sub, c - start) : 0u;
@@ -200,21 +204,21 @@ cudaError_t launch_gather_pts(const float4 *pts, const uint32_t *idx, int64_t n,
     return cudaGetLastError();
 }
 
-cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int every_tile, uint32_t *n_sub,
-                              cudaStream_t s) {
+cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int every_tile, uint32_t dense_min,
+                              uint32_t *n_sub, uint32_t *n_dense, uint32_t *n_split, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_count_subs<<<blocks_for(n, 256), 256, 0, s>>>(count, n, max_sub, every_tile, n_sub);
+    k_count_subs<<<blocks_for(n, 256), 256, 0, s>>>(count, n, max_sub, every_tile, dense_min, n_sub, n_dense,
+                                                    n_split);
     return cudaGetLastError();
 }
 
 cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
                               int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min,
-                              uint32_t *n_dense, uint32_t *split_list, uint32_t *n_split, int4 *subs,
-                              cudaStream_t s) {
+                              uint32_t *split_list, uint32_t *split_cursor, int4 *subs, cudaStream_t s) {
     if (ntiles_total == 0) return cudaSuccess;
     k_build_subs<<<blocks_for(ntiles_total, 256), 256, 0, s>>>(count, tile_off, sub_off, ntiles_total, max_sub,
-                                                               every_tile, dense_min, n_dense, split_list,
-                                                               n_split, subs);
+                                                               every_tile, dense_min, split_list, split_cursor,
+                                                               subs);
     return cudaGetLastError();
 }
 
