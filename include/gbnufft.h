@@ -223,7 +223,9 @@ int gbn_graph_destroy(gbn_graph *graph);
 /* Linear CG on N x = rhs, n_iter iterations: the reference has no CG-SENSE routine (its
  * linear CG on the normal equations, pics/proximal_func.py:379-406, is commented out), so
  * this is that algorithm with forward_backward as N.  Inner products in FP64; res_norms
- * (device double[n_iter], may be NULL) receives ||r|| after every iteration. */
+ * (device double[n_iter], may be NULL) receives ||r|| after every iteration.  With several
+ * trajectory groups N is block-diagonal and the CG runs on all groups' images as one
+ * vector (one set of scalars), not one CG per group. */
 int gbn_cg_sense(gbn_plan *plan, const void *sens, gbn_layout sens_layout, const float *dcf,
                  const void *rhs, void *x, int32_t n_iter, double *res_norms, int32_t flags,
                  gbn_stream_t stream);

@@ -260,3 +260,23 @@ def test_pipe_menon_dcf_needs_one_coil():
     plan.set_points([torch.zeros(10, dtype=torch.float64, device="cuda")] * 2)
     with pytest.raises(RuntimeError):
         plan.pipe_menon_dcf(3)
+
+
+def test_fista_ragged_frames_match_per_frame_oracle():
+    """gbn_ista_haar over two trajectory groups of different sizes: the normal operator is
+    block-diagonal over frames and the Haar tiles never cross an image, so each frame's
+    iterate equals a separate FP64 FISTA on that frame."""
+    rng = np.random.default_rng(51)
+    shape, nc = (32, 32), 2
+    counts = [3000, 1700]
+    off = [0, counts[0], counts[0] + counts[1]]
+    xs = rng.uniform(-np.pi, np.pi, (2, off[-1]))
+    p = P.NufftPlan(2, shape, n_coil=nc, n_traj=2, eps=EPS_OP)
+    p.set_points([torch.tensor(v, device="cuda") for v in xs], traj_offsets=off)
+    rhs = _crand(rng, (2,) + shape + (nc,))
+    x = p.ista(torch.from_numpy(rhs).cuda(), 5, 0.5, 1e-2, 2, fista=True)
+    for g in range(2):
+        a, b = off[g], off[g + 1]
+        ref = SO.fista(_normal64((xs[0][a:b], xs[1][a:b]), shape), rhs[g].astype(np.complex128), 5, 0.5, 1e-2,
+                       2, (0, 1))
+        assert rel(x[g], ref) < 1e-4
