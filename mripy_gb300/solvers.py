@@ -11,7 +11,8 @@ wavelet soft-threshold (pics/CS_MRI_solvers_func.py, pics/proximal_func.py).
                     NUFFT / SENSE operators with T = DWTnd('haar') (or no T) run natively
                     (gbn_ista_haar: normal operator + one fused gradient-step / Haar prox /
                     momentum kernel per iteration, one graph); any other operator runs
-                    ``IST_32`` / ``FIST_32`` (:75-86, 207-224) on its callables.
+                    ``IST_32`` / ``FIST_32`` (:75-86, 207-224) on its callables, or ``IST_3`` /
+                    ``FIST_3`` (:63-73, 189-205) when it has no forward_backward.
 * ``prox_l1_soft_thresh2``, ``prox_l1_Tf_soft_thresh2``   proximal_func.py:20-24, 46-52
 * ``DWTnd``         DWTnd with the Haar wavelet (pics/operators_class.py:394-416; pywt's
                     wavedecn + coeffs_to_array layout, dwt/dwt_func.py:15-23) on the GPU
@@ -21,8 +22,8 @@ import torch
 
 from . import plan as _plan
 
-__all__ = ["cg_sense", "IST_32", "FIST_32", "IST_wrap", "FIST_wrap", "prox_l1_Tf_soft_thresh2",
-           "prox_l1_soft_thresh2", "DWTnd"]
+__all__ = ["cg_sense", "IST_32", "FIST_32", "IST_3", "FIST_3", "IST_2", "FIST_2", "IST_wrap", "FIST_wrap",
+           "prox_l1_Tf_soft_thresh2", "prox_l1_soft_thresh2", "DWTnd"]
 
 
 def _vdot(a, b):
@@ -134,6 +135,59 @@ def FIST_32(Afunc, invAAfunc, invAfunc, Tfunc, invTfunc, b, Nite, step, th, verb
     return x
 
 
+def IST_3(Afunc, invAfunc, Tfunc, invTfunc, b, Nite, step, th, verbose=False):
+    """IST with the operator applied as forward and adjoint (CS_MRI_solvers_func.py:63-73):
+    for operators without forward_backward."""
+    x_acc = step * invAfunc(b)
+    x = x_acc
+    for _ in range(Nite):
+        x = prox_l1_Tf_soft_thresh2(Tfunc, invTfunc, x_acc, th)
+        r = Afunc(x) - b
+        x_acc = x_acc - step * invAfunc(r)
+        if verbose:
+            print(float(np.linalg.norm(np.asarray(r.cpu() if isinstance(r, torch.Tensor) else r))))
+    return x
+
+
+def FIST_3(Afunc, invAfunc, Tfunc, invTfunc, b, Nite, step, th, verbose=False):
+    """FISTA with the operator applied as forward and adjoint (CS_MRI_solvers_func.py:190-205)."""
+    y = step * invAfunc(b)
+    y_acc = y * 0
+    x_pre = y
+    t = [1.0] * (Nite + 1)
+    x = y
+    for k in range(Nite):
+        r = Afunc(y) - b
+        y_acc = y_acc - step * invAfunc(r)
+        x = prox_l1_Tf_soft_thresh2(Tfunc, invTfunc, y_acc, th)
+        t[k + 1] = (1 + (1 + 4 * t[k] ** 2) ** 0.5) / 2
+        y = x + ((t[k] - 1) / t[k + 1]) * (x - x_pre)
+        x_pre = x
+        if verbose:
+            print(float(np.linalg.norm(np.asarray(r.cpu() if isinstance(r, torch.Tensor) else r))))
+    return x
+
+
+class _Identity:
+    def forward(self, v):
+        return v
+
+    def backward(self, v):
+        return v
+
+
+def IST_2(Afunc, invAfunc, b, Nite, step, th, verbose=False):
+    """IST_3 without a transform (CS_MRI_solvers_func.py:29-40)."""
+    T = _Identity()
+    return IST_3(Afunc, invAfunc, T.backward, T.forward, b, Nite, step, th, verbose)
+
+
+def FIST_2(Afunc, invAfunc, b, Nite, step, th, verbose=False):
+    """FIST_3 without a transform (CS_MRI_solvers_func.py:151-166)."""
+    T = _Identity()
+    return FIST_3(Afunc, invAfunc, T.backward, T.forward, b, Nite, step, th, verbose)
+
+
 def _haar_level(Topt, dim_axes):
     """Level of a Haar DWTnd over exactly the image axes, 0 for no transform, else None."""
     if Topt is None:
@@ -148,7 +202,10 @@ def _wrap(fista, Aopt, Topt, b, Nite, step, th):
     step = 0.1 if step is None else step
     th = 0.04 if th is None else th
     if not hasattr(Aopt, "forward_backward"):
-        raise TypeError("the operator needs forward_backward (the *_32 solver forms)")
+        # the reference's *_3 / *_2 forms: forward and adjoint applied separately
+        T = _Identity() if Topt is None else Topt
+        solver = FIST_3 if fista else IST_3
+        return solver(Aopt.forward, Aopt.backward, T.backward, T.forward, b, Nite, step, th)
     dim = getattr(getattr(Aopt, "Bopt", Aopt), "dim", None)
     native = (hasattr(Aopt, "normal_solver") and dim is not None and Nite >= 1
               and _haar_level(Topt, tuple(range(dim))) is not None
@@ -164,13 +221,7 @@ def _wrap(fista, Aopt, Topt, b, Nite, step, th):
             x = x.reshape(invAb.shape)
             return x.cpu().numpy().astype(np.complex128) if was_np else x
     if Topt is None:
-        class _Id:
-            def forward(self, v):
-                return v
-
-            def backward(self, v):
-                return v
-        Topt = _Id()
+        Topt = _Identity()
     solver = FIST_32 if fista else IST_32
     return solver(Aopt.forward, Aopt.forward_backward, Aopt.backward, Topt.backward, Topt.forward, b, Nite, step,
                   th)

@@ -72,6 +72,42 @@ def test_fista_matches_reference_loop():
     assert np.allclose(out.numpy(), ref, atol=1e-10)
 
 
+class _ForwardAdjointOp:
+    """an operator without forward_backward: mripy's wrappers fall back to the *_3 forms"""
+    def __init__(self, A):
+        self.A = A
+
+    def forward(self, x):
+        return self.A @ x
+
+    def backward(self, y):
+        return self.A.conj().T @ y
+
+
+def test_fista_without_forward_backward_matches_fist3_loop():
+    rng = np.random.default_rng(4)
+    A = (rng.standard_normal((40, 30)) + 1j * rng.standard_normal((40, 30))) / 8
+    b = rng.standard_normal(40) + 1j * rng.standard_normal(40)
+    # numpy restatement of FIST_3 (CS_MRI_solvers_func.py:189-205) with T = identity
+    y = 0.5 * (A.conj().T @ b)
+    y_acc = np.zeros_like(y)
+    x_pre = y
+    t = np.ones(16)
+    for k in range(15):
+        r = A @ y - b
+        y_acc = y_acc - 0.5 * (A.conj().T @ r)
+        a = np.abs(y_acc) - 0.05
+        a[a < 0] = 0
+        x = y_acc / (np.abs(y_acc) + 1e-6) * a
+        t[k + 1] = (1 + (1 + 4 * t[k] ** 2) ** 0.5) / 2
+        y = x + ((t[k] - 1) / t[k + 1]) * (x - x_pre)
+        x_pre = x
+    out = solvers.FIST_wrap(_ForwardAdjointOp(torch.from_numpy(A)), None, torch.from_numpy(b), 15, 0.5, 0.05)
+    assert np.allclose(out.numpy(), x, atol=1e-10)
+    out_ist = solvers.IST_wrap(_ForwardAdjointOp(A), None, b, 15, 0.5, 0.05)     # numpy in, numpy out
+    assert isinstance(out_ist, np.ndarray)
+
+
 def test_ist_decreases_objective():
     rng = np.random.default_rng(2)
     A = torch.from_numpy((rng.standard_normal((50, 20)) + 1j * rng.standard_normal((50, 20))) / 10)
