@@ -280,3 +280,28 @@ def test_fista_ragged_frames_match_per_frame_oracle():
         ref = SO.fista(_normal64((xs[0][a:b], xs[1][a:b]), shape), rhs[g].astype(np.complex128), 5, 0.5, 1e-2,
                        2, (0, 1))
         assert rel(x[g], ref) < 1e-4
+
+
+# ---------------------------------------------------------------- ADMM (pics/CS_MRI_solvers_func.py:321-333)
+def test_admm_sense_cuda_matches_fp64_admm_on_oracle_operators():
+    from mripy_gb300 import admm
+    rng = np.random.default_rng(60)
+    shape, nc = (32, 32), 3
+    coords = _uniform_coords(rng)
+    S = synth.coil_maps(shape, nc, rng)
+    x = synth.ellipse_phantom(shape[0], rng)
+    y = O.nufft_type2(coords, (x[..., None] * S).astype(np.complex128), shape, eps=EPS_OP)
+    nft = ops.NUFFT2d(shape)
+    nft.set_ktraj(*coords)
+    A = ops.joint2operators(ops.espirit(S), nft)
+    yt = torch.from_numpy(y.astype(np.complex64)).cuda()
+    xr = admm.ADMM_l2Afxnb_l1x(A.forward, A.backward, yt, 4, 0.5, 0.01, 1.0)
+    assert isinstance(xr, torch.Tensor) and xr.is_cuda and xr.shape == shape + (1,)
+
+    def Af(v):
+        return O.nufft_type2(coords, v * S, shape, eps=EPS_OP)
+
+    def AHf(k):
+        return np.sum(np.conj(S) * O.nufft_type1(coords, k, shape, eps=EPS_OP), axis=-1, keepdims=True)
+    ref = admm.ADMM_l2Afxnb_l1x(Af, AHf, y, 4, 0.5, 0.01, 1.0)
+    assert rel(xr, ref) < 1e-3
