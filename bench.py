@@ -23,6 +23,8 @@ replayed from one CUDA graph; value = (samples x coils) / step time.  Also repor
   solver       c2: 20 CG-SENSE iterations; c4: Pipe-Menon dcf + 30 IST iterations with a
                level-4 Haar L1 prox (each iteration one CUDA graph)
   autograd     c5: loss ||A(x; k) - y||^2 and its gradients with respect to image and trajectory
+  --part espirit / haar (c2, c4): ESPIRiT coil maps and the Haar transform / wavelet prox on
+               the workload's coil data, beside their FP64 host restatements
 
 --impl reference times mripy's CPU NUFFT algorithm (the oracle port; mripy itself is
 Python + numba and is not installed on the GPU host) on the same workload.
@@ -604,6 +606,103 @@ def autograd_time(torch, wl, tuning, steps=20):
                         "(type-1) and trajectory gradient (pad, FFT, weight-derivative interp)"}
 
 
+def _centre(shape, n):
+    return tuple(slice(m // 2 - n // 2, m // 2 - n // 2 + n) for m in shape)
+
+
+def espirit_time(torch, wl, reps=5):
+    """ESPIRiT coil maps (espirit/espirit_func.py) from the centre of the workload's fully
+    sampled multi-coil k-space: 2-D 32^2 calibration region, 16^2 window; 3-D 24^3, 8^3.
+    pad_before_espirit 0 (the reference default: eigen step on the calibration grid, maps
+    interpolated by FFT) and, in 2-D, 1 (eigen step on every image pixel).  Beside the GPU
+    time: the FP64 numpy restatement on the host (one run) and the maps' agreement with it;
+    the eigen kernel alone is timed with CUDA events on the full-image case."""
+    from mripy_gb300 import espirit as E
+    from oracle import espirit_oracle as EO
+    d = wl.dim
+    axes = tuple(range(d))
+    ksp = EO.ft_forward(wl.base_image[..., None] * wl.sens, axes)
+    calib, win = (32, (16, 16)) if d == 2 else (24, (8, 8, 8))
+    xcrop = np.ascontiguousarray(ksp[_centre(wl.shape, calib)]).astype(np.complex64)
+    xc = torch.from_numpy(xcrop).cuda()
+    x_shape = wl.shape + (wl.n_coil,)
+    out = {"calibration": [calib] * d, "window": list(win), "coils": wl.n_coil}
+    for pb in ((0, 1) if d == 2 else (0,)):
+        E.espirit_nd(xc, x_shape, hkwin_shape=win, pad_before_espirit=pb)          # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            vg, sg, info = E.espirit_nd(xc, x_shape, hkwin_shape=win, pad_before_espirit=pb, return_info=True)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / reps
+        t1 = time.perf_counter()
+        vr, sr, _ = EO.espirit(xcrop.astype(np.complex128), x_shape, hkwin_shape=win, pad_before_espirit=pb,
+                               return_info=True)
+        s_cpu = time.perf_counter() - t1
+        v = vg.cpu().numpy()
+        s_map = sg.cpu().numpy()
+        keep = sr > 0.05
+        agree = np.abs(np.sum(v * np.conj(vr), axis=-1)) / (np.linalg.norm(v, axis=-1) * np.linalg.norm(vr, axis=-1)
+                                                             + 1e-30)
+        out["pad_before_espirit_%d" % pb] = {
+            "ms_gpu": round(ms, 3), "s_cpu_fp64_port": round(s_cpu, 3), "cpu_cores": 1,
+            "kept_singular_vectors": int(info["nsv"]),
+            "eigen_pixels": int(np.prod(wl.shape)) if pb else calib ** d,
+            "map_agreement_q01": round(float(np.quantile(agree[keep], 0.01)), 6),
+            "eigenvalue_map_rel_err": float("%.2e" % (np.linalg.norm(s_map[keep] - sr[keep]) /
+                                                      np.linalg.norm(sr[keep])))}
+        if pb == 1:
+            # the eigen kernel alone on the same shape: (pixels, kept vectors, coils)
+            nsv = int(info["nsv"])
+            a = torch.randn((int(np.prod(wl.shape)), nsv, wl.n_coil), dtype=torch.complex64, device="cuda")
+            stream = torch.cuda.current_stream()
+            flush_buf = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+            t_k, _ = event_time(torch, lambda: E.espirit_eigen(a), 10, stream, lambda: flush_buf.fill_(1.0))
+            nbytes = a.numel() * 8
+            out["eigen_kernel"] = {"ms": round(t_k, 4), "pixels": int(a.shape[0]), "nsv": nsv, "coils": wl.n_coil,
+                                   "power_iterations": 64, "input_bytes": nbytes,
+                                   "input_GBps": round(nbytes / (t_k * 1e-3) / 1e9, 1)}
+    return out
+
+
+def haar_time(torch, wl, level=4, reps=20):
+    """Level-4 orthonormal Haar transform (mripy's DWTnd('haar') through pywt) over the
+    spatial axes of the workload's image (the SENSE-combined image the IST solver
+    thresholds) and of its coil stack (coils interleaved as the trailing axis): forward,
+    inverse and the fused wavelet-L1 prox, each one kernel, timed with CUDA events (L2
+    flushed between launches) against the measured HBM copy bandwidth; the FP64 numpy
+    restatement on the host beside it."""
+    from mripy_gb300 import plan as P
+    from oracle import solver_oracle as SO
+    axes = tuple(range(wl.dim))
+    stream = torch.cuda.current_stream()
+    flush_buf = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    flush = lambda: flush_buf.fill_(1.0)            # noqa: E731
+    peak, peak_kind = peaks()
+    out = {"level": level, "axes": list(axes), "peak": "%s %.0f GB/s" % (peak_kind, peak)}
+    for case, shape in (("image", wl.shape), ("coil_stack", wl.shape + (wl.n_coil,))):
+        g = torch.Generator(device="cuda").manual_seed(5)
+        x = torch.randn(shape, dtype=torch.complex64, device="cuda", generator=g)
+        c = torch.empty_like(x)
+        y = torch.empty_like(x)
+        nbytes = 2 * x.numel() * 8                   # read + write of the complex64 array
+        res = {"shape": list(shape), "bytes_per_launch": nbytes}
+        for name, fn in (("forward", lambda: P.haar_dwt(x, level, axes, out=c)),
+                         ("inverse", lambda: P.haar_dwt(c, level, axes, inverse=True, out=y)),
+                         ("prox", lambda: P.prox_haar(x, 0.1, level, axes, out=y))):
+            fn()
+            t, _ = event_time(torch, fn, reps, stream, flush)
+            gbs = nbytes / (t * 1e-3) / 1e9
+            res[name] = {"ms": round(t, 4), "GBps": round(gbs, 1), "frac_of_hbm": round(gbs / peak, 3)}
+        xs = x.cpu().numpy().astype(np.complex128)
+        t0 = time.perf_counter()
+        ref = SO.haar_dwt(xs, level, axes)
+        res["cpu_fp64_port_forward_s"] = round(time.perf_counter() - t0, 3)
+        res["forward_rel_err_vs_port"] = float("%.2e" % (np.linalg.norm(c.cpu().numpy() - ref) / np.linalg.norm(ref)))
+        out[case] = res
+    return out
+
+
 def cpu_baseline(wl, reps=1):
     """The FP64 C restatement of mripy's CPU NUFFT (oracle/) on the host cores: fwd + adj
     of group 0.  2-D: every coil, all samples; 3-D: 1 coil and the first 400,000 samples
@@ -667,6 +766,10 @@ def run_solver_only(args, wl):
                           eps=wl.eps, cache_file=args.tune_cache)
     if args.part == "autograd":
         return {"workload": wl.description, "part": "autograd", "autograd": autograd_time(torch, wl, tuning)}
+    if args.part == "espirit":
+        return {"workload": wl.description, "part": "espirit", "espirit": espirit_time(torch, wl)}
+    if args.part == "haar":
+        return {"workload": wl.description, "part": "haar", "haar": haar_time(torch, wl)}
     res = cg_sense_time(torch, wl, coords) if wl.name == "c2" else ist_time(torch, wl, tuning)
     return {"workload": wl.description, "part": "solver", "solver": res}
 
@@ -684,12 +787,14 @@ def main():
     ap.add_argument("--tune-cache", default=None,
                     help="JSON file of autotuner results: read if it holds this workload's key, else "
                          "written; lets a profiler run reuse the tiling of an earlier run")
-    ap.add_argument("--part", default="all", choices=["all", "solver", "autograd"],
+    ap.add_argument("--part", default="all", choices=["all", "solver", "autograd", "espirit", "haar"],
                     help="solver: only the solver timing of c2 (CG-SENSE) or c4 (IST); autograd: only "
-                         "the differentiable step of c5; one JSON line with its figures (for profiling)")
+                         "the differentiable step of c5; espirit: ESPIRiT maps from c2's or c4's coil "
+                         "k-space; haar: the Haar transform and prox on c2's or c4's coil stack; one "
+                         "JSON line with its figures (for profiling)")
     args = ap.parse_args()
     if args.part != "all":
-        ok = {"solver": ("c2", "c4"), "autograd": ("c5",)}[args.part]
+        ok = {"solver": ("c2", "c4"), "autograd": ("c5",), "espirit": ("c2", "c4"), "haar": ("c2", "c4")}[args.part]
         if args.workload not in ok or args.impl != "gb300":
             ap.error("--part %s takes --workload %s with the gb300 arm" % (args.part, " or ".join(ok)))
         from mripy_gb300 import build

@@ -234,10 +234,13 @@ struct HaarGeom {
     int s[3];            // spatial sizes (1 beyond dim), s[dim-1] fastest
     int nt[3];           // tiles per axis = s >> L
     int64_t tiles_img;   // tiles per image
-    int64_t n_img;       // n_outer * n_inner
-    int64_t inner;       // images interleaved element by element (trailing axis)
+    int64_t n_outer;     // images (each with `inner` interleaved channels)
+    int64_t inner;       // channels interleaved element by element (trailing axis)
     int64_t P;           // pixels per image
-    int tpb_log;         // log2 tiles per thread block
+    int cpb;             // channels per unit (a power of two)
+    int64_t chunks;      // channel chunks per image = ceil(inner / cpb)
+    int64_t n_units;     // units = (image, tile, chunk), chunk fastest
+    int upb_log;         // log2 units per thread block
 };
 int haar_geom(int dim, const int32_t *shape, int level, int64_t n_outer, int64_t n_inner, HaarGeom &h);
 // one IST/FISTA step on Haar tiles (pics/CS_MRI_solvers_func.py:75-86, 207-224):

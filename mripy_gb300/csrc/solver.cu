@@ -13,9 +13,10 @@
 //    (pics/proximal_func.py:46-52, soft threshold :20-24: v / (|v| + 1e-6) * max(|v| - th, 0))
 //    with T the orthonormal level-L Haar transform (DWTnd, pics/operators_class.py:394-416,
 //    wavelet 'haar'), and FISTA's momentum y = x + (t_k - 1)/t_{k+1} (x - x_pre).  A level-L
-//    Haar transform maps each tile of 2^L cells per axis onto itself, so one block loads
-//    whole tiles into shared memory, runs L forward levels, thresholds, runs L inverse
-//    levels and writes x: one read and one write of each vector per step.
+//    Haar transform maps each tile of 2^L cells per axis onto itself, so one block takes
+//    whole tiles: level 1 runs in registers on 2^DIM cubes read straight from the vectors
+//    (its thresholded bands stay there), levels 2..L on the approximations in shared
+//    memory, then the inverse back out: one read and one write of each vector per step.
 //  * gbn_haar_dwt: the same tile transform, writing (or reading) the coefficients in the
 //    layout of pywt.coeffs_to_array (approximation block first along every axis, then the
 //    detail blocks of the coarsest level, ..., the finest level's last).
@@ -29,8 +30,8 @@ namespace {
 
 constexpr int kVecThreads = 256;
 constexpr int kHaarThreads = 256;
-constexpr int kHaarMaxElems = 4096;     // complex cells per block (32 KB of shared memory)
-constexpr int kHaarPairs = kHaarMaxElems / 2 / kHaarThreads;  // butterflies per thread per pass
+constexpr int kHaarMaxElems = 4096;     // complex elements per block (32 KB of shared memory)
+constexpr int kHaarBlockElems = 2048;   // elements per block when tiles are smaller than that
 
 int vec_blocks(int64_t n) {
     const int64_t b = (n + kVecThreads - 1) / kVecThreads;
@@ -242,135 +243,99 @@ __global__ void __launch_bounds__(kVecThreads) k_dcf_scale(const float2 *__restr
 }
 
 // ---- Haar tiles ------------------------------------------------------------------------
-// Element e of a block: tile (e >> (DIM*L)) of the block, in-tile cell c with c[DIM-1]
-// fastest, L bits per axis.  In-tile coefficients after the forward levels sit where
-// pywt's layout would put them for an image of one tile: level l acts on the leading
-// (T >> l)^DIM cube, approximations in the lower half of every axis.
-// A tile decoded once per block: the base element of its image and its tile coordinates
-// along each axis (21 bits each), so the per-element addresses need no division.
+// A level-L Haar transform maps each tile of T = 2^L cells per axis onto itself.  Blocks
+// take whole units, a unit being (image, tile, channel chunk) with the chunk fastest, so the
+// chunks of one tile run side by side and share the cache lines of interleaved channels.
+//
+// Inside a block the transform runs in place on 2^DIM cubes: level l combines the cells
+// base + h*bits (h = 2^(l-1), base a multiple of 2h along every axis) into the approximation,
+// kept at base, and the 2^DIM - 1 detail bands at the other corners.  Level 1 runs in
+// registers on cubes loaded straight from the image (the prox keeps its thresholded details
+// there); levels 2..L run on the approximation lattice in shared memory, one barrier each.
+// Shared memory holds a unit's cells as [cell][channel], cell = in-tile (x, y, z) with L bits
+// per axis and the last axis fastest.
 struct TileRef {
-    int64_t img_base;
-    int64_t tcp;
+    int64_t base;  // element of (image, channel chunk start, pixel 0)
+    int64_t tcp;   // tile coordinates, 21 bits per axis
+    int nch;       // channels of the chunk that exist (<= cpb)
 };
-constexpr int kHaarMaxTiles = 512;  // tiles per block (blocks hold at least 512 cells)
+constexpr int kHaarMaxUnits = 512;
 
 template <int DIM>
-__device__ __forceinline__ TileRef haar_tile(const HaarGeom &h, int64_t tile) {
-    const int64_t img = tile / h.tiles_img;
-    int64_t tr = tile - img * h.tiles_img;
-    int64_t packed = 0;
+__device__ __forceinline__ TileRef haar_unit(const HaarGeom &h, int64_t u) {
+    const int64_t chunk = u % h.chunks;
+    int64_t r = u / h.chunks;
+    const int64_t tile = r % h.tiles_img;
+    const int64_t outer = r / h.tiles_img;
+    int64_t tr = tile, packed = 0;
 #pragma unroll
     for (int d = DIM - 1; d >= 0; --d) {
         packed |= (tr % h.nt[d]) << (21 * d);
         tr /= h.nt[d];
     }
-    const int64_t outer = img / h.inner;
-    return TileRef{outer * h.P * h.inner + (img - outer * h.inner), packed};
+    const int64_t c0 = chunk * h.cpb;
+    const int64_t left = h.inner - c0;
+    return TileRef{outer * h.P * h.inner + c0, packed, (int)(left < h.cpb ? left : h.cpb)};
 }
 
 __device__ __forceinline__ int tile_coord(int64_t packed, int d) { return (int)((packed >> (21 * d)) & 0x1FFFFF); }
 
-// image element of in-tile cell `el` (c[DIM-1] fastest, L bits per axis)
+// image element of in-tile cell (coordinates c[]) and channel ch of a unit
 template <int DIM>
-__device__ __forceinline__ int64_t haar_pix_addr(const HaarGeom &h, const TileRef &t, int el) {
+__device__ __forceinline__ int64_t haar_pix_addr(const HaarGeom &h, const TileRef &t, const int *c, int ch) {
     const int T = 1 << h.L;
     int64_t pix = 0;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        const int c = (el >> (h.L * (DIM - 1 - d))) & (T - 1);
-        pix = pix * h.s[d] + (int64_t)tile_coord(t.tcp, d) * T + c;
-    }
-    return t.img_base + pix * h.inner;
+    for (int d = 0; d < DIM; ++d) pix = pix * h.s[d] + (int64_t)tile_coord(t.tcp, d) * T + c[d];
+    return t.base + pix * h.inner + ch;
 }
 
-// position of in-tile coefficient `el` in pywt.coeffs_to_array's layout
+// element of in-tile cell c[] (in-place layout) in pywt.coeffs_to_array's layout: the cell
+// belongs to level l = the lowest level at which one of its coordinates is an odd multiple
+// of 2^(l-1) (all coordinates 0: the level-L approximation), band bit b_d = (c_d >> (l-1)) & 1,
+// position within the band c_d >> l; band (b_0..) of level l starts at (s_d >> l) * b_d
 template <int DIM>
-__device__ __forceinline__ int64_t haar_coeff_addr(const HaarGeom &h, const TileRef &t, int el) {
-    const int T = 1 << h.L;
-    int cell[DIM];
-    int m = 0;
+__device__ __forceinline__ int64_t haar_coeff_addr(const HaarGeom &h, const TileRef &t, const int *c, int ch) {
+    int l = h.L;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        cell[d] = (el >> (h.L * (DIM - 1 - d))) & (T - 1);
-        m = max(m, cell[d]);
-    }
-    // band level j: T >> j <= m < T >> (j - 1); m = 0 is the level-L approximation
-    const int j = m == 0 ? h.L : h.L - (31 - __clz(m));
-    const int hj = 1 << (h.L - j);
+    for (int d = 0; d < DIM; ++d)
+        if (c[d]) l = min(l, __ffs(c[d]));
     int64_t pix = 0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        const int tc = tile_coord(t.tcp, d);
-        const int g = cell[d] >= hj ? (h.s[d] >> j) + tc * hj + (cell[d] - hj) : tc * hj + cell[d];
+        const int b = (c[d] >> (l - 1)) & 1;
+        const int g = (b ? (h.s[d] >> l) : 0) + tile_coord(t.tcp, d) * (1 << (h.L - l)) + (c[d] >> l);
         pix = pix * h.s[d] + g;
     }
-    return t.img_base + pix * h.inner;
+    return t.base + pix * h.inner + ch;
 }
 
-// One butterfly pass along axis `ax` over the leading n^DIM cube of every tile in the
-// block: forward  (c_ax = 2k, 2k+1) -> (k, n/2 + k) as ((e + o)/sqrt2, (e - o)/sqrt2);
-// inverse the transpose.  Pairs are read into registers, then written after a barrier.
-template <int DIM, bool INV>
-__device__ void haar_pass(float2 *sm, int L, int ln, int ax, int ntiles_blk) {
-    const int per_tile_log = DIM * ln - 1;
-    const int total = ntiles_blk << per_tile_log;
+// in-tile cell coordinates of element e of a unit's cells (last axis fastest, L bits each)
+template <int DIM>
+__device__ __forceinline__ void cell_coords(int cell, int L, int *c) {
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; --d) {
+        c[d] = cell & ((1 << L) - 1);
+        cell >>= L;
+    }
+}
+
+// 2^DIM-point Haar butterflies on v[q], q's bit (DIM-1-d) selecting the upper cell along
+// axis d; forward and inverse are the same orthonormal map, applied axis by axis (0 first)
+template <int DIM>
+__device__ __forceinline__ void cube_butterfly(float2 *v) {
     const float r2 = 0.70710678118654752440f;
-    float2 va[kHaarPairs], vb[kHaarPairs];
-    int ia[kHaarPairs], ib[kHaarPairs];
 #pragma unroll
-    for (int j = 0; j < kHaarPairs; ++j) {
-        const int q = threadIdx.x + j * kHaarThreads;
-        ia[j] = -1;
-        if (q >= total) continue;
-        const int tl = q >> per_tile_log;
-        int r = q & ((1 << per_tile_log) - 1);
-        int k = 0, base = tl << (DIM * L);
+    for (int d = 0; d < DIM; ++d) {
+        const int bit = 1 << (DIM - 1 - d);
 #pragma unroll
-        for (int d = DIM - 1; d >= 0; --d) {
-            const int eb = d == ax ? ln - 1 : ln;
-            const int cd = r & ((1 << eb) - 1);
-            r >>= eb;
-            if (d == ax)
-                k = cd;
-            else
-                base += cd << (L * (DIM - 1 - d));
-        }
-        const int stride_ax = 1 << (L * (DIM - 1 - ax));
-        const int lo = base + (2 * k) * stride_ax, hi = base + (2 * k + 1) * stride_ax;
-        const int a_pos = base + k * stride_ax, d_pos = base + ((1 << (ln - 1)) + k) * stride_ax;
-        if (!INV) {
-            const float2 e = sm[lo], o = sm[hi];
-            va[j] = make_float2((e.x + o.x) * r2, (e.y + o.y) * r2);
-            vb[j] = make_float2((e.x - o.x) * r2, (e.y - o.y) * r2);
-            ia[j] = a_pos;
-            ib[j] = d_pos;
-        } else {
-            const float2 a = sm[a_pos], d = sm[d_pos];
-            va[j] = make_float2((a.x + d.x) * r2, (a.y + d.y) * r2);
-            vb[j] = make_float2((a.x - d.x) * r2, (a.y - d.y) * r2);
-            ia[j] = lo;
-            ib[j] = hi;
+        for (int q = 0; q < (1 << DIM); ++q) {
+            if (q & bit) continue;
+            const float2 e = v[q], o = v[q | bit];
+            v[q] = make_float2((e.x + o.x) * r2, (e.y + o.y) * r2);
+            v[q | bit] = make_float2((e.x - o.x) * r2, (e.y - o.y) * r2);
         }
     }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < kHaarPairs; ++j) {
-        if (ia[j] < 0) continue;
-        sm[ia[j]] = va[j];
-        sm[ib[j]] = vb[j];
-    }
-    __syncthreads();
-}
-
-template <int DIM>
-__device__ void haar_forward(float2 *sm, int L, int ntiles_blk) {
-    for (int l = 0; l < L; ++l)
-        for (int ax = 0; ax < DIM; ++ax) haar_pass<DIM, false>(sm, L, L - l, ax, ntiles_blk);
-}
-template <int DIM>
-__device__ void haar_inverse(float2 *sm, int L, int ntiles_blk) {
-    for (int l = L - 1; l >= 0; --l)
-        for (int ax = 0; ax < DIM; ++ax) haar_pass<DIM, true>(sm, L, L - l, ax, ntiles_blk);
 }
 
 __device__ __forceinline__ float2 soft_thresh(float2 v, float th) {
@@ -379,16 +344,114 @@ __device__ __forceinline__ float2 soft_thresh(float2 v, float th) {
     return make_float2(v.x * s, v.y * s);
 }
 
+// Work item w of level l >= 1 in a block: channel (fastest), cube, unit.  Its cube corner
+// cells are corner[d] = 2h * cube_d + h * bit_d with h = 2^(l-1).
+struct CubeItem {
+    int unit, ch;
+    int corner[3];
+};
+template <int DIM>
+__device__ __forceinline__ CubeItem cube_item(int w, int L, int l, int cpb_log) {
+    CubeItem it;
+    it.ch = w & ((1 << cpb_log) - 1);
+    int r = w >> cpb_log;
+    const int cb = L - l;  // bits per axis of the level's cube index
+    const int cubes_log = DIM * cb;
+    it.unit = r >> cubes_log;
+    int cube = r & ((1 << cubes_log) - 1);
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; --d) {
+        it.corner[d] = (cube & ((1 << cb) - 1)) << l;
+        cube >>= cb;
+    }
+    for (int d = DIM; d < 3; ++d) it.corner[d] = 0;
+    return it;
+}
+
+// shared-memory element of cell c[] (plus offset h * bits(q)) of a unit, channel ch
+template <int DIM>
+__device__ __forceinline__ int sm_index(const CubeItem &it, int q, int h, int L, int cpb_log) {
+    int cell = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) cell = (cell << L) | (it.corner[d] + (((q >> (DIM - 1 - d)) & 1) ? h : 0));
+    return (((it.unit << (DIM * L)) | cell) << cpb_log) | it.ch;
+}
+
+// levels 2..L (forward) or L..2 (inverse) on the approximation lattice in shared memory;
+// with th >= 0 the forward pass soft-thresholds each level's details, and the level-L
+// approximation, as they are produced
+template <int DIM, bool INV>
+__device__ void haar_levels_smem(float2 *sm, int L, int cpb_log, int n_units, float th) {
+    for (int step = 0; step < L - 1; ++step) {
+        const int l = INV ? L - step : 2 + step;
+        const int h = 1 << (l - 1);
+        const int items = n_units << (DIM * (L - l) + cpb_log);
+        for (int w = threadIdx.x; w < items; w += kHaarThreads) {
+            const CubeItem it = cube_item<DIM>(w, L, l, cpb_log);
+            float2 v[1 << DIM];
+            int idx[1 << DIM];
+#pragma unroll
+            for (int q = 0; q < (1 << DIM); ++q) {
+                idx[q] = sm_index<DIM>(it, q, h, L, cpb_log);
+                v[q] = sm[idx[q]];
+            }
+            cube_butterfly<DIM>(v);
+            if (!INV && th >= 0.f) {
+#pragma unroll
+                for (int q = 0; q < (1 << DIM); ++q)
+                    if (q || l == L) v[q] = soft_thresh(v[q], th);
+            }
+#pragma unroll
+            for (int q = 0; q < (1 << DIM); ++q) sm[idx[q]] = v[q];
+        }
+        __syncthreads();
+    }
+}
+
+constexpr int kHaarCubes = 16;  // level-1 cubes per thread, times 2^DIM (4096-cell blocks, 256 threads)
+
+// first unit of the block, the number of units it holds, and their decoded references
+template <int DIM>
+__device__ __forceinline__ int haar_block_units(const HaarGeom &h, TileRef *units) {
+    const int64_t u0 = (int64_t)blockIdx.x << h.upb_log;
+    const int64_t left = h.n_units - u0;
+    const int nu = left < ((int64_t)1 << h.upb_log) ? (int)left : (1 << h.upb_log);
+    for (int t = threadIdx.x; t < nu; t += kHaarThreads) units[t] = haar_unit<DIM>(h, u0 + t);
+    return nu;
+}
+
+// global elements of a level-1 cube's 2^DIM cells
+template <int DIM>
+__device__ __forceinline__ void cube_addrs(const HaarGeom &h, const TileRef &t, const CubeItem &it, int64_t *g) {
+    int c[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) c[d] = it.corner[d];
+    const int64_t g0 = haar_pix_addr<DIM>(h, t, c, it.ch);
+    int64_t stride = h.inner;
+    int64_t off[3];
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; --d) {
+        off[d] = stride;
+        stride *= h.s[d];
+    }
+#pragma unroll
+    for (int q = 0; q < (1 << DIM); ++q) {
+        int64_t a = g0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            if ((q >> (DIM - 1 - d)) & 1) a += off[d];
+        g[q] = a;
+    }
+}
+
 template <int DIM, bool MOM>
 __global__ void __launch_bounds__(kHaarThreads) k_haar_step(HaarStepArgs a) {
+    constexpr int NQ = 1 << DIM;
+    constexpr int CPT = kHaarCubes >> DIM;
     extern __shared__ float2 sm[];
     const HaarGeom &h = a.h;
-    const int tile_log = DIM * h.L;
-    const int blk_elems = 1 << (tile_log + h.tpb_log);
-    const int64_t ntiles = h.tiles_img * h.n_img;
-    const int64_t tile0 = (int64_t)blockIdx.x << h.tpb_log;
-    const int64_t left = ntiles - tile0;
-    const int ntiles_blk = left < ((int64_t)1 << h.tpb_log) ? (int)left : (1 << h.tpb_log);
+    const int L = h.L, cpb_log = __ffs(h.cpb) - 1;
+    __shared__ TileRef units[kHaarMaxUnits];
     __shared__ float c_mom;
     __shared__ double t_next;
     if (MOM && threadIdx.x == 0) {
@@ -397,43 +460,82 @@ __global__ void __launch_bounds__(kHaarThreads) k_haar_step(HaarStepArgs a) {
         t_next = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
         c_mom = (float)((t - 1.0) / t_next);
     }
-    __shared__ TileRef tiles[kHaarMaxTiles];
-    for (int t = threadIdx.x; t < ntiles_blk; t += kHaarThreads) tiles[t] = haar_tile<DIM>(h, tile0 + t);
+    const int nu = haar_block_units<DIM>(h, units);
     __syncthreads();
-    const int el_mask = (1 << tile_log) - 1;
-    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
-        const int tl = e >> tile_log;
-        if (tl >= ntiles_blk) {
-            sm[e] = make_float2(0.f, 0.f);
-            continue;
-        }
-        const int64_t g = haar_pix_addr<DIM>(h, tiles[tl], e & el_mask);
+    const float cm = MOM ? c_mom : 0.f;
+    // one element: gradient update, then (after the transform) the output with momentum
+    auto load = [&](int64_t g) {
         float2 v = a.acc[g];
         if (a.q) {
-            const float2 q = a.q[g], b = a.rhs[g];
-            v.x -= a.step * (q.x - b.x);
-            v.y -= a.step * (q.y - b.y);
+            const float2 qv = a.q[g], b = a.rhs[g];
+            v.x -= a.step * (qv.x - b.x);
+            v.y -= a.step * (qv.y - b.y);
             a.acc[g] = v;
         }
-        sm[e] = v;
-    }
-    __syncthreads();
-    haar_forward<DIM>(sm, h.L, ntiles_blk);
-    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) sm[e] = soft_thresh(sm[e], a.th);
-    __syncthreads();
-    haar_inverse<DIM>(sm, h.L, ntiles_blk);
-    const float c = MOM ? c_mom : 0.f;
-    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
-        const int tl = e >> tile_log;
-        if (tl >= ntiles_blk) continue;
-        const int64_t g = haar_pix_addr<DIM>(h, tiles[tl], e & el_mask);
-        const float2 x = sm[e];
+        return v;
+    };
+    auto store = [&](int64_t g, float2 x) {
         if (MOM) {
             const float2 xp = a.x_pre[g];
-            a.y[g] = make_float2(x.x + c * (x.x - xp.x), x.y + c * (x.y - xp.y));
+            a.y[g] = make_float2(x.x + cm * (x.x - xp.x), x.y + cm * (x.y - xp.y));
             a.x_pre[g] = x;
         } else {
             a.x_out[g] = x;
+        }
+    };
+    if (L == 0) {
+        // plain soft threshold, element by element
+        const int n = nu << cpb_log;
+        for (int e = threadIdx.x; e < n; e += kHaarThreads) {
+            const TileRef &t = units[e >> cpb_log];
+            const int ch = e & (h.cpb - 1);
+            if (ch >= t.nch) continue;
+            const int c[3] = {0, 0, 0};
+            const int64_t g = haar_pix_addr<DIM>(h, t, c, ch);
+            store(g, soft_thresh(load(g), a.th));
+        }
+    } else {
+        const int items = nu << (DIM * (L - 1) + cpb_log);
+        float2 det[CPT][NQ];  // level-1 bands, thresholded (the approximation too when L == 1)
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+            const int w = threadIdx.x + j * kHaarThreads;
+            if (w >= items) continue;
+            const CubeItem it = cube_item<DIM>(w, L, 1, cpb_log);
+            const TileRef &t = units[it.unit];
+            const bool ok = it.ch < t.nch;
+            int64_t g[NQ];
+            cube_addrs<DIM>(h, t, it, g);
+            float2 v[NQ];
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) v[q] = ok ? load(g[q]) : make_float2(0.f, 0.f);
+            cube_butterfly<DIM>(v);
+#pragma unroll
+            for (int q = 1; q < NQ; ++q) det[j][q] = soft_thresh(v[q], a.th);
+            if (L == 1)
+                det[j][0] = soft_thresh(v[0], a.th);
+            else
+                sm[sm_index<DIM>(it, 0, 1, L, cpb_log)] = v[0];
+        }
+        __syncthreads();
+        haar_levels_smem<DIM, false>(sm, L, cpb_log, nu, a.th);
+        haar_levels_smem<DIM, true>(sm, L, cpb_log, nu, -1.f);
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+            const int w = threadIdx.x + j * kHaarThreads;
+            if (w >= items) continue;
+            const CubeItem it = cube_item<DIM>(w, L, 1, cpb_log);
+            const TileRef &t = units[it.unit];
+            if (it.ch >= t.nch) continue;
+            float2 v[NQ];
+            v[0] = L == 1 ? det[j][0] : sm[sm_index<DIM>(it, 0, 1, L, cpb_log)];
+#pragma unroll
+            for (int q = 1; q < NQ; ++q) v[q] = det[j][q];
+            cube_butterfly<DIM>(v);
+            int64_t g[NQ];
+            cube_addrs<DIM>(h, t, it, g);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) store(g[q], v[q]);
         }
     }
     if (MOM) {
@@ -452,46 +554,82 @@ __global__ void __launch_bounds__(kHaarThreads) k_haar_step(HaarStepArgs a) {
 template <int DIM, bool INV>
 __global__ void __launch_bounds__(kHaarThreads) k_haar_dwt(HaarGeom h, const float2 *__restrict__ in,
                                                            float2 *__restrict__ out) {
+    constexpr int NQ = 1 << DIM;
     extern __shared__ float2 sm[];
-    const int tile_log = DIM * h.L;
-    const int blk_elems = 1 << (tile_log + h.tpb_log);
-    const int64_t ntiles = h.tiles_img * h.n_img;
-    const int64_t tile0 = (int64_t)blockIdx.x << h.tpb_log;
-    const int64_t left = ntiles - tile0;
-    const int ntiles_blk = left < ((int64_t)1 << h.tpb_log) ? (int)left : (1 << h.tpb_log);
-    __shared__ TileRef tiles[kHaarMaxTiles];
-    for (int t = threadIdx.x; t < ntiles_blk; t += kHaarThreads) tiles[t] = haar_tile<DIM>(h, tile0 + t);
+    const int L = h.L, cpb_log = __ffs(h.cpb) - 1;
+    __shared__ TileRef units[kHaarMaxUnits];
+    const int nu = haar_block_units<DIM>(h, units);
     __syncthreads();
-    const int el_mask = (1 << tile_log) - 1;
-    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
-        const int tl = e >> tile_log;
-        if (tl >= ntiles_blk) {
-            sm[e] = make_float2(0.f, 0.f);
-            continue;
+    const int cell_log = DIM * L;
+    const int n_el = nu << (cell_log + cpb_log);
+    if (L == 0) {
+        for (int e = threadIdx.x; e < n_el; e += kHaarThreads) {
+            const TileRef &t = units[e >> cpb_log];
+            const int ch = e & (h.cpb - 1);
+            if (ch >= t.nch) continue;
+            const int c[3] = {0, 0, 0};
+            const int64_t g = haar_pix_addr<DIM>(h, t, c, ch);
+            out[g] = in[g];
         }
-        const int64_t g = INV ? haar_coeff_addr<DIM>(h, tiles[tl], e & el_mask)
-                              : haar_pix_addr<DIM>(h, tiles[tl], e & el_mask);
-        sm[e] = in[g];
+        return;
     }
-    __syncthreads();
-    if (INV)
-        haar_inverse<DIM>(sm, h.L, ntiles_blk);
-    else
-        haar_forward<DIM>(sm, h.L, ntiles_blk);
-    for (int e = threadIdx.x; e < blk_elems; e += kHaarThreads) {
-        const int tl = e >> tile_log;
-        if (tl >= ntiles_blk) continue;
-        const int64_t g = INV ? haar_pix_addr<DIM>(h, tiles[tl], e & el_mask)
-                              : haar_coeff_addr<DIM>(h, tiles[tl], e & el_mask);
-        out[g] = sm[e];
+    const int items = nu << (DIM * (L - 1) + cpb_log);
+    if (!INV) {
+        for (int w = threadIdx.x; w < items; w += kHaarThreads) {
+            const CubeItem it = cube_item<DIM>(w, L, 1, cpb_log);
+            const TileRef &t = units[it.unit];
+            const bool ok = it.ch < t.nch;
+            int64_t g[NQ];
+            cube_addrs<DIM>(h, t, it, g);
+            float2 v[NQ];
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) v[q] = ok ? in[g[q]] : make_float2(0.f, 0.f);
+            cube_butterfly<DIM>(v);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) sm[sm_index<DIM>(it, q, 1, L, cpb_log)] = v[q];
+        }
+        __syncthreads();
+        haar_levels_smem<DIM, false>(sm, L, cpb_log, nu, -1.f);
+        for (int e = threadIdx.x; e < n_el; e += kHaarThreads) {
+            const TileRef &t = units[e >> (cell_log + cpb_log)];
+            const int ch = e & (h.cpb - 1);
+            if (ch >= t.nch) continue;
+            int c[3];
+            cell_coords<DIM>((e >> cpb_log) & ((1 << cell_log) - 1), L, c);
+            out[haar_coeff_addr<DIM>(h, t, c, ch)] = sm[e];
+        }
+    } else {
+        for (int e = threadIdx.x; e < n_el; e += kHaarThreads) {
+            const TileRef &t = units[e >> (cell_log + cpb_log)];
+            const int ch = e & (h.cpb - 1);
+            float2 v = make_float2(0.f, 0.f);
+            if (ch < t.nch) {
+                int c[3];
+                cell_coords<DIM>((e >> cpb_log) & ((1 << cell_log) - 1), L, c);
+                v = in[haar_coeff_addr<DIM>(h, t, c, ch)];
+            }
+            sm[e] = v;
+        }
+        __syncthreads();
+        haar_levels_smem<DIM, true>(sm, L, cpb_log, nu, -1.f);
+        for (int w = threadIdx.x; w < items; w += kHaarThreads) {
+            const CubeItem it = cube_item<DIM>(w, L, 1, cpb_log);
+            const TileRef &t = units[it.unit];
+            if (it.ch >= t.nch) continue;
+            float2 v[NQ];
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) v[q] = sm[sm_index<DIM>(it, q, 1, L, cpb_log)];
+            cube_butterfly<DIM>(v);
+            int64_t g[NQ];
+            cube_addrs<DIM>(h, t, it, g);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) out[g[q]] = v[q];
+        }
     }
 }
 
-int64_t haar_blocks(const HaarGeom &h) {
-    const int64_t ntiles = h.tiles_img * h.n_img;
-    return (ntiles + ((int64_t)1 << h.tpb_log) - 1) >> h.tpb_log;
-}
-size_t haar_smem(const HaarGeom &h) { return sizeof(float2) << (h.dim * h.L + h.tpb_log); }
+int64_t haar_blocks(const HaarGeom &h) { return (h.n_units + ((int64_t)1 << h.upb_log) - 1) >> h.upb_log; }
+size_t haar_smem(const HaarGeom &h) { return (sizeof(float2) * h.cpb) << (h.dim * h.L + h.upb_log); }
 
 }  // namespace
 
@@ -516,11 +654,17 @@ int haar_geom(int dim, const int32_t *shape, int level, int64_t n_outer, int64_t
         h.tiles_img *= h.nt[d];
     }
     h.inner = n_inner;
-    h.n_img = n_outer * n_inner;
-    // tiles per block: at least 512 cells per block (so at most kHaarMaxTiles tiles), at most 4096
-    int tpb_log = 0;
-    while (((dim * level) + tpb_log) < 9) ++tpb_log;
-    h.tpb_log = tpb_log;
+    h.n_outer = n_outer;
+    // channels per unit: interleaved channels of one tile side by side, within 4096 elements
+    const int64_t cells = (int64_t)1 << (dim * level);
+    h.cpb = 1;
+    while (h.cpb * 2 <= n_inner && cells * h.cpb * 2 <= kHaarMaxElems) h.cpb *= 2;
+    h.chunks = (n_inner + h.cpb - 1) / h.cpb;
+    h.n_units = n_outer * h.tiles_img * h.chunks;
+    // units per block: up to 2048 elements (one unit when a unit is larger)
+    int upb_log = 0;
+    while (((cells * h.cpb) << (upb_log + 1)) <= kHaarBlockElems && (1 << (upb_log + 1)) <= kHaarMaxUnits) ++upb_log;
+    h.upb_log = upb_log;
     if (haar_blocks(h) > 0x7fffffff) return record_error(GBN_ERR_CAPACITY, "Haar transform: too many tiles");
     return GBN_OK;
 }

@@ -375,11 +375,13 @@ def test_tma_planes_3d_match_thread_staging(nc, icg, tile):
 @pytest.mark.parametrize("dim", [2, 3])
 def test_host_entry_points_pinned_and_pageable(dim):
     """gbn_type{1,2,21}_host give the device path's results whether the caller's arrays are
-    pageable (staged copies) or pinned (read and written by the kernels directly)."""
+    pageable (staged copies), pinned (read and written by the kernels directly, the samples
+    a spread gathers copied in bulk) or pinned at an 8-byte offset from a 16-byte boundary;
+    the dcf's length is not a multiple of 16 bytes."""
     import ctypes
     from mripy_gb300 import _native as N
     rng = np.random.default_rng(25)
-    shape, nc, M = ((64, 48), 4, 6000) if dim == 2 else ((20, 18, 16), 4, 5000)
+    shape, nc, M = ((64, 48), 4, 6001) if dim == 2 else ((20, 18, 16), 4, 5001)
     xs = rng.uniform(-np.pi, np.pi, (dim, M))
     xs[:, :2000] *= 0.1                                          # split tiles (atomic flush)
     p = NufftPlan(dim, shape, n_coil=nc, eps=5e-6, max_nspread=6 if dim == 3 else None)
@@ -393,8 +395,16 @@ def test_host_entry_points_pinned_and_pageable(dim):
     lib = N.lib()
     sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     vp = lambda t: ctypes.c_void_p(t.data_ptr())
-    for pinned in (False, True):
-        pin = (lambda t: t.pin_memory()) if pinned else (lambda t: t)
+    def pin_offset(t):           # pinned, starting 8 bytes past a 16-byte boundary
+        flat = t.reshape(-1).view(torch.uint8)
+        buf = torch.empty(flat.numel() + 8, dtype=torch.uint8).pin_memory()
+        assert buf.data_ptr() % 16 == 0
+        out = buf[8:].view(t.dtype).reshape(t.shape)
+        out.copy_(t)
+        return out
+
+    for pinned in (False, True, "offset"):
+        pin = {False: (lambda t: t), True: (lambda t: t.pin_memory()), "offset": pin_offset}[pinned]
         h_img, h_c = pin(torch.from_numpy(img)), pin(torch.from_numpy(c))
         h_dcf = pin(torch.from_numpy(dcf))
         o_k = pin(torch.empty((M, nc), dtype=torch.complex64))
