@@ -445,7 +445,7 @@ __device__ __forceinline__ void cube_addrs(const HaarGeom &h, const TileRef &t, 
 }
 
 template <int DIM, bool MOM>
-__global__ void __launch_bounds__(kHaarThreads) k_haar_step(HaarStepArgs a) {
+__global__ void __launch_bounds__(kHaarThreads, 4) k_haar_step(HaarStepArgs a) {
     constexpr int NQ = 1 << DIM;
     constexpr int CPT = kHaarCubes >> DIM;
     extern __shared__ float2 sm[];
