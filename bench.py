@@ -229,6 +229,33 @@ def algorithmic_bytes(M, n_coil, dim, grid_cells, n_inst):
     return 8 * M * n_coil + 4 * dim * M + 8 * grid_cells * n_inst
 
 
+def stencil_footprint(coords, offsets, nf, ns):
+    """Grid cells inside at least one sample's stencil, summed over trajectory groups: the
+    cells an interp must read at least once.  A sample at x (radians) has its first tap at
+    ((1 + floor((x mod 2 pi) / h)) - ns) mod nf, h = 2 pi / nf, and W = 2 ns taps per axis,
+    as the prep kernel places it."""
+    W = 2 * ns
+    total = 0
+    for g in range(len(offsets) - 1):
+        a, b = int(offsets[g]), int(offsets[g + 1])
+        if b <= a:
+            continue
+        idx = []
+        for d, x in enumerate(coords):
+            h = 2 * np.pi / nf[d]
+            m = 1 + np.floor(np.mod(np.asarray(x[a:b], dtype=np.float64), 2 * np.pi) / h).astype(np.int64)
+            idx.append((m - ns) % nf[d])
+        occ = np.zeros(tuple(nf), dtype=bool)
+        occ[tuple(idx)] = True
+        for d in range(len(nf)):
+            cov = occ.copy()
+            for sft in range(1, W):
+                cov |= np.roll(occ, sft, axis=d)
+            occ = cov
+        total += int(np.count_nonzero(occ))
+    return total
+
+
 def flops(M, n_coil, W, dim):
     T = W ** dim
     return 4 * T * M * n_coil + T * M
@@ -377,6 +404,15 @@ def run_gpu(args, wl):
                                           else "of fallback 6.8 TB/s"),
                           "algorithmic_bytes_per_launch": bytes_dir,
                           "fp32_tflops_achieved": round(fl / (t_dom * 1e-3) / 1e12, 2)}
+    # interp bytes counting only the grid cells some stencil reaches (the spread writes the
+    # whole grid, so its bytes stay on the full grid)
+    fp_cells = stencil_footprint(wl.coords, wl.offsets, info["nf"], info["nspread"])
+    interp_bytes_fp = 8 * M * n_coil + 4 * wl.dim * M + 8 * fp_cells * n_coil
+    result["roofline"]["interp_footprint"] = {
+        "cells_touched": fp_cells, "grid_cells": G * wl.n_traj, "frac_of_grid": round(fp_cells / (G * wl.n_traj), 4),
+        "interp_bytes_footprint": interp_bytes_fp, "interp_bytes_full_grid": bytes_dir,
+        "interp_gbs_footprint": round(interp_bytes_fp / (t_interp * 1e-3) / 1e9, 1),
+        "interp_gbs_full_grid": round(bytes_dir / (t_interp * 1e-3) / 1e9, 1)}
     # the stencil kernels are bound by arithmetic (spread) or shared-memory reads (interp)
     # rather than HBM: the binding resource is the largest of the three demand/peak times
     fp32_peak = fp32_peak_tflops()

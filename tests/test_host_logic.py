@@ -172,3 +172,16 @@ def test_two_rank_gloo_timing_reduction():
         assert p.exitcode == 0
     assert [o[1] for o in out] == [15.0, 15.0]   # every rank sees the max step time
     assert [o[2] for o in out] == [2000, 2000]   # weak scaling: whole-job units = world * per-replica
+
+
+def test_stencil_footprint_counts_cells_once():
+    import bench
+    nf, ns = (32, 32), 3
+    one = bench.stencil_footprint([np.array([0.1]), np.array([6.2])], [0, 1], nf, ns)
+    assert one == (2 * ns) ** 2                       # a stencil across the grid's edge wraps
+    apart = bench.stencil_footprint([np.array([0.1, 3.0]), np.array([0.1, 3.0])], [0, 2], nf, ns)
+    assert apart == 2 * (2 * ns) ** 2
+    same = bench.stencil_footprint([np.array([0.1, 0.1]), np.array([0.1, 0.1])], [0, 2], nf, ns)
+    assert same == (2 * ns) ** 2                      # overlapping stencils count once
+    groups = bench.stencil_footprint([np.array([0.1, 0.1]), np.array([0.1, 0.1])], [0, 1, 2], nf, ns)
+    assert groups == 2 * (2 * ns) ** 2                # but once per trajectory group
