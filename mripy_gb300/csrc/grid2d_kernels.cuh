@@ -236,28 +236,44 @@ __global__ void __launch_bounds__(512) k_spread2d(SpreadArgs a) {
             if (lo >= hi) continue;
             const float2 v = st_v[s * CG + c];
             const float *w = st_w + s * 32;
-            // per lane: the column weight folded into the coil value, and the tap's tile column
-            float2 wyv[L::KT];
-            int ly[L::KT];
-#pragma unroll
-            for (int t = 0; t < L::KT; ++t) {
-                const int ky = q + t * L::NQ;
-                const bool in = ky < 16;
-                const float wy = in ? w[16 + (in ? ky : 0)] : 0.f;
-                ly[t] = in ? st_y[s * 16 + (in ? ky : 0)] : -1;
-                wyv[t] = make_float2(wy * v.x, wy * v.y);
-            }
-            const float *wx_row = w - r.x;
-            float2 *dst = acc + (size_t)lo * TY * CG + c;
+            if constexpr (CG == 1) {
+                // one coil: lane (xo, ky) takes y tap ky on every other row from lo + xo, so
+                // 32 lanes cover 16 tap slots on two rows at once
+                const int ky = lane & 15, xo = lane >> 4;
+                const int yy = st_y[s * 16 + ky];
+                const float wy = w[16 + ky];
+                const float2 wyv1 = make_float2(wy * v.x, wy * v.y);
+                const float *wx_row1 = w - r.x;
+                float2 *dst1 = acc + (size_t)(lo + xo) * TY + yy;
 #pragma unroll 4
-            for (int row = lo; row < hi; ++row, dst += TY * CG) {
-                const float wx = wx_row[row];
-                const float2 wx2 = make_float2(wx, wx);
+                for (int row = lo + xo; row < hi; row += 2, dst1 += 2 * TY) {
+                    const float wx = wx_row1[row];
+                    if (yy >= 0) *dst1 = __ffma2_rn(make_float2(wx, wx), wyv1, *dst1);
+                }
+            } else {
+                // per lane: the column weight folded into the coil value, and the tap's tile column
+                float2 wyv[L::KT];
+                int ly[L::KT];
 #pragma unroll
                 for (int t = 0; t < L::KT; ++t) {
-                    if (ly[t] >= 0) {
-                        float2 *cell = dst + (size_t)ly[t] * CG;
-                        *cell = __ffma2_rn(wx2, wyv[t], *cell);
+                    const int ky = q + t * L::NQ;
+                    const bool in = ky < 16;
+                    const float wy = in ? w[16 + (in ? ky : 0)] : 0.f;
+                    ly[t] = in ? st_y[s * 16 + (in ? ky : 0)] : -1;
+                    wyv[t] = make_float2(wy * v.x, wy * v.y);
+                }
+                const float *wx_row = w - r.x;
+                float2 *dst = acc + (size_t)lo * TY * CG + c;
+#pragma unroll 4
+                for (int row = lo; row < hi; ++row, dst += TY * CG) {
+                    const float wx = wx_row[row];
+                    const float2 wx2 = make_float2(wx, wx);
+#pragma unroll
+                    for (int t = 0; t < L::KT; ++t) {
+                        if (ly[t] >= 0) {
+                            float2 *cell = dst + (size_t)ly[t] * CG;
+                            *cell = __ffma2_rn(wx2, wyv[t], *cell);
+                        }
                     }
                 }
             }

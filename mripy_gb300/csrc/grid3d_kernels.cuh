@@ -469,27 +469,45 @@ __global__ void __launch_bounds__(256) k_spread3d(SpreadArgs a) {
             if (yl >= yh) continue;
             const float2 v = st_v[s * CG + c];
             const float *w = st_w + s * 48;
-            float wz[L::KT];
-            int lz[L::KT];
-#pragma unroll
-            for (int t = 0; t < L::KT; ++t) {
-                const int kz = q + t * L::NQ;
+            if constexpr (CG == 1) {
+                // one coil: lane (yo, kz) takes z tap kz on every other y row from yl + yo, so
+                // 32 lanes cover 16 tap slots on two rows at once
+                const int kz = lane & 15, yo = lane >> 4;
                 const int z = r.z + kz;
-                const bool ok = kz < W && (unsigned)z < (unsigned)e[2];
-                wz[t] = ok ? w[32 + kz] : 0.f;
-                lz[t] = ok ? z : -1;
-            }
-            for (int x = xl; x < xh; ++x) {
-                const float wx = w[x - r.x];
-                for (int y = yl; y < yh; ++y) {
-                    const float wxy = wx * w[16 + y - r.y];
-                    float2 *rowp = acc + ((size_t)x * TY + y) * TZ * CG + c;
+                const bool zok = kz < W && (unsigned)z < (unsigned)e[2];
+                const float wz1 = zok ? w[32 + kz] : 0.f;
+                const float2 vz = make_float2(wz1 * v.x, wz1 * v.y);
+                for (int x = xl; x < xh; ++x) {
+                    const float wx = w[x - r.x];
+                    float2 *rowp = acc + ((size_t)x * TY + yl + yo) * TZ + z;
+                    for (int y = yl + yo; y < yh; y += 2, rowp += 2 * TZ) {
+                        const float wxy = wx * w[16 + y - r.y];
+                        if (zok) *rowp = __ffma2_rn(make_float2(wxy, wxy), vz, *rowp);
+                    }
+                }
+            } else {
+                float wz[L::KT];
+                int lz[L::KT];
 #pragma unroll
-                    for (int t = 0; t < L::KT; ++t) {
-                        if (lz[t] >= 0) {
-                            float2 *cell = rowp + (size_t)lz[t] * CG;
-                            const float ww = wxy * wz[t];
-                            *cell = __ffma2_rn(make_float2(ww, ww), v, *cell);
+                for (int t = 0; t < L::KT; ++t) {
+                    const int kz = q + t * L::NQ;
+                    const int z = r.z + kz;
+                    const bool ok = kz < W && (unsigned)z < (unsigned)e[2];
+                    wz[t] = ok ? w[32 + kz] : 0.f;
+                    lz[t] = ok ? z : -1;
+                }
+                for (int x = xl; x < xh; ++x) {
+                    const float wx = w[x - r.x];
+                    for (int y = yl; y < yh; ++y) {
+                        const float wxy = wx * w[16 + y - r.y];
+                        float2 *rowp = acc + ((size_t)x * TY + y) * TZ * CG + c;
+#pragma unroll
+                        for (int t = 0; t < L::KT; ++t) {
+                            if (lz[t] >= 0) {
+                                float2 *cell = rowp + (size_t)lz[t] * CG;
+                                const float ww = wxy * wz[t];
+                                *cell = __ffma2_rn(make_float2(ww, ww), v, *cell);
+                            }
                         }
                     }
                 }
