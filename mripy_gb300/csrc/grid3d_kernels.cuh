@@ -94,43 +94,72 @@ __global__ void __launch_bounds__(256) k_interp3d(InterpArgs a) {
             const float d = (lane < 16 ? p.x : p.y) + (float)(ns - 1 - kk);
             myw = exp2f(-beta * d * d);
         }
-        float wy[L::WMAX];
+        float2 acc = make_float2(0.f, 0.f);
+        if constexpr (CG == 1) {
+            // one coil: lane (yo, kz) takes z tap kz on every other y row from yo, so 32
+            // lanes cover 16 tap slots on two rows at once; each lane's y weights come from
+            // the lanes 16.. that evaluated them
+            constexpr int HW = (L::WMAX + 1) / 2;
+            const int kz = lane & 15, yo = lane >> 4;
+            float wyl[HW];
 #pragma unroll
-        for (int k = 0; k < L::WMAX; ++k) wy[k] = __shfl_sync(0xffffffffu, myw, 16 + k);
-        float wz[L::KT];
-#pragma unroll
-        for (int t = 0; t < L::KT; ++t) {
-            const int kz = q + t * L::NQ;
-            const float d = p.z + (float)(ns - 1 - kz);
-            wz[t] = kz < W ? exp2f(-g.beta2[2] * d * d) : 0.f;
-        }
-        // a lane's z taps are fixed: sum wx wy * G per tap slot, apply wz once at the end
-        float2 at[L::KT];
-#pragma unroll
-        for (int t = 0; t < L::KT; ++t) at[t] = make_float2(0.f, 0.f);
-        const float2 *base = win + (((size_t)rel[0] * WY + rel[1]) * WZ + rel[2]) * CG + c;
+            for (int i = 0; i < HW; ++i) wyl[i] = __shfl_sync(0xffffffffu, myw, 16 + min(2 * i + yo, 15));
+            const float dz = p.z + (float)(ns - 1 - kz);
+            const float wz1 = kz < W ? exp2f(-g.beta2[2] * dz * dz) : 0.f;
+            float2 at1 = make_float2(0.f, 0.f);
+            const float2 *base1 = win + (((size_t)rel[0] * WY + rel[1] + yo) * WZ + rel[2]) + kz;
 #pragma unroll 1
-        for (int kx = 0; kx < W; ++kx) {
-            const float wx = __shfl_sync(0xffffffffu, myw, kx);
-            const float2 *plane = base + (size_t)kx * WY * WZ * CG;
+            for (int kx = 0; kx < W; ++kx) {
+                const float wx = __shfl_sync(0xffffffffu, myw, kx);
+                const float2 *plane = base1 + (size_t)kx * WY * WZ;
 #pragma unroll
-            for (int ky = 0; ky < L::WMAX; ++ky) {
-                if (WT == 0 && ky >= W) break;
-                const float wxy = wx * wy[ky];
-                const float2 wxy2 = make_float2(wxy, wxy);
-                const float2 *row = plane + (size_t)ky * WZ * CG;
-#pragma unroll
-                for (int t = 0; t < L::KT; ++t) {
-                    const int kz = q + t * L::NQ;
-                    if (kz < W) at[t] = __ffma2_rn(wxy2, row[kz * CG], at[t]);
+                for (int i = 0; i < HW; ++i) {
+                    if (WT == 0 && 2 * i >= W) break;
+                    if (2 * i + yo < W && kz < W) {
+                        const float wxy = wx * wyl[i];
+                        at1 = __ffma2_rn(make_float2(wxy, wxy), plane[(size_t)2 * i * WZ], at1);
+                    }
                 }
             }
-        }
-        float2 acc = make_float2(0.f, 0.f);
+            acc = make_float2(wz1 * at1.x, wz1 * at1.y);
+        } else {
+            float wy[L::WMAX];
 #pragma unroll
-        for (int t = 0; t < L::KT; ++t) {
-            acc.x = fmaf(wz[t], at[t].x, acc.x);
-            acc.y = fmaf(wz[t], at[t].y, acc.y);
+            for (int k = 0; k < L::WMAX; ++k) wy[k] = __shfl_sync(0xffffffffu, myw, 16 + k);
+            float wz[L::KT];
+#pragma unroll
+            for (int t = 0; t < L::KT; ++t) {
+                const int kz = q + t * L::NQ;
+                const float d = p.z + (float)(ns - 1 - kz);
+                wz[t] = kz < W ? exp2f(-g.beta2[2] * d * d) : 0.f;
+            }
+            // a lane's z taps are fixed: sum wx wy * G per tap slot, apply wz once at the end
+            float2 at[L::KT];
+#pragma unroll
+            for (int t = 0; t < L::KT; ++t) at[t] = make_float2(0.f, 0.f);
+            const float2 *base = win + (((size_t)rel[0] * WY + rel[1]) * WZ + rel[2]) * CG + c;
+#pragma unroll 1
+            for (int kx = 0; kx < W; ++kx) {
+                const float wx = __shfl_sync(0xffffffffu, myw, kx);
+                const float2 *plane = base + (size_t)kx * WY * WZ * CG;
+#pragma unroll
+                for (int ky = 0; ky < L::WMAX; ++ky) {
+                    if (WT == 0 && ky >= W) break;
+                    const float wxy = wx * wy[ky];
+                    const float2 wxy2 = make_float2(wxy, wxy);
+                    const float2 *row = plane + (size_t)ky * WZ * CG;
+#pragma unroll
+                    for (int t = 0; t < L::KT; ++t) {
+                        const int kz = q + t * L::NQ;
+                        if (kz < W) at[t] = __ffma2_rn(wxy2, row[kz * CG], at[t]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < L::KT; ++t) {
+                acc.x = fmaf(wz[t], at[t].x, acc.x);
+                acc.y = fmaf(wz[t], at[t].y, acc.y);
+            }
         }
 #pragma unroll
         for (int off = CG; off < 32; off <<= 1) {

@@ -136,8 +136,13 @@ class _NUFFTnd:
     def plan(self, n_coil):
         p = self._plans.get(n_coil)
         if p is None:
+            # tiles tuned for several coils per block do not fit plans with fewer coils (the
+            # one-coil density estimation): those take the library's defaults
+            tuning = self.tuning
+            if tuning is not None and n_coil < getattr(tuning, "coil_group", 0):
+                tuning = None
             p = NufftPlan(self.dim, self.im_shape, n_coil=n_coil, n_traj=1, eps=self.eps, iflag=1, df=1.0,
-                          max_nspread=self.max_nspread, tuning=self.tuning)
+                          max_nspread=self.max_nspread, tuning=tuning)
             p.set_points(self._coords())
             self._plans[n_coil] = p
         return p
