@@ -167,39 +167,64 @@ __global__ void __launch_bounds__(512) k_interp2d_tma(InterpArgs a, const __grid
             const float sc = (q == 0 && a.weight) ? a.weight[j] : 1.f;
             // the item's coils in passes of CG (lanes = CG coils x tap slots)
             const int passes = MULTI ? t.passes : 1;
-            for (int ps = 0; ps < passes; ++ps) {
-                const int coil = it.cg0 + ps * CG + c;
-                float2 acc[L::KT];
+            if constexpr (CG == 1 && !MULTI) {
+                // one coil: lane (xo, ky) takes y tap ky on every other x row from xo, so 32
+                // lanes cover 16 tap slots on two rows at once
+                const int ky1 = lane & 15, xo = lane >> 4;
+                const float wy1 = __shfl_sync(0xffffffffu, myw, 16 + ky1);
+                float2 acc1 = make_float2(0.f, 0.f);
+                const float2 *rb = win + (rel0 + xo) * t.BY + rel1 + off1 + ky1;
 #pragma unroll
-                for (int tt = 0; tt < L::KT; ++tt) acc[tt] = make_float2(0.f, 0.f);
-                const float2 *rowbase = win + (ps * CG + c) * t.CS + rel0 * t.BY + rel1 + off1;
-#pragma unroll
-                for (int kx = 0; kx < L::WMAX; ++kx) {
-                    if (WT == 0 && kx >= W) break;
-                    float wx;
-                    if constexpr (MULTI) wx = wxs[kx];
-                    else wx = __shfl_sync(0xffffffffu, myw, kx);
-                    const float2 wx2 = make_float2(wx, wx);
-                    const float2 *row = rowbase + kx * t.BY;
-#pragma unroll
-                    for (int tt = 0; tt < L::KT; ++tt) {
-                        const int ky = q + tt * L::NQ;
-                        if (ky < W) acc[tt] = __ffma2_rn(wx2, row[ky], acc[tt]);
-                    }
+                for (int i = 0; i < (L::WMAX + 1) / 2; ++i) {
+                    if (WT == 0 && 2 * i >= W) break;
+                    const int kx = 2 * i + xo;
+                    const float wx = __shfl_sync(0xffffffffu, myw, kx < 16 ? kx : 15);
+                    if (kx < W && ky1 < W) acc1 = __ffma2_rn(make_float2(wx, wx), rb[2 * i * t.BY], acc1);
                 }
-                float ax = 0.f, ay = 0.f;
+                const float wyl = ky1 < W ? wy1 : 0.f;
+                float ax = wyl * acc1.x, ay = wyl * acc1.y;
 #pragma unroll
-                for (int tt = 0; tt < L::KT; ++tt) {
-                    ax = fmaf(wy[tt], acc[tt].x, ax);
-                    ay = fmaf(wy[tt], acc[tt].y, ay);
-                }
-#pragma unroll
-                for (int off = CG; off < 32; off <<= 1) {
+                for (int off = 1; off < 32; off <<= 1) {
                     ax += __shfl_xor_sync(0xffffffffu, ax, off);
                     ay += __shfl_xor_sync(0xffffffffu, ay, off);
                 }
-                if (q == 0 && coil < g.n_coil)
-                    a.c[(int64_t)j * a.c_elem + (int64_t)coil * a.c_coil] = make_float2(ax * sc, ay * sc);
+                if (lane == 0 && it.cg0 < g.n_coil)
+                    a.c[(int64_t)j * a.c_elem + (int64_t)it.cg0 * a.c_coil] = make_float2(ax * sc, ay * sc);
+            } else {
+                for (int ps = 0; ps < passes; ++ps) {
+                    const int coil = it.cg0 + ps * CG + c;
+                    float2 acc[L::KT];
+#pragma unroll
+                    for (int tt = 0; tt < L::KT; ++tt) acc[tt] = make_float2(0.f, 0.f);
+                    const float2 *rowbase = win + (ps * CG + c) * t.CS + rel0 * t.BY + rel1 + off1;
+#pragma unroll
+                    for (int kx = 0; kx < L::WMAX; ++kx) {
+                        if (WT == 0 && kx >= W) break;
+                        float wx;
+                        if constexpr (MULTI) wx = wxs[kx];
+                        else wx = __shfl_sync(0xffffffffu, myw, kx);
+                        const float2 wx2 = make_float2(wx, wx);
+                        const float2 *row = rowbase + kx * t.BY;
+#pragma unroll
+                        for (int tt = 0; tt < L::KT; ++tt) {
+                            const int ky = q + tt * L::NQ;
+                            if (ky < W) acc[tt] = __ffma2_rn(wx2, row[ky], acc[tt]);
+                        }
+                    }
+                    float ax = 0.f, ay = 0.f;
+#pragma unroll
+                    for (int tt = 0; tt < L::KT; ++tt) {
+                        ax = fmaf(wy[tt], acc[tt].x, ax);
+                        ay = fmaf(wy[tt], acc[tt].y, ay);
+                    }
+#pragma unroll
+                    for (int off = CG; off < 32; off <<= 1) {
+                        ax += __shfl_xor_sync(0xffffffffu, ax, off);
+                        ay += __shfl_xor_sync(0xffffffffu, ay, off);
+                    }
+                    if (q == 0 && coil < g.n_coil)
+                        a.c[(int64_t)j * a.c_elem + (int64_t)coil * a.c_coil] = make_float2(ax * sc, ay * sc);
+                }
             }
         }
         __syncthreads();  // every read of this buffer (and of ring[b]) is done: refill both

@@ -94,12 +94,25 @@ def espirit_nd(xcrop, x_shape, nsingularv=150, hkwin_shape=(16, 16), pad_before_
     st = a.stride()
     view = torch.as_strided(a, win + moves + (nc,), st[:d] + st[:d] + (st[d],))
     hmtx = view.reshape(int(np.prod(win)), -1)
-    _, s, vh = torch.linalg.svd(hmtx, full_matrices=False)
+    r, ncol = int(hmtx.shape[0]), int(hmtx.shape[1])
+    gram = r <= ncol and r * r * ncol <= (1 << 30)
+    if gram:
+        # short, wide Hankel matrices (2-D calibration): singular values and right vectors
+        # from the FP64 Gram matrix H H^H and its eigendecomposition, about twice as fast as
+        # the SVD there; the kept vectors v_k = U_k^H H / s_k have s_k >= nsigv_th * s_0
+        h64 = hmtx.to(torch.complex128)
+        lam, U = torch.linalg.eigh(h64 @ h64.conj().T)
+        s = lam.flip(0).clamp_min(0.0).sqrt()
+        U = U.flip(1)
+    else:
+        _, s, vh = torch.linalg.svd(hmtx, full_matrices=False)
     s_host = s.cpu().numpy()
     nsv = nsingularv
     for k in range(len(s_host)):
         if s_host[k] > s_host[0] * nsigv_th:
             nsv = k
+    if gram:
+        vh = ((U[:, :nsv].conj().T @ h64) / s[:nsv, None]).to(torch.complex64)
     if pad_before_espirit == 0:
         n = tuple(min(pad_fact * int(a.shape[k]), int(x_shape[k])) for k in range(d))
     else:
