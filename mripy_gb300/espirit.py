@@ -95,13 +95,15 @@ def espirit_nd(xcrop, x_shape, nsingularv=150, hkwin_shape=(16, 16), pad_before_
     view = torch.as_strided(a, win + moves + (nc,), st[:d] + st[:d] + (st[d],))
     hmtx = view.reshape(int(np.prod(win)), -1)
     r, ncol = int(hmtx.shape[0]), int(hmtx.shape[1])
-    gram = r <= ncol and r * r * ncol <= (1 << 30)
+    gram = r <= ncol
     if gram:
-        # short, wide Hankel matrices (2-D calibration): singular values and right vectors
-        # from the FP64 Gram matrix H H^H and its eigendecomposition, about twice as fast as
-        # the SVD there; the kept vectors v_k = U_k^H H / s_k have s_k >= nsigv_th * s_0
-        h64 = hmtx.to(torch.complex128)
-        lam, U = torch.linalg.eigh(h64 @ h64.conj().T)
+        # wide Hankel matrices: singular values and right vectors from the Gram matrix H H^H
+        # and its FP64 eigendecomposition, 2-2.5x faster than the SVD on GB300.  The product
+        # is FP64 up to r^2 c = 2^30 (2-D calibrations), FP32 beyond (3-D), where it blurs only
+        # singular values far below the kept ones; the kept vectors v_k = U_k^H H / s_k have
+        # s_k >= nsigv_th * s_0, and the maps depend on their span alone
+        h = hmtx.to(torch.complex128) if r * r * ncol <= (1 << 30) else hmtx
+        lam, U = torch.linalg.eigh((h @ h.conj().T).to(torch.complex128))
         s = lam.flip(0).clamp_min(0.0).sqrt()
         U = U.flip(1)
     else:
@@ -112,7 +114,7 @@ def espirit_nd(xcrop, x_shape, nsingularv=150, hkwin_shape=(16, 16), pad_before_
         if s_host[k] > s_host[0] * nsigv_th:
             nsv = k
     if gram:
-        vh = ((U[:, :nsv].conj().T @ h64) / s[:nsv, None]).to(torch.complex64)
+        vh = ((U[:, :nsv].conj().T.to(h.dtype) @ h) / s[:nsv, None].to(h.real.dtype)).to(torch.complex64)
     if pad_before_espirit == 0:
         n = tuple(min(pad_fact * int(a.shape[k]), int(x_shape[k])) for k in range(d))
     else:

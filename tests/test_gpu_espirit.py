@@ -92,3 +92,19 @@ def test_espirit_3d_matches_oracle():
     keep = sr > 0.05
     assert np.linalg.norm(sg[keep] - sr[keep]) / np.linalg.norm(sr[keep]) < 1e-3
     assert np.quantile(_agreement(vg, vr, keep), 0.01) > 0.999
+
+
+def test_espirit_3d_wide_calibration_matches_oracle():
+    """A 3-D calibration whose Hankel matrix (512 x 8788) takes the FP32 Gram product."""
+    rng = np.random.default_rng(64)
+    shape, nc = (32, 32, 32), 4
+    xcrop, S, x = _calib(shape, nc, 20, rng)
+    vg, sg, info = E.espirit_nd(xcrop, shape + (nc,), hkwin_shape=(8, 8, 8), return_info=True)
+    vr, sr, iref = EO.espirit(xcrop, shape + (nc,), hkwin_shape=(8, 8, 8), return_info=True)
+    assert info["nsv"] == iref["nsv"]
+    s0 = iref["singular_values"][0]
+    kept = iref["singular_values"] > 0.2 * s0
+    assert np.allclose(info["singular_values"][kept], iref["singular_values"][kept], rtol=1e-4)
+    keep = sr > 0.05
+    assert np.linalg.norm(sg[keep] - sr[keep]) / np.linalg.norm(sr[keep]) < 1e-3
+    assert np.quantile(_agreement(vg, vr, keep), 0.01) > 0.999
