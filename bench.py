@@ -637,7 +637,7 @@ def autograd_time(torch, wl, tuning, steps=20):
     ms = e0.elapsed_time(e1) / steps
     M, nc = wl.M, wl.n_coil
     return {"steps": steps, "ms_per_step": round(ms, 4), "value": round(M * nc / (ms * 1e-3) / 1e6, 2),
-            "unit": UNIT, "loss": float(loss), "grad_k_rms": float(k.grad.pow(2).mean().sqrt()),
+            "unit": UNIT, "loss": float(loss.detach()), "grad_k_rms": float(k.grad.pow(2).mean().sqrt()),
             "includes": "bin sort of the perturbed trajectory, type-2, loss, backward: image gradient "
                         "(type-1) and trajectory gradient (pad, FFT, weight-derivative interp)"}
 

@@ -136,6 +136,10 @@ struct gbn_graph {
 
 namespace {
 
+// spread-list entries (sample x tile) up to which set_points sizes the list's keys and values
+// by a bound and synchronises once (256 MB of keys and values)
+constexpr uint64_t kOneSyncEntries = (uint64_t)1 << 25;
+
 int ensure(gbn_plan *p, DevBuf &b, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (b.cap >= bytes) return GBN_OK;
@@ -523,6 +527,50 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
             return cub::DeviceScan::ExclusiveSum(tmp, bytes, tc, to, (int)M, s);
         }));
     }
+    // The spread list (one entry per sample and tile its stencil reaches) has E = sum of the
+    // touch counts entries.  When a bound on E fits kOneSyncEntries, its keys are written
+    // before E is known and the work-item counts are queued behind them, so one host
+    // synchronisation returns E, the counts and the status together (set_points on a changing
+    // trajectory, as in a differentiable reconstruction, then costs one round trip).  Per axis
+    // a W-cell stencil reaches at most ceil((W-1)/T) + 1 tiles, one more when a partial last
+    // tile sits at the wrap, and never more than the axis has.
+    uint64_t bound = (uint64_t)M;
+    for (int d = 0; d < p->dim; ++d) {
+        const Geom &g = p->gs;
+        const uint64_t per = (uint64_t)((g.W - 1 + g.tile[d] - 1) / g.tile[d] + (g.nf[d] % g.tile[d] ? 2 : 1));
+        bound *= std::min<uint64_t>(per, (uint64_t)g.ntile[d]);
+    }
+    const bool one_sync = M > 0 && bound <= kOneSyncEntries;
+    uint32_t *scount = p->spread_count.as<uint32_t>();
+    // 3-D: spread tiles with at least dense_min samples (the k-space centre of radial
+    // trajectories) accumulate with compensated sums; status word 1 counts their work items,
+    // word 2 the split tiles (zeroed before each spread), word 3 is the split list's cursor
+    const uint32_t dense_min = p->dim == 3 && p->dense_min > 0 ? (uint32_t)p->dense_min : 0u;
+    GBN_TRY(ensure(p, p->split_tiles, sizeof(uint32_t) * (size_t)std::max<int64_t>(Ts, 1)));
+    // the plane-streaming 3-D interp holds a chunk of kPlaneSamples samples' state; work
+    // items of at most that size stream each window once
+    const int interp_max_sub = interp3d_planes_smem(p->gi, interp_cg(p), p->interp_threads) > 0
+                                   ? std::min(p->max_sub, kPlaneSamples)
+                                   : p->max_sub;
+    SubsJob js{&p->gs, scount, &p->spread_tile_off, &p->nsub, &p->sub_off, 1, p->max_sub, dense_min,
+               p->kstatus + 1, p->kstatus + 2};
+    SubsJob ji{&p->gi, home_count, &p->home_tile_off, &p->nsub_i, &p->sub_off_i, 0, interp_max_sub, 0u, nullptr,
+               nullptr};
+    uint32_t sizes[6] = {0, 0, 0, 0, 0, 0};  // spread last offset / count, interp ditto, dense, split
+    auto queue_counts = [&]() -> int {
+        GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, 3 * sizeof(uint32_t), s));
+        GBN_TRY(subs_count(p, js, sizes, s));
+        GBN_TRY(subs_count(p, ji, sizes + 2, s));
+        GBN_CUDA(cudaMemcpyAsync(sizes + 4, p->kstatus + 1, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        return GBN_OK;
+    };
+    if (one_sync) {
+        GBN_TRY(ensure(p, p->dup_keys, sizeof(uint32_t) * (size_t)bound));
+        GBN_TRY(ensure(p, p->dup_vals, sizeof(uint32_t) * (size_t)bound));
+        GBN_CUDA(launch_dup_keys(p->pts.as<float4>(), M, p->traj_off_d.as<int64_t>(), nt, p->gs, to,
+                                 p->dup_keys.as<uint32_t>(), p->dup_vals.as<uint32_t>(), scount, s));
+        GBN_TRY(queue_counts());
+    }
     uint64_t last_off = 0;
     uint32_t last_cnt = 0, status = 0;
     if (M > 0) {
@@ -534,6 +582,7 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
     if (status & 1u) return fail(GBN_ERR_ARG, "non-finite trajectory coordinate");
     const uint64_t E = M > 0 ? last_off + last_cnt : 0;
     if (E >= ((uint64_t)1 << 31)) return fail(GBN_ERR_CAPACITY, "spread list above 2^31 entries");
+    if (one_sync && E > bound) return fail(GBN_ERR_INTERNAL, "spread list above its bound");
     p->n_dup = (int64_t)E;
     const size_t Eb = (size_t)std::max<uint64_t>(E, 1);
     GBN_TRY(ensure(p, p->dup_keys, sizeof(uint32_t) * Eb));
@@ -541,9 +590,9 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
     GBN_TRY(ensure(p, p->dup_keys_sorted, sizeof(uint32_t) * Eb));
     GBN_TRY(ensure(p, p->dup_idx, sizeof(uint32_t) * Eb));
     GBN_TRY(ensure(p, p->dup_pts, sizeof(float4) * Eb));
-    uint32_t *scount = p->spread_count.as<uint32_t>();
-    GBN_CUDA(launch_dup_keys(p->pts.as<float4>(), M, p->traj_off_d.as<int64_t>(), nt, p->gs, to,
-                             p->dup_keys.as<uint32_t>(), p->dup_vals.as<uint32_t>(), scount, s));
+    if (!one_sync)
+        GBN_CUDA(launch_dup_keys(p->pts.as<float4>(), M, p->traj_off_d.as<int64_t>(), nt, p->gs, to,
+                                 p->dup_keys.as<uint32_t>(), p->dup_vals.as<uint32_t>(), scount, s));
     if (E > 0) {
         uint32_t *kin = p->dup_keys.as<uint32_t>(), *vin = p->dup_vals.as<uint32_t>();
         uint32_t *kout = p->dup_keys_sorted.as<uint32_t>(), *vout = p->dup_idx.as<uint32_t>();
@@ -564,26 +613,10 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
         }));
         GBN_CUDA(launch_gather_pts(p->pts.as<float4>(), vout, M, p->home_pts.as<float4>(), s));
     }
-    // 3-D: spread tiles with at least dense_min samples (the k-space centre of radial
-    // trajectories) accumulate with compensated sums; status word 1 counts their work items,
-    // word 2 the split tiles (zeroed before each spread), word 3 is the split list's cursor
-    const uint32_t dense_min = p->dim == 3 && p->dense_min > 0 ? (uint32_t)p->dense_min : 0u;
-    GBN_TRY(ensure(p, p->split_tiles, sizeof(uint32_t) * (size_t)std::max<int64_t>(Ts, 1)));
-    GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, 3 * sizeof(uint32_t), s));
-    // the plane-streaming 3-D interp holds a chunk of kPlaneSamples samples' state; work
-    // items of at most that size stream each window once
-    const int interp_max_sub = interp3d_planes_smem(p->gi, interp_cg(p), p->interp_threads) > 0
-                                   ? std::min(p->max_sub, kPlaneSamples)
-                                   : p->max_sub;
-    SubsJob js{&p->gs, scount, &p->spread_tile_off, &p->nsub, &p->sub_off, 1, p->max_sub, dense_min,
-               p->kstatus + 1, p->kstatus + 2};
-    SubsJob ji{&p->gi, home_count, &p->home_tile_off, &p->nsub_i, &p->sub_off_i, 0, interp_max_sub, 0u, nullptr,
-               nullptr};
-    uint32_t sizes[6] = {0, 0, 0, 0, 0, 0};  // spread last offset / count, interp ditto, dense, split
-    GBN_TRY(subs_count(p, js, sizes, s));
-    GBN_TRY(subs_count(p, ji, sizes + 2, s));
-    GBN_CUDA(cudaMemcpyAsync(sizes + 4, p->kstatus + 1, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    GBN_CUDA(cudaStreamSynchronize(s));
+    if (!one_sync) {
+        GBN_TRY(queue_counts());
+        GBN_CUDA(cudaStreamSynchronize(s));
+    }
     GBN_TRY(subs_build(p, js, sizes, p->spread_subs, p->split_tiles.as<uint32_t>(), p->kstatus + 3,
                        &p->n_spread_sub, s));
     GBN_TRY(subs_build(p, ji, sizes + 2, p->interp_subs, nullptr, nullptr, &p->n_interp_sub, s));
