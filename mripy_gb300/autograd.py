@@ -39,14 +39,16 @@ def _points_for_backward(ctx, coords):
 
 def _group_scale(plan, img, inverse):
     """Multiply each trajectory group's image by M_g (inverse=True) to undo type-1's 1/M_g.
-    The per-group factors are built once per set of points (no host copy per call)."""
+    The per-group factors depend on the group sizes alone: they are built once per set of
+    group offsets, not per set of points (a host-to-device copy each step would cost more
+    than the multiply)."""
+    off = tuple(int(v) for v in plan.traj_offsets)
     cache = getattr(plan, "_group_scale_cache", None)
-    if cache is None or cache[0] != plan.points_generation or cache[1] != img.device:
-        off = plan.traj_offsets
+    if cache is None or cache[0] != off or cache[1] != img.device:
         counts = torch.tensor([off[g + 1] - off[g] for g in range(plan.n_traj)], dtype=torch.float32,
                               device=img.device)
         inv = torch.where(counts > 0, 1.0 / counts.clamp(min=1.0), torch.zeros_like(counts))
-        cache = (plan.points_generation, img.device, counts, inv)
+        cache = (off, img.device, counts, inv)
         plan._group_scale_cache = cache
     s = cache[2] if inverse else cache[3]
     return img * s.view((-1,) + (1,) * (img.dim() - 1))
