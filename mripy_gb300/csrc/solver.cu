@@ -409,6 +409,7 @@ __device__ void haar_levels_smem(float2 *sm, int L, int cpb_log, int n_units, fl
 }
 
 constexpr int kHaarCubes = 16;  // level-1 cubes per thread, times 2^DIM (4096-cell blocks, 256 threads)
+static_assert(kHaarCubes * kHaarThreads == kHaarMaxElems, "a block's level-1 cubes must fit its threads");
 
 // first unit of the block, the number of units it holds, and their decoded references
 template <int DIM>
@@ -665,6 +666,9 @@ int haar_geom(int dim, const int32_t *shape, int level, int64_t n_outer, int64_t
     int upb_log = 0;
     while (((cells * h.cpb) << (upb_log + 1)) <= kHaarBlockElems && (1 << (upb_log + 1)) <= kHaarMaxUnits) ++upb_log;
     h.upb_log = upb_log;
+    // the kernels give each thread at most kHaarCubes / 2^dim level-1 cubes of a block
+    if (((cells * h.cpb) << upb_log) > kHaarMaxElems)
+        return record_error(GBN_ERR_INTERNAL, "Haar transform: block above its element budget");
     if (haar_blocks(h) > 0x7fffffff) return record_error(GBN_ERR_CAPACITY, "Haar transform: too many tiles");
     return GBN_OK;
 }
