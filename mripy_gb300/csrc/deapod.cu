@@ -42,6 +42,13 @@ __global__ void k_build_table(int m, int nf, double tau, float *tab) {
 
 __global__ void k_fill_one(float *tab) { tab[0] = 1.f; }
 
+// entry D - 1 of a kernel argument's per-axis array, read with constant indices (a run-time
+// index would copy the whole argument block to local memory in every thread)
+template <class T>
+__device__ __forceinline__ T last_axis(const T (&v)[3], int D) {
+    return D == 3 ? v[2] : (D == 2 ? v[1] : v[0]);
+}
+
 // grid index of image index i along one dim: band cells are [0, m - m/2) and [nf - m/2, nf)
 __device__ __forceinline__ int grid_index(int i, int m, int nf) {
     const int g = i - m / 2;
@@ -89,7 +96,7 @@ __device__ __forceinline__ BandRow band_row(const DeapodArgs &a, const Decomp &d
         r.s = a.tab[0][r.p];
         r.gbase = grid_index((int)r.p, a.m[0], g.nf[0]);
     }
-    const int ml = a.m[D - 1];
+    const int ml = last_axis(a.m, D);
     r.i0 = r.seg_i * dc.seg;
     r.seg_len = min(dc.seg, ml - r.i0);
     r.c0 = chunk * dc.cc;
@@ -165,13 +172,15 @@ __global__ void __launch_bounds__(kThreads) k_pad(DeapodArgs a, Decomp dc, Src s
     }
     const Geom &g = a.g;
     const int D = g.dim;
-    const int ml = a.m[D - 1], Ld = g.nf[D - 1];
-    const float *tl = a.tab[D - 1];
+    const int ml = last_axis(a.m, D), Ld = last_axis(g.nf, D);
+    const float *tl = last_axis(a.tab, D);
     const BandRow r = band_row(a, dc, blockIdx.x, true);
     const int SP = dc.seg + 1;
 
-    // stage the scaled pixels of the segment for the coil chunk
+    // stage the scaled pixels of the segment for the coil chunk (unrolled: several image
+    // loads in flight per thread)
     const int n = r.n_cc * r.seg_len;
+#pragma unroll 4
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
         int cc, k;
         if (dc.coil_fast) {
@@ -212,15 +221,17 @@ __global__ void __launch_bounds__(kThreads) k_crop(DeapodArgs a, Decomp dc, cons
     extern __shared__ float2 st_crop[];
     const Geom &g = a.g;
     const int D = g.dim;
-    const int ml = a.m[D - 1], Ld = g.nf[D - 1];
-    const float *tl = a.tab[D - 1];
+    const int ml = last_axis(a.m, D), Ld = last_axis(g.nf, D);
+    const float *tl = last_axis(a.tab, D);
     const BandRow r = band_row(a, dc, blockIdx.x, true);
     const int SP = dc.seg + 1;
     const float s = a.grp_scale ? r.s * a.grp_scale[r.grp] : r.s;
 
-    // read the band runs of the coil chunk's grid rows
+    // read the band runs of the coil chunk's grid rows (unrolled: several grid loads in
+    // flight per warp)
     const int nch = (r.seg_len + 31) >> 5;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll 4
     for (int w = warp; w < r.n_cc * nch; w += nw) {
         const int cc = w / nch;
         const int k = (w - cc * nch) * 32 + lane;
@@ -256,8 +267,8 @@ __global__ void __launch_bounds__(kThreads) k_crop_sense(DeapodArgs a, Decomp dc
     constexpr int KP = kSenseSeg / kThreads;
     const Geom &g = a.g;
     const int D = g.dim;
-    const int ml = a.m[D - 1], Ld = g.nf[D - 1];
-    const float *tl = a.tab[D - 1];
+    const int ml = last_axis(a.m, D), Ld = last_axis(g.nf, D);
+    const float *tl = last_axis(a.tab, D);
     const BandRow r = band_row(a, dc, blockIdx.x, false);
     const int SP = dc.seg + 1;
     const bool sens_coil_fast = SL.coil_stride < SL.elem_stride;
@@ -292,15 +303,16 @@ __global__ void __launch_bounds__(kThreads) k_crop_sense(DeapodArgs a, Decomp dc
 #pragma unroll
         for (int k = 0; k < KP; ++k) {
             const int kk = threadIdx.x + k * kThreads;
-            if (kk >= r.seg_len) break;
-            float ax = acc[k].x, ay = acc[k].y;
-            for (int cc = 0; cc < n_cc; ++cc) {
-                const float2 v = rows[(int64_t)(c0 + cc) * g.G + cell[k]];
-                const float2 sv = st_cs[cc * SP + kk];
-                ax += sv.x * v.x + sv.y * v.y;
-                ay += sv.x * v.y - sv.y * v.x;
+            if (kk < r.seg_len) {  // a guard, not a break: the loop stays unrolled, acc in registers
+                float ax = acc[k].x, ay = acc[k].y;
+                for (int cc = 0; cc < n_cc; ++cc) {
+                    const float2 v = rows[(int64_t)(c0 + cc) * g.G + cell[k]];
+                    const float2 sv = st_cs[cc * SP + kk];
+                    ax += sv.x * v.x + sv.y * v.y;
+                    ay += sv.x * v.y - sv.y * v.x;
+                }
+                acc[k] = make_float2(ax, ay);
             }
-            acc[k] = make_float2(ax, ay);
         }
     }
 
@@ -309,10 +321,11 @@ __global__ void __launch_bounds__(kThreads) k_crop_sense(DeapodArgs a, Decomp dc
 #pragma unroll
     for (int k = 0; k < KP; ++k) {
         const int kk = threadIdx.x + k * kThreads;
-        if (kk >= r.seg_len) break;
-        const int i = r.i0 + kk;
-        const float f = s * tl[i];
-        dst[(r.p * ml + i) * XL.elem_stride] = make_float2(acc[k].x * f, acc[k].y * f);
+        if (kk < r.seg_len) {
+            const int i = r.i0 + kk;
+            const float f = s * tl[i];
+            dst[(r.p * ml + i) * XL.elem_stride] = make_float2(acc[k].x * f, acc[k].y * f);
+        }
     }
 }
 

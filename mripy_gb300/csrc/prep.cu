@@ -59,7 +59,11 @@ __global__ void k_prep(const T *__restrict__ x, const T *__restrict__ y, const T
     float f[3] = {0.f, 0.f, 0.f};
     int c0[3] = {0, 0, 0};
     bool bad = false;
-    for (int d = 0; d < dim; ++d) {
+    // loops over all three axes with a guard (not up to dim): unrolled, so the per-axis
+    // arrays and the Geom fields are indexed by constants and stay out of local memory
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (d >= dim) continue;
         double xs = (double)src[d][j] * df;
         if (!isfinite(xs)) { bad = true; continue; }
         const int nf = gs.nf[d];
@@ -81,7 +85,9 @@ __global__ void k_prep(const T *__restrict__ x, const T *__restrict__ y, const T
     const int g = group_of(traj_off, gs.n_traj, j);
     int t[3] = {0, 0, 0};
     uint32_t touch = 1;
-    for (int d = 0; d < dim; ++d) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (d >= dim) continue;
         int cc = c0[d] + ns - 1;
         if (cc >= gi.nf[d]) cc -= gi.nf[d];
         t[d] = cc / gi.tile[d];
@@ -103,7 +109,9 @@ __global__ void k_dup_keys(const float4 *__restrict__ pts, int64_t M, const int6
     int c0[3];
     unpack_cells(dim, __float_as_uint(pts[j].w), c0[0], c0[1], c0[2]);
     int n[3] = {1, 1, 1}, t0[3] = {0, 0, 0};
-    for (int d = 0; d < dim; ++d) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (d >= dim) continue;
         n[d] = touched_tiles(c0[d], gs.W, gs.nf[d], gs.tile[d], gs.ntile[d]);
         t0[d] = c0[d] / gs.tile[d];
     }
