@@ -31,6 +31,9 @@ def _spread_candidates(dim, n_coil):
             for th in (128, 256):
                 out.append(((4 * th // 32, 4 * 32 // cg), th, cg))
         out += [((16, 32), 256, 8), ((32, 32), 256, 8)]
+        if n_coil < 4:
+            # one-coil plans (the plain per-instance path): 128-thread blocks measured best
+            out += [((16, 32), 128, 8), ((32, 32), 128, 8)]
     elif dim == 3:
         for cg in groups:
             for th in (128, 256):
