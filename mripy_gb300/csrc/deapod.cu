@@ -28,6 +28,7 @@ namespace gbn {
 namespace {
 
 constexpr int kStageElems = 4096;  // staged complex values per band block (32 KB)
+constexpr int64_t kMinBandBlocks = 1024;  // band blocks a pad/crop launch aims for (~7 per SM)
 constexpr int kZeroChunk = 8192;   // cells per zero block
 constexpr int kThreads = 256;
 constexpr int kSenseSeg = 1024;    // crop_sense: at most 4 pixels per thread
@@ -334,7 +335,7 @@ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // seg_cap: longest segment of the last image dim per block; chunked: coil chunks are
 // separate blocks (pad, crop) rather than a loop inside the block (crop_sense);
 // zero: the launch also fills the out-of-band slabs (pad)
-Decomp make_decomp(const DeapodArgs &a, int seg_cap, bool chunked, bool zero, bool coil_fast) {
+Decomp make_decomp(const DeapodArgs &a, int seg_cap, bool chunked, bool zero, bool coil_fast, int min_cc = 1) {
     const Geom &g = a.g;
     const int D = g.dim;
     Decomp dc{};
@@ -344,6 +345,15 @@ Decomp make_decomp(const DeapodArgs &a, int seg_cap, bool chunked, bool zero, bo
     dc.seg = ml < seg_cap ? ml : seg_cap;
     dc.nseg = (int)ceil_div(ml, dc.seg);
     dc.cc = (int)std::max<int64_t>(1, std::min<int64_t>(g.n_coil, kStageElems / (dc.seg + 1)));
+    if (chunked) {
+        // equal chunks (16 coils: 8 + 8, not 15 + 1), and more of them while the launch has
+        // few rows (a 2-D image of a few hundred rows): enough blocks to fill the GPU, down
+        // to min_cc coils per chunk
+        int64_t ncc = ceil_div(g.n_coil, dc.cc);
+        const int64_t rows = (int64_t)g.n_traj * dc.n_outer * dc.nseg;
+        while (rows * ncc < kMinBandBlocks && ncc < g.n_coil && ceil_div(g.n_coil, 2 * ncc) >= min_cc) ncc *= 2;
+        dc.cc = (int)ceil_div(g.n_coil, std::min<int64_t>(ncc, g.n_coil));
+    }
     dc.ncc = chunked ? (int)ceil_div(g.n_coil, dc.cc) : 1;
     dc.nband = (int64_t)g.n_traj * dc.n_outer * dc.ncc * dc.nseg;
     dc.coil_fast = coil_fast;
@@ -370,6 +380,26 @@ bool empty(const DeapodArgs &a) {
     return false;
 }
 
+// Coils per chunk for an image in host memory (pinned, read or written by the kernel over
+// the host link): with coils fastest, 8 coils keep each pixel's 64-byte run in one block;
+// 2-coil chunks (16-byte pieces) made the c2 host-buffer step 25 % slower.
+// The query is skipped while the stream is being captured into a graph (host-buffer calls
+// are never captured).
+int host_min_cc(const void *img, bool coil_fast, int n_coil, cudaStream_t s) {
+    if (!coil_fast) return 1;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return 1;
+    }
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, img) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return at.type == cudaMemoryTypeHost ? std::min(8, n_coil) : 1;
+}
+
 cudaError_t check_blocks(int64_t n) {
     return n > 0x7FFFFFFF ? cudaErrorInvalidConfiguration : cudaSuccess;
 }
@@ -390,7 +420,8 @@ cudaError_t launch_build_tables(int dim, const int m[3], const int nf[3], double
 
 cudaError_t launch_pad(const DeapodArgs &a, const float2 *img, gbn_layout L, float2 *grid, cudaStream_t s) {
     if (empty(a)) return cudaSuccess;
-    const Decomp dc = make_decomp(a, kStageElems - 1, true, true, L.coil_stride < L.elem_stride);
+    const bool cf = L.coil_stride < L.elem_stride;
+    const Decomp dc = make_decomp(a, kStageElems - 1, true, true, cf, host_min_cc(img, cf, a.g.n_coil, s));
     const int64_t nb = dc.nband + dc.nzero;
     if (cudaError_t e = check_blocks(nb)) return e;
     k_pad<ImageSrc><<<(unsigned)nb, kThreads, stage_bytes(dc), s>>>(a, dc, ImageSrc{img, L}, grid);
@@ -399,7 +430,8 @@ cudaError_t launch_pad(const DeapodArgs &a, const float2 *img, gbn_layout L, flo
 
 cudaError_t launch_crop(const DeapodArgs &a, const float2 *grid, float2 *img, gbn_layout L, cudaStream_t s) {
     if (empty(a)) return cudaSuccess;
-    const Decomp dc = make_decomp(a, kStageElems - 1, true, false, L.coil_stride < L.elem_stride);
+    const bool cf = L.coil_stride < L.elem_stride;
+    const Decomp dc = make_decomp(a, kStageElems - 1, true, false, cf, host_min_cc(img, cf, a.g.n_coil, s));
     if (cudaError_t e = check_blocks(dc.nband)) return e;
     k_crop<<<(unsigned)dc.nband, kThreads, stage_bytes(dc), s>>>(a, dc, grid, img, L);
     return cudaGetLastError();
@@ -408,7 +440,8 @@ cudaError_t launch_crop(const DeapodArgs &a, const float2 *grid, float2 *img, gb
 cudaError_t launch_pad_sense(const DeapodArgs &a, const float2 *x, gbn_layout XL, const float2 *sens,
                              gbn_layout SL, float2 *grid, cudaStream_t s) {
     if (empty(a)) return cudaSuccess;
-    const Decomp dc = make_decomp(a, kStageElems - 1, true, true, SL.coil_stride < SL.elem_stride);
+    const bool cf = SL.coil_stride < SL.elem_stride;
+    const Decomp dc = make_decomp(a, kStageElems - 1, true, true, cf, host_min_cc(x, cf, a.g.n_coil, s));
     const int64_t nb = dc.nband + dc.nzero;
     if (cudaError_t e = check_blocks(nb)) return e;
     k_pad<SenseSrc><<<(unsigned)nb, kThreads, stage_bytes(dc), s>>>(a, dc, SenseSrc{x, XL, sens, SL}, grid);
