@@ -359,3 +359,70 @@ def nudft_type2_coord_grad(coords, Fk, shape, grad_c, df=1.0, iflag=1):
             dc = (E * (-s * 1j * ks[d][None, :])) @ F2                         # (m, nt)
             out[a:a + step, d] = np.real(np.conj(g2[a:a + step]) * dc).sum(axis=1) * df
     return out
+
+
+# ---------------------------------------------------------------- exact sums, separable forms
+# The same exact sums as nudft_type1 / nudft_type2, arranged so that full-size checks
+# (millions of samples, 128^3 images) finish in seconds: the phase exp(s i k.x) is the
+# product of one factor per axis, so the sums contract one axis at a time as matrix
+# products instead of forming the (pixels x samples) phase matrix.
+
+def _axis_phase(x, m, s):
+    """exp(s i k x) for the centred frequencies k of one axis: (len(x), m) complex128."""
+    return np.exp(s * 1j * np.multiply.outer(np.asarray(x, dtype=np.float64), freqs(m)))
+
+
+def nudft_type2_at(coords, Fk, shape, samples, df=1.0, iflag=1, chunk=64):
+    """sum_k F_k exp(-s i k.x_j) for the listed sample indices only (exact, FP64).
+    Fk: (*shape, *trail).  Returns (len(samples), *trail)."""
+    s = -1.0 if iflag < 0 else 1.0
+    dim = len(shape)
+    F2, trail = _split(np.asarray(Fk, dtype=np.complex128), dim)
+    nt = F2.shape[-1]
+    idx = np.asarray(samples, dtype=np.int64)
+    xs = [np.asarray(v, dtype=np.float64)[idx] * df for v in coords]
+    out = np.empty((len(idx), nt), dtype=np.complex128)
+    for a in range(0, len(idx), chunk):
+        b = min(a + chunk, len(idx))
+        # last axis: (n, m_last) @ (m_last, rest) with the axis moved to the front
+        E = _axis_phase(xs[dim - 1][a:b], shape[dim - 1], -s)
+        T = np.moveaxis(F2, dim - 1, 0).reshape(shape[dim - 1], -1)
+        T = (E @ T).reshape((b - a,) + tuple(shape[:dim - 1]) + (nt,))
+        for d in range(dim - 2, -1, -1):
+            E = _axis_phase(xs[d][a:b], shape[d], -s)              # (n, m_d)
+            T = np.einsum("n...kc,nk->n...c", T, E)                # contract axis d (the last spatial one left)
+        out[a:b] = T.reshape(b - a, nt)
+    return out.reshape((len(idx),) + trail)
+
+
+def nudft_type1_box(coords, c, shape, pix_axes, df=1.0, iflag=1, chunk=1 << 16):
+    """(1/M) sum_j c_j exp(s i k.x_j) at the pixels of a box: the outer product of the
+    per-axis index lists pix_axes[d] (indices into the image axis d).  Exact, FP64.
+    c: (M, *trail).  Returns (len(pix_axes[0]), ..., *trail)."""
+    s = -1.0 if iflag < 0 else 1.0
+    dim = len(shape)
+    xs = [np.asarray(v, dtype=np.float64).reshape(-1) * df for v in coords]
+    c2, trail = _split(np.asarray(c, dtype=np.complex128), 1)
+    M, nt = c2.shape
+    ks = [freqs(m)[np.asarray(p, dtype=np.int64)] for m, p in zip(shape, pix_axes)]
+    sizes = [len(k) for k in ks]
+    # split the axes into two groups: left = the first half, right = the rest and the coils;
+    # per chunk  out[left, right] += L^T R  with  L[j] = prod of left phases (outer product)
+    # and  R[j] = prod of right phases x c_j, so the (pixels x samples) products run in BLAS
+    h = (dim + 1) // 2
+    out = np.zeros((int(np.prod(sizes[:h])), int(np.prod(sizes[h:])) * nt), dtype=np.complex128)
+    for a in range(0, M, chunk):
+        b = min(a + chunk, M)
+        n = b - a
+        L = np.ones((n, 1), dtype=np.complex128)
+        for d in range(h):
+            Ed = np.exp(s * 1j * np.multiply.outer(xs[d][a:b], ks[d]))
+            L = (L[:, :, None] * Ed[:, None, :]).reshape(n, -1)
+        R = np.ones((n, 1), dtype=np.complex128)
+        for d in range(h, dim):
+            Ed = np.exp(s * 1j * np.multiply.outer(xs[d][a:b], ks[d]))
+            R = (R[:, :, None] * Ed[:, None, :]).reshape(n, -1)
+        R = (R[:, :, None] * c2[a:b][:, None, :]).reshape(n, -1)
+        out += L.T @ R
+    out /= M
+    return out.reshape(tuple(sizes) + trail)
