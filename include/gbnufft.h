@@ -101,6 +101,8 @@ typedef struct {
     int32_t interp_coil_group;
     int64_t dense_subproblems; /* spread subproblems with compensated accumulation */
     int32_t spread_kernels;    /* kernels the plan's last spread launched (0 before one) */
+    int64_t split_tiles;       /* spread tiles shared by several work items (float atomics; 0 means
+                                  the spread is bitwise reproducible run to run) */
 } gbn_plan_info;
 
 /* element strides (in complex64 elements) of a strided complex array */
@@ -130,6 +132,12 @@ int gbn_plan_get_info(const gbn_plan *plan, gbn_plan_info *out);
  * planes) gave up since the last call, which also clears it; else GBN_OK.  No counterpart
  * in the reference (its kernels have no waits). */
 int gbn_plan_status(gbn_plan *plan, gbn_stream_t stream);
+/* Self-test of the path above, no counterpart in the reference: one thread arms an mbarrier
+ * for 16 bytes that never arrive (no copy is issued, so nothing is in flight), waits with
+ * the interp kernels' bounded wait cut to `probes` probes (1 .. 65536, each suspending at
+ * most ~1 us) and, when the wait gives up, sets the status bit those kernels set.  The next
+ * gbn_plan_status then returns GBN_ERR_TIMEOUT and clears it. */
+int gbn_plan_check_wait_expiry(gbn_plan *plan, uint32_t probes, gbn_stream_t stream);
 
 /* Sorts the samples into spatial bins (device coordinates, float32 or float64,
  * x/y/z each of length traj_offsets[n_traj]; unused dims may be NULL).
@@ -283,8 +291,12 @@ int gbn_prox_haar(int32_t dim, const int32_t *shape, int32_t level, int64_t n_ou
  * so nothing is allocated.  Limits: M <= GBN_NOALLOC_MAX_SAMPLES, nspread <= 8, ms % 8 == 0,
  * mt % 16 == 0, grid of at most GBN_NOALLOC_MAX_TILES 16x32 tiles (else GBN_ERR_CAPACITY).
  * All calls share the array: calls that overlap on the GPU race, so order them on one
- * stream.  The first call on a device resolves the array's address; make it before any
- * stream capture. */
+ * stream.  The first call on a device resolves the array's address and, under CUDA's lazy
+ * module loading, is where the driver commits the array's memory on that device (so it can
+ * fail with GBN_ERR_CUDA when the device is full): make it during set-up, before any stream
+ * capture.  The address is kept for the device's primary context; after cudaDeviceReset,
+ * or from a different driver context, it is stale.  A sample with a non-finite coordinate
+ * is left out (it adds nothing to the grid; the plan path reports it as an error instead). */
 #define GBN_NOALLOC_MAX_SAMPLES 262144
 #define GBN_NOALLOC_MAX_TILES 16384
 int gbn_spread2d_noalloc(int coord_dtype, const void *x, const void *y, int64_t M, const void *c,

@@ -19,7 +19,8 @@ GBN_FFT_INVERSE = 1
 # every function the header declares, for the export check in the CPU tests
 EXPORTED = (
     "gbn_version", "gbn_status_string", "gbn_last_error", "gbn_grid_params",
-    "gbn_plan_create", "gbn_plan_destroy", "gbn_plan_get_info", "gbn_plan_status", "gbn_set_points", "gbn_plan_grid",
+    "gbn_plan_create", "gbn_plan_destroy", "gbn_plan_get_info", "gbn_plan_status", "gbn_plan_check_wait_expiry",
+    "gbn_set_points", "gbn_plan_grid",
     "gbn_spread", "gbn_interp", "gbn_fft", "gbn_pad_deapod", "gbn_crop_deapod",
     "gbn_type1", "gbn_type2", "gbn_type21",
     "gbn_sense_forward", "gbn_sense_adjoint", "gbn_sense_normal",
@@ -54,7 +55,7 @@ class PlanInfo(ctypes.Structure):
         ("interp_tile", ctypes.c_int32 * 3), ("coil_group", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("interp_threads", ctypes.c_int32), ("max_subproblem", ctypes.c_int32), ("device_bytes", ctypes.c_int64),
         ("interp_coil_group", ctypes.c_int32), ("dense_subproblems", ctypes.c_int64),
-        ("spread_kernels", ctypes.c_int32),
+        ("spread_kernels", ctypes.c_int32), ("split_tiles", ctypes.c_int64),
     ]
 
 
@@ -94,6 +95,7 @@ def _declare(lib):
         "gbn_plan_destroy": ([_vp], _i32),
         "gbn_plan_get_info": ([_vp, P(PlanInfo)], _i32),
         "gbn_plan_status": ([_vp, _vp], _i32),
+        "gbn_plan_check_wait_expiry": ([_vp, ctypes.c_uint32, _vp], _i32),
         "gbn_set_points": ([_vp, _i32, _vp, _vp, _vp, P(_i64), _vp], _i32),
         "gbn_plan_grid": ([_vp], _vp),
         "gbn_spread": ([_vp, _vp, Layout, _vp, _vp], _i32),

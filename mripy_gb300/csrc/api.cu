@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "tma.cuh"
 
 using namespace gbn;
 
@@ -232,6 +233,7 @@ DeapodArgs deapod_args(const gbn_plan *p, bool with_group_scale) {
 }
 
 int fft_exec(gbn_plan *p, float2 *grid, int direction, cudaStream_t s) {
+    NvtxRange range("gbn fft");
     if (!p->fft_ok) return fail(GBN_ERR_STATE, "no FFT plan");
     GBN_FFT(cufftSetStream(p->fft, s));
     GBN_FFT(cufftExecC2C(p->fft, (cufftComplex *)grid, (cufftComplex *)grid,
@@ -249,6 +251,7 @@ int dir_type1(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_FORWARD : 
 int dir_type2(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_INVERSE : GBN_FFT_FORWARD; }
 
 int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, float2 *grid, cudaStream_t s) {
+    NvtxRange range("gbn spread");
     // tiles covered by several work items start from zero; when they are most of the grid
     // (dense trajectories), one memset of the whole grid is cheaper than per-tile blocks
     const bool memset_grid = 2 * p->n_split > (int64_t)p->gs.ntiles * p->gs.n_traj;
@@ -372,6 +375,7 @@ bool grid_tensor_map3d(gbn_plan *p, const float2 *grid, int cg, int BY, int BZ) 
 }
 
 int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const float *weight, cudaStream_t s) {
+    NvtxRange range("gbn interp");
     InterpArgs a;
     a.g = p->gi;
     a.subs = p->interp_subs.as<int4>();
@@ -474,6 +478,7 @@ __global__ void k_iota(uint32_t *v, int64_t n) {
 
 int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const void *z, const int64_t *off,
                     cudaStream_t s) {
+    NvtxRange range("gbn set_points");
     GBN_TRY(check_plan(p, false));
     const int nt = p->desc.n_traj;
     if (!off) return fail(GBN_ERR_ARG, "traj_offsets is null");
@@ -858,6 +863,30 @@ int gbn_plan_status(gbn_plan *p, gbn_stream_t stream) {
     return fail(GBN_ERR_TIMEOUT, "status word " + std::to_string(st) + ": a TMA window wait gave up");
 }
 
+}  // extern "C"
+
+namespace {
+// the bounded-wait self-test kernel: an mbarrier armed for bytes no copy will deliver
+__global__ void k_wait_selftest(uint32_t probes, uint32_t *status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    gbn::mbar_init(&bar, 1);
+    gbn::fence_barrier_init();
+    gbn::mbar_arrive_expect_tx(&bar, 16);
+    if (!gbn::mbar_wait_bounded(&bar, 0, probes)) atomicOr(status, gbn::kStatusTmaTimeout);
+}
+}  // namespace
+
+extern "C" {
+
+int gbn_plan_check_wait_expiry(gbn_plan *p, uint32_t probes, gbn_stream_t stream) {
+    if (!p) return fail(GBN_ERR_ARG, "null plan");
+    if (probes < 1 || probes > 65536) return fail(GBN_ERR_ARG, "probes must be in 1 .. 65536");
+    k_wait_selftest<<<1, 32, 0, (cudaStream_t)stream>>>(probes, p->kstatus);
+    GBN_CUDA(cudaGetLastError());
+    return GBN_OK;
+}
+
 int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     if (!p || !o) return fail(GBN_ERR_ARG, "null argument");
     std::memset(o, 0, sizeof(*o));
@@ -881,6 +910,7 @@ int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     o->interp_coil_group = interp_cg(p);
     o->dense_subproblems = p->n_dense_sub;
     o->spread_kernels = p->spread_kernels;
+    o->split_tiles = p->n_split;
     o->device_bytes = (int64_t)p->device_bytes;
     return GBN_OK;
 }

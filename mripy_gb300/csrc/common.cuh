@@ -14,9 +14,20 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <nvtx3/nvToolsExt.h>  // header-only NVTX v3: stage ranges on a profiler's timeline
+
 #include "../../include/gbnufft.h"
 
 namespace gbn {
+
+// NVTX range around one host-side stage (set_points, pad, FFT, interp, spread, crop): the
+// stages show on a profiler's timeline; a few nanoseconds when no tool is attached
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 constexpr int kMaxW = 40;          // 2*nspread; nspread <= 20 (eps down to 1e-33 in 2-D gives 17)
 constexpr int kSplitFlag = 1;      // tile is covered by more than one subproblem

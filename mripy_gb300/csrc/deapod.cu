@@ -419,6 +419,7 @@ cudaError_t launch_build_tables(int dim, const int m[3], const int nf[3], double
 }
 
 cudaError_t launch_pad(const DeapodArgs &a, const float2 *img, gbn_layout L, float2 *grid, cudaStream_t s) {
+    NvtxRange range("gbn pad");
     if (empty(a)) return cudaSuccess;
     const bool cf = L.coil_stride < L.elem_stride;
     const Decomp dc = make_decomp(a, kStageElems - 1, true, true, cf, host_min_cc(img, cf, a.g.n_coil, s));
@@ -429,6 +430,7 @@ cudaError_t launch_pad(const DeapodArgs &a, const float2 *img, gbn_layout L, flo
 }
 
 cudaError_t launch_crop(const DeapodArgs &a, const float2 *grid, float2 *img, gbn_layout L, cudaStream_t s) {
+    NvtxRange range("gbn crop");
     if (empty(a)) return cudaSuccess;
     const bool cf = L.coil_stride < L.elem_stride;
     const Decomp dc = make_decomp(a, kStageElems - 1, true, false, cf, host_min_cc(img, cf, a.g.n_coil, s));
@@ -439,6 +441,7 @@ cudaError_t launch_crop(const DeapodArgs &a, const float2 *grid, float2 *img, gb
 
 cudaError_t launch_pad_sense(const DeapodArgs &a, const float2 *x, gbn_layout XL, const float2 *sens,
                              gbn_layout SL, float2 *grid, cudaStream_t s) {
+    NvtxRange range("gbn pad (SENSE)");
     if (empty(a)) return cudaSuccess;
     const bool cf = SL.coil_stride < SL.elem_stride;
     const Decomp dc = make_decomp(a, kStageElems - 1, true, true, cf, host_min_cc(x, cf, a.g.n_coil, s));
@@ -450,6 +453,7 @@ cudaError_t launch_pad_sense(const DeapodArgs &a, const float2 *x, gbn_layout XL
 
 cudaError_t launch_crop_sense(const DeapodArgs &a, const float2 *grid, const float2 *sens, gbn_layout SL,
                               float2 *x, gbn_layout XL, cudaStream_t s) {
+    NvtxRange range("gbn crop (SENSE)");
     if (empty(a)) return cudaSuccess;
     const Decomp dc = make_decomp(a, kSenseSeg, false, false, false);
     if (cudaError_t e = check_blocks(dc.nband)) return e;

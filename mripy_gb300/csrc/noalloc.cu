@@ -24,12 +24,17 @@
 //
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current (host code must not pass the symbol
-// itself: on the host it is only a stand-in, not a device address).  Make that first call
-// before any stream capture.
+// itself: on the host it is only a stand-in, not a device address), and keeps it for the
+// life of the process.  Under CUDA's lazy module loading that first call is also where the
+// driver commits the array's memory on the device, so it can fail for lack of memory: make
+// it during set-up, before any stream capture.  The kept address belongs to the device's
+// primary context (the runtime's); after cudaDeviceReset, or from another driver context
+// on the same device, it is stale, so such callers must not use this entry point.
 //
 // Non-finite coordinates are not reported here (that would need a host synchronisation);
-// such samples are binned at cell 0.  The result matches gbn_spread on the same inputs up to
-// FP32 summation order.
+// a sample with a non-finite coordinate is left out: it reaches no tile and adds nothing
+// to the grid.  The result matches gbn_spread on the same (finite) inputs up to FP32
+// summation order.
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -99,7 +104,9 @@ struct NaGeom {
     double df;
 };
 
-// per sample: packed record (same format as the plan's) and the per-tile counts
+// per sample: packed record (same format as the plan's) and the per-tile counts.  A sample
+// with a non-finite coordinate gets the record's z slot set to 1 (unused in 2-D, else 0)
+// and is counted in no tile, so the scatter lists it nowhere and the spread never reads it.
 template <typename T>
 __global__ void k_na_prep(const T *__restrict__ x, const T *__restrict__ y, NaGeom g, float4 *__restrict__ pts,
                           uint32_t *__restrict__ count) {
@@ -111,7 +118,10 @@ __global__ void k_na_prep(const T *__restrict__ x, const T *__restrict__ y, NaGe
     int c0[2] = {0, 0};
     for (int d = 0; d < 2; ++d) {
         const double xs = (double)src[d][j] * g.df;
-        if (!isfinite(xs)) continue;
+        if (!isfinite(xs)) {
+            pts[j] = make_float4(0.f, 0.f, 1.f, 0.f);
+            return;
+        }
         const double h = kTwoPiNa / nf[d];
         const double xi = na_py_mod(xs, kTwoPiNa);
         const int64_t m = 1 + (int64_t)na_py_floordiv(xi, h);
@@ -173,7 +183,11 @@ __device__ void na_block_scan(const uint32_t *in, uint32_t *out, int n, uint32_t
 __device__ uint32_t na_identity(uint32_t v) { return v; }
 __device__ uint32_t na_nsub(uint32_t v) { return v == 0 ? 1u : (v + kNaMaxSub - 1) / kNaMaxSub; }
 
-// tile offsets, cleared cursors and the work table; meta[0] = number of work items
+// tile offsets, cleared cursors and the work table; meta[0] = number of work items.
+// One block of 1024 threads does it all: each thread scans up to 16 tile counts, and the
+// thread of a tile writes that tile's work items one by one (up to M / 256 for a tile that
+// holds every sample).  Serial work, but small next to the spread, and it needs no second
+// launch or grid-wide synchronisation.
 __global__ void __launch_bounds__(1024) k_na_layout(int ntiles, uint32_t *__restrict__ count,
                                                     uint32_t *__restrict__ tile_off, uint32_t *__restrict__ sub_off,
                                                     uint32_t *__restrict__ cursor, int4 *__restrict__ subs,
@@ -199,8 +213,10 @@ __global__ void k_na_scatter(NaGeom g, const float4 *__restrict__ pts, const uin
                              uint32_t *__restrict__ cursor, uint32_t *__restrict__ idx) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= g.M) return;
+    const float4 p = pts[j];
+    if (p.z != 0.f) return;  // non-finite coordinate: in no tile
     int c0x, c0y, c0z;
-    unpack_cells(2, __float_as_uint(pts[j].w), c0x, c0y, c0z);
+    unpack_cells(2, __float_as_uint(p.w), c0x, c0y, c0z);
     const int n0 = touched_tiles(c0x, g.W, g.nf0, kNaTX, g.nt0);
     const int n1 = touched_tiles(c0y, g.W, g.nf1, kNaTY, g.nt1);
     for (int a = 0; a < n0; ++a)

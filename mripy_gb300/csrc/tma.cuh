@@ -42,10 +42,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// bounded wait for the phase with the given parity to complete: at most kTmaWaitLimit
-// suspended probes of ~kTmaSuspendNs each (about two seconds in all)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kTmaWaitLimit; ++i)
+// bounded wait for the phase with the given parity to complete: at most `limit` suspended
+// probes of ~kTmaSuspendNs each (kTmaWaitLimit: about two seconds in all)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t limit = kTmaWaitLimit) {
+    for (uint32_t i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -131,9 +131,11 @@ def espirit_nd(xcrop, x_shape, nsingularv=150, hkwin_shape=(16, 16), pad_before_
         vim = _ft_backward(_pad_center(_ft_forward(vim, dims), full), dims)
         sim = _ft_backward(_pad_center(_ft_forward(sim, dims), full), dims)
     vim = vim / (1e-6 + torch.linalg.vector_norm(vim, dim=d, keepdim=True))
-    sim = sim.real
-    sim = sim / sim.max()
-    vim = torch.where((sim < sigv_th)[..., None], torch.zeros((), dtype=vim.dtype, device=vim.device), vim)
+    # sim / max(sim) on the complex map as numpy evaluates it (espirit_func.py:95, 212):
+    # the divisor is the element of largest real part; the threshold compares real parts
+    flat = sim.reshape(-1)
+    sim = sim / flat[torch.argmax(flat.real)]
+    vim = torch.where((sim.real < sigv_th)[..., None], torch.zeros((), dtype=vim.dtype, device=vim.device), vim)
     sim = sim.abs()
     if was_np:
         vim, sim = vim.cpu().numpy().astype(np.complex128), sim.cpu().numpy().astype(np.float64)

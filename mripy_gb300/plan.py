@@ -171,12 +171,18 @@ class NufftPlan:
             "threads": inf.threads, "interp_threads": inf.interp_threads, "max_subproblem": inf.max_subproblem,
             "device_bytes": inf.device_bytes, "interp_coil_group": inf.interp_coil_group,
             "dense_subproblems": inf.dense_subproblems,
-            "spread_kernels": inf.spread_kernels,
+            "spread_kernels": inf.spread_kernels, "split_tiles": inf.split_tiles,
         }
 
     def status(self, stream=None):
         """Synchronise and raise GbnError(GBN_ERR_TIMEOUT) if a kernel's bounded wait gave up."""
         N.check(self._lib.gbn_plan_status(self._h, _stream(stream)))
+
+    def check_wait_expiry(self, probes=64, stream=None):
+        """Self-test of the bounded-wait status path: a one-thread kernel waits for bytes that
+        never arrive, gives up after ``probes`` probes and sets the plan's timeout bit (read
+        and cleared by ``status()``)."""
+        N.check(self._lib.gbn_plan_check_wait_expiry(self._h, int(probes), _stream(stream)))
 
     def grid(self):
         """The plan's oversampled grid buffer as a (n_traj*n_coil, *nf) complex64 view."""

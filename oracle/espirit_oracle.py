@@ -17,16 +17,19 @@ they call:
                       ifftshift
 * ``espirit``         the whole function
 
-The reference cannot run as written on this interpreter (np.int, map objects inside np.ix_,
-and espirit_2d's threshold reads ``nsing_th``, which is undefined); the restatement follows
-espirit_3d's ``nsigv_th`` in both.  Kept as in the reference: the kept count is the LAST
+The reference does not run as written on Python 3 with numpy 2 (np.int, map objects inside
+np.ix_), and espirit_2d's threshold reads ``nsing_th``, which is undefined; the restatement
+follows espirit_3d's ``nsigv_th`` in both.  Kept as in the reference: the kept count is the LAST
 index k with s[k] > s[0] * nsigv_th (so one fewer than the singular values above it).
-Deviations: the eigenvector phase is canonical (the first coil with a non-zero component
-made real and non-negative) where the reference keeps LAPACK's arbitrary per-pixel phase;
-after the FFT resampling the eigenvalue map is complex, and its real part is normalised and
-thresholded.  Parity of this restatement is pinned by its properties on synthetic data with
-known coil maps (``tests/test_espirit_oracle.py``): the maps it returns equal the true maps
-up to one phase per pixel inside the object.
+Deviation: the eigenvector phase is canonical (the first coil with a non-zero component
+made real and non-negative) where the reference keeps LAPACK's arbitrary per-pixel phase.
+Parity is pinned against the reference's own outputs (``tests/golden/golden_espirit.npz``,
+made by ``tests/golden/make_golden_solvers.py`` from espirit_func.py itself): the
+eigenvalue maps agree to rounding, and the coil maps agree up to one phase per pixel
+wherever no FFT resampling follows the eigen step (resampling maps of arbitrary per-pixel
+phase, as the reference does with pad_before_espirit = 0 and a smaller calibration grid,
+gives phase-dependent values there).  ``tests/test_espirit_oracle.py`` also checks the
+recovery of known coil maps.
 """
 import numpy as np
 
@@ -122,9 +125,17 @@ def espirit(xcrop, x_shape, nsingularv=150, hkwin_shape=(16, 16), pad_before_esp
         Vim = ft_backward(pad_center(ft_forward(Vim, axes), x_shape[:d]), axes)
         sim = ft_backward(pad_center(ft_forward(sim, axes), x_shape[:d]), axes)
     Vim = Vim / (1e-6 + np.linalg.norm(Vim, axis=d))[..., None]
-    sim = np.real(sim)
-    sim = sim / np.max(sim)
-    Vim[sim < sigv_th] = 0
+    sim = normalise_eigenvalues(sim)
+    Vim[np.real(sim) < sigv_th] = 0
     if return_info:
         return Vim, np.abs(sim), {"nsv": nsv, "singular_values": s}
     return Vim, np.abs(sim)
+
+
+def normalise_eigenvalues(sim):
+    """sim / max(sim) as espirit_func.py:95 / 212 evaluates it on the complex map: numpy
+    orders complex numbers by real part (then imaginary part), so the divisor is the
+    element of largest real part, imaginary part and all; the threshold that follows
+    (sim < sigv_th) compares real parts the same way."""
+    flat = np.asarray(sim, dtype=np.complex128).reshape(-1)
+    return sim / flat[np.lexsort((flat.imag, flat.real))[-1]]

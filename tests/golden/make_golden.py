@@ -20,7 +20,8 @@ are registered before the import:
   (``normalise_idft=True``), like ``numpy.fft.ifftn``.
 * ``matplotlib`` and ``pywt``: no-op modules (plotting and wavelets only).
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py /path/to/mripy
+        (or set MRIPY_REFERENCE to the checkout's root and omit the argument)
 """
 import os
 import sys
@@ -82,6 +83,14 @@ def _install_stubs():
     sys.modules["pyfftw.interfaces.cache"] = cache
 
     sys.modules["pywt"] = types.ModuleType("pywt")
+
+
+def reference_root():
+    """The mripy checkout to run: the first command-line argument, else $MRIPY_REFERENCE."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MRIPY_REFERENCE")
+    if not root or not os.path.isdir(os.path.join(root, "fft")):
+        sys.exit("usage: %s /path/to/mripy  (or set MRIPY_REFERENCE)" % os.path.basename(sys.argv[0]))
+    return root
 
 
 def load_reference(ref_root):
@@ -211,7 +220,7 @@ def make_3d(nft, opc):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = reference_root()
     nft, opc = load_reference(ref_root)
     for name, data in (("golden_1d.npz", make_1d(nft)),
                        ("golden_2d.npz", make_2d(nft)),
