@@ -83,6 +83,7 @@ struct gbn_plan {
     Geom gs{}, gi{};
     int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256, interp_coil_group = 0;
     int interp_staging = 0;  // 0: tensor copies where the grid allows, 1: thread loads
+    int spread_variant = 0;  // 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes
     int dense_min = kDenseDefault;  // 3-D spread tiles with this many samples use compensated sums (0: never)
     int64_t n_dense_sub = 0;
     int64_t n_split = 0;  // spread tiles covered by more than one subproblem (listed in split_tiles)
@@ -270,6 +271,8 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
     a.weight = weight;
     a.grid = grid;
     a.any_dense = p->n_dense_sub > 0 ? 1 : 0;
+    a.variant = p->spread_variant;
+    a.status = p->kstatus;
     int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
     while (cg > 1 && spread_smem_bytes(p->gs, cg) > smem_budget(p)) cg /= 2;
     if (spread_smem_bytes(p->gs, cg) > (size_t)p->smem_optin)
@@ -698,6 +701,11 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         return fail(GBN_ERR_ARG, "interp_staging must be 0 or 1");
     }
     p->interp_staging = desc->interp_staging;
+    if (desc->spread_variant < 0 || desc->spread_variant > 2) {
+        delete p;
+        return fail(GBN_ERR_ARG, "spread_variant must be 0, 1 or 2");
+    }
+    p->spread_variant = desc->spread_variant;
     p->dense_min = desc->dense_tile_samples > 0 ? desc->dense_tile_samples
                                                 : (desc->dense_tile_samples < 0 ? 0 : kDenseDefault);
     p->threads = desc->threads > 0 ? desc->threads : 256;
@@ -860,7 +868,9 @@ int gbn_plan_status(gbn_plan *p, gbn_stream_t stream) {
     GBN_CUDA(cudaMemcpy(&st, p->kstatus, sizeof(st), cudaMemcpyDeviceToHost));
     if (st == 0) return GBN_OK;
     GBN_CUDA(cudaMemset(p->kstatus, 0, sizeof(uint32_t)));
-    return fail(GBN_ERR_TIMEOUT, "status word " + std::to_string(st) + ": a TMA window wait gave up");
+    return fail(GBN_ERR_TIMEOUT, "status word " + std::to_string(st) +
+                                     ": a bounded wait gave up (bit 2: an interp tensor copy, bit 4: the 3-D spread's "
+                                     "batch ring)");
 }
 
 }  // extern "C"

@@ -128,6 +128,8 @@ struct SpreadArgs {
     const float *weight;      // per sample (original index) or null: density compensation
     float2 *grid;
     int any_dense;            // some subproblems carry kDenseFlag (compensated accumulation)
+    int variant;              // 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes (gbn_plan_desc)
+    uint32_t *status;         // the plan's status word (bounded waits of the cube kernel)
 };
 struct InterpArgs {
     Geom g;

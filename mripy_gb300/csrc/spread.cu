@@ -7,6 +7,9 @@
 #include "dispatch.cuh"
 #include "grid2d_kernels.cuh"
 #include "grid3d_kernels.cuh"
+#include "spread3d_cube.cuh"
+
+#include <algorithm>
 
 namespace gbn {
 
@@ -40,9 +43,56 @@ static bool reg3d_path(const Geom &g, int coil_group, int threads) {
            g.tile[0] * g.tile[1] == kRegRows * (threads / 32) && g.tile[2] == kRegCols * (32 / coil_group);
 }
 
+// the cube kernel applies: 3-D, 8 coils per block, a tile of 8 or 16 cubes of 4^3 cells;
+// returns its consumer warps (0 where it does not apply or the caller did not choose it)
+static int cube_path(const Geom &g, int coil_group, int variant) {
+    if (variant != 2 || !grid3d_applies(g) || coil_group != 8) return 0;
+    for (int nwc : {8, 16})
+        if (cube_tile_ok(g.tile, nwc)) return nwc;
+    return 0;
+}
+
 int spread_kernel_count(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads) {
     if (n_sub == 0) return 0;
-    return (reg3d_path(a.g, coil_group, threads) && a.any_dense) ? 2 : 1;
+    const bool two = cube_path(a.g, coil_group, a.variant) || reg3d_path(a.g, coil_group, threads);
+    return (two && a.any_dense) ? 2 : 1;
+}
+
+static int device_sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// persistent cube kernel: as many blocks as fit on the GPU at once (at most one per unit),
+// each walking units blockIdx.x, blockIdx.x + gridDim.x, ...
+template <int WT, int NWC, bool KAHAN>
+static cudaError_t launch_cube_instance(const SpreadArgs &a, int64_t n_units, int n_cg, cudaStream_t s) {
+    const CubeLayout L = cube_layout(a.g.tile, NWC);
+    const int threads = (NWC + kCubeProducers) * 32;
+    const int vec = ((uintptr_t)a.grid % 16 == 0) && (a.g.nf[2] % 2 == 0);
+    auto kern = k_spread3d_cube<WT, NWC, KAHAN>;
+    cudaError_t e = set_smem(kern, L.bytes);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, L.bytes);
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = std::min<int64_t>(n_units, (int64_t)std::max(per_sm, 1) * device_sm_count());
+    kern<<<(unsigned)blocks, threads, L.bytes, s>>>(a, a.status, vec, n_units, n_cg);
+    return cudaGetLastError();
+}
+
+template <int WT, int NWC>
+static cudaError_t launch_cube(const SpreadArgs &a, int64_t n_sub, cudaStream_t s) {
+    const int n_cg = (a.g.n_coil + 7) / 8;
+    const int64_t n_units = n_sub * n_cg;
+    cudaError_t e = launch_cube_instance<WT, NWC, false>(a, n_units, n_cg, s);
+    if (e == cudaSuccess && a.any_dense) e = launch_cube_instance<WT, NWC, true>(a, n_units, n_cg, s);
+    return e;
 }
 
 cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads, cudaStream_t s) {
@@ -74,6 +124,13 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
                 err = cudaGetLastError();
             }
         }));
+        return err;
+    }
+    // 3-D cube kernel (8 coils per block): plain sums, then (if any) compensated ones
+    if (const int nwc = cube_path(a.g, coil_group, a.variant)) {
+        GBN_DISPATCH_W(a.g.W, {
+            err = nwc == 16 ? launch_cube<WT, 16>(a, n_sub, s) : launch_cube<WT, 8>(a, n_sub, s);
+        });
         return err;
     }
     // 3-D register-tile kernel

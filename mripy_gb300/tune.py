@@ -22,28 +22,32 @@ _CACHE = {}
 
 
 def _spread_candidates(dim, n_coil):
-    """(tile, threads, coil_group) triples: the register-tile kernels' own tiles (rows of 4
-    per warp, 4 columns per lane) for 4 and 8 coils per block, plus shared-memory tiles."""
+    """(tile, threads, coil_group, spread_variant) tuples: the register-tile kernels' own
+    tiles (rows of 4 per warp, 4 columns per lane) for 4 and 8 coils per block, in 3-D with 8
+    coils also the cube kernel's tiles (8 or 16 cubes of 4^3 cells), plus shared-memory tiles."""
     out = []
     groups = [cg for cg in (8, 4) if n_coil >= cg]
     if dim == 2:
         for cg in groups:
             for th in (128, 256):
-                out.append(((4 * th // 32, 4 * 32 // cg), th, cg))
-        out += [((16, 32), 256, 8), ((32, 32), 256, 8)]
+                out.append(((4 * th // 32, 4 * 32 // cg), th, cg, 0))
+        out += [((16, 32), 256, 8, 0), ((32, 32), 256, 8, 0)]
         if n_coil < 4:
             # one-coil plans (the plain per-instance path): 128-thread blocks measured best
-            out += [((16, 32), 128, 8), ((32, 32), 128, 8)]
+            out += [((16, 32), 128, 8, 0), ((32, 32), 128, 8, 0)]
     elif dim == 3:
         for cg in groups:
             for th in (128, 256):
                 rows = 4 * th // 32
                 for ty in (4, 8, 16):
                     if rows % ty == 0:
-                        out.append(((rows // ty, ty, 4 * 32 // cg), th, cg))
-        out += [((8, 8, 32), 256, 8)]
+                        out.append(((rows // ty, ty, 4 * 32 // cg), th, cg, 1 if cg == 8 else 0))
+        if n_coil >= 8:
+            for tile in ((8, 8, 8), (4, 8, 16), (8, 8, 16), (16, 8, 8)):
+                out.append((tile, 256, 8, 2))
+        out += [((8, 8, 32), 256, 8, 0)]
     else:
-        out = [((t,), 256, 8) for t in (1024, 512, 2048)]
+        out = [((t,), 256, 8, 0) for t in (1024, 512, 2048)]
     return out
 
 
@@ -59,7 +63,8 @@ def candidate_tunings(dim, n_coil):
     """Every configuration the search below can time: the spread candidates, then the interp
     ones (each with the other kernel at library defaults)."""
     _, interp_c = _candidates(dim)
-    out = [Tuning(spread_tile=t, threads=th, coil_group=cg) for t, th, cg in _spread_candidates(dim, n_coil)]
+    out = [Tuning(spread_tile=t, threads=th, coil_group=cg, spread_variant=v)
+           for t, th, cg, v in _spread_candidates(dim, n_coil)]
     out += [Tuning(interp_tile=t, interp_threads=th, interp_coil_group=cg)
             for t in interp_c for th in _interp_threads(dim) for cg in _interp_coil_groups(n_coil)]
     return out
@@ -144,16 +149,18 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
     _, interp_c = _candidates(dim)
     best_s = best_i = None
     # spread tiling (interp at default), then interp tiling (spread at the winner)
-    for tile, th, cg in _spread_candidates(dim, n_coil):
-        tu = Tuning(spread_tile=tile, threads=th, coil_group=cg)
+    for tile, th, cg, var in _spread_candidates(dim, n_coil):
+        # the cube kernel needs long work items to keep its ring full: time it at 4096
+        tu = Tuning(spread_tile=tile, threads=th, coil_group=cg, spread_variant=var,
+                    max_subproblem=4096 if var == 2 else 0)
         try:
             t_s, _ = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
         except Exception:
             continue
         if verbose:
-            print("spread", tile, th, cg, t_s)
+            print("spread", tile, th, cg, var, t_s)
         if best_s is None or t_s < best_s[0]:
-            best_s = (t_s, tile, th, cg)
+            best_s = (t_s, tile, th, cg, var)
     icg = _interp_coil_groups(n_coil)
     for tile in interp_c:
         for th in _interp_threads(dim):
@@ -170,9 +177,10 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
     if best_s is None or best_i is None:
         raise RuntimeError("no tuning candidate ran")
     best = None
-    for ms in (64, 128, 256, 512):
+    for ms in ((1024, 2048, 4096, 8192) if best_s[4] == 2 else (64, 128, 256, 512, 1024)):
         tu = Tuning(spread_tile=best_s[1], threads=best_s[2], coil_group=best_s[3], interp_tile=best_i[1],
-                    interp_threads=best_i[2], interp_coil_group=best_i[3], max_subproblem=ms)
+                    interp_threads=best_i[2], interp_coil_group=best_i[3], max_subproblem=ms,
+                    spread_variant=best_s[4])
         t_s, t_i = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
         if verbose:
             print("max_subproblem", ms, t_s + t_i)
@@ -188,7 +196,7 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
         stored[key] = {"spread_tile": list(tuning.spread_tile), "interp_tile": list(tuning.interp_tile),
                        "max_subproblem": tuning.max_subproblem, "coil_group": tuning.coil_group,
                        "threads": tuning.threads, "interp_threads": tuning.interp_threads,
-                       "interp_coil_group": tuning.interp_coil_group}
+                       "interp_coil_group": tuning.interp_coil_group, "spread_variant": tuning.spread_variant}
         with open(cache_file, "w") as f:
             json.dump(stored, f, indent=1)
     return tuning
