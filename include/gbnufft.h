@@ -79,9 +79,11 @@ typedef struct {
     int32_t dense_tile_samples; /* 3-D spread: tiles with at least this many samples (the
                                    k-space centre of radial data) accumulate with Kahan-
                                    compensated FP32 sums; 0 = 32768, negative = never */
-    int32_t spread_variant;     /* 3-D spread with 8 coils per block: 0 = library choice,
-                                   1 = warp rows (tile (4 x warps / TY, TY, 16)), 2 = 4^3-cell
-                                   cubes fed by producer warps (tile of 8 or 16 cubes) */
+    int32_t spread_variant;     /* 3-D spread with 8 coils per block: 0 = library choice
+                                   (cubes on the default 8^3 tile, warp rows on a caller's
+                                   tile), 1 = warp rows (tile (4 x warps / TY, TY, 16)),
+                                   2 = 4^3-cell cubes fed by producer warps (tile of 8 or 16
+                                   cubes; default work items of 4096 samples) */
 } gbn_plan_desc;
 
 typedef struct {

@@ -1,5 +1,5 @@
 // 3-D spread (type-1 gridding) with 8 coils per block: cubic register footprints fed by
-// producer warps through an mbarrier ring, in persistent blocks.
+// producer warps through an mbarrier ring.
 //
 // Output-stationary like k_spread3d_reg: a work item owns one output tile (or a slice of a
 // dense tile's samples) and every output cell is summed by one thread, in the sample order.
@@ -11,19 +11,21 @@
 // k_spread3d_reg.
 //
 // Staging is decoupled from the arithmetic.  The block walks a fixed sequence of (work
-// item, coil group) units -- block b takes units b, b + gridDim.x, ... -- and numbers their
-// 32-sample batches consecutively.  Batch t goes to slot t % kCubeSlots of a ring in shared
-// memory and is filled by producer warp t % kCubeProducers: sample records, the separable
+// item, coil group) units -- block b takes units b, b + gridDim.x, ...; the launcher gives
+// one unit per block -- and numbers their 32-sample batches consecutively.  Batch t goes to
+// slot t % kCubeSlots of a ring in shared memory and is filled by producer warp
+// t % kCubeProducers: sample records, the separable
 // weights of every tile plane / row / column in FP32, the 8 coil values times the optional
 // density weight, and for every consumer warp the ordered list of the batch's samples whose
 // stencil reaches its cube, built by ballots.  The producer waits on the slot's `empty`
 // mbarrier until every consumer lane has released the slot's previous batch, and arrives on
 // `full` when its writes are done.  Consumer warps walk the same sequence: wait on `full`,
 // run their own list, arrive on `empty`; after a unit's last batch they write their cube
-// and start the next unit from zero.  Cubes of one tile get unequal shares of its samples
-// (a tile's samples cluster on one side), so within one unit some consumer warps finish
-// early; the ring (8 batches) lets them run ahead into the next unit instead of idling, and
-// no block-wide barrier runs after the set-up.
+// and start the next unit from zero.  No block-wide barrier runs after the set-up: a
+// consumer warp with a long list in one batch is evened out by short lists in the next
+// seven.  (Cubes of one tile also get unequal shares of its samples over a whole unit -- a
+// tile's samples cluster on one side -- which the ring cannot absorb; on the 3-D radial
+// workload the cube warps' work per tile is 84 % balanced.)
 //
 // Every wait is bounded (kTmaWaitLimit probes of ~1 us); a wait that gives up sets
 // kStatusSpreadTimeout in the plan's status word and goes on with the slot as it is, so no

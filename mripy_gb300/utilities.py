@@ -28,3 +28,28 @@ def scaling(b):
         # numpy orders complex numbers lexicographically (real part, then imaginary)
         return flat[np.lexsort((flat.imag, flat.real))[-1]]
     return flat.max()
+
+
+def universal_threshold(im, axes=None):
+    """Wavelet soft threshold from the data's own noise level: Donoho and Johnstone's
+    universal threshold sigma * sqrt(2 ln N) (Biometrika 81:425, 1994), with sigma the
+    median absolute finest-scale diagonal Haar detail coefficient / 0.6745 (over real and
+    imaginary parts) and N the pixel count.  For an IST/FISTA solve on data scaled by
+    ``optscaling``, ``im`` is the scaled adjoint image; the result is used as ``th``.
+    mripy takes ``th`` as a fixed number (examples/pics_IST_3dute_wavelet_L1.py:94); this
+    helper only chooses one for data whose noise level differs from that example's."""
+    from .solvers import DWTnd
+    t = im if isinstance(im, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(np.asarray(im)))
+    t = t.to("cuda", torch.complex64)
+    axes = tuple(range(min(t.dim(), 3))) if axes is None else tuple(axes)
+    c = DWTnd("haar", level=1, axes=axes).backward(t)
+    sl = [slice(None)] * c.dim()
+    for a in axes:
+        sl[a] = slice(c.shape[a] // 2, None)
+    d = c[tuple(sl)].reshape(-1)
+    parts = torch.cat([d.real, d.imag]).abs()
+    sigma = float(parts.median()) / 0.6745
+    n = 1
+    for a in axes:
+        n *= int(t.shape[a])
+    return sigma * float(np.sqrt(2.0 * np.log(n)))

@@ -174,3 +174,42 @@ def test_fista_haar_3d_matches_fp64_iterates():
         yv = xx + ((t[it] - 1) / t[it + 1]) * (xx - x_pre)
         x_pre = xx
     assert rel(xg, xx) < 1e-3
+
+
+def test_ist_haar_3d_optscaled_matches_fp64_iterates():
+    """The C4 solve's recipe at 32^3: data divided by optscaling (max |A^H y|,
+    utilities/utilities_func.py:381-383) as examples/pics_IST_3dute_wavelet_L1.py:79-80 does,
+    then IST_wrap with DWTnd('haar', 4), step 0.1, th 0.06; the GPU iterates follow the FP64
+    restatement with the oracle operators (IST_32, CS_MRI_solvers_func.py:75-86)."""
+    from mripy_gb300.utilities import optscaling
+    rng = np.random.default_rng(34)
+    n, nc, it = 32, 2, 10
+    shape = (n, n, n)
+    kk = synth.centre_out_radial_3d(1250, n)
+    dcf = np.maximum(np.sqrt(kk[0] ** 2 + kk[1] ** 2 + kk[2] ** 2), 1e-3) ** 2
+    dcf = dcf / dcf.mean()
+    S = synth.coil_maps(shape, nc, rng)
+    x = synth.ellipsoid_phantom(n, rng)
+    op64 = O.NUFFT3dOracle(shape, dcf)
+    op64.normalize_set_ktraj(np.stack(kk))
+    y = op64.forward((x[..., None] * S).astype(np.complex128))
+    y = y + 0.01 * np.abs(y).mean() * (rng.standard_normal(y.shape) + 1j * rng.standard_normal(y.shape))
+
+    nft = ops.NUFFT3d(shape, dcf)
+    nft.normalize_set_ktraj(np.stack(kk))
+    A = ops.joint2operators(ops.espirit(S), nft)
+    yt = torch.tensor(y.astype(np.complex64), device="cuda")
+    s_gpu = optscaling(A, yt)
+
+    def back64(kd):
+        return np.sum(np.conj(S) * op64.backward(kd), axis=-1, keepdims=True)
+
+    def normal64(v):
+        return np.sum(np.conj(S) * op64.forward_backward(v * S), axis=-1, keepdims=True)
+
+    s64 = float(np.max(np.abs(back64(y))))
+    assert abs(s_gpu - s64) / s64 < 1e-4
+    W = solvers.DWTnd("haar", level=4, axes=(0, 1, 2))
+    xg = solvers.IST_wrap(A, W, yt / s_gpu, it, 0.1, 0.06)
+    x64 = SO.ist(normal64, back64(y / s64), it, 0.1, 0.06, 4, (0, 1, 2))
+    assert rel(xg, x64) < 1e-3

@@ -253,8 +253,9 @@ def test_3d_warp_kernels_against_oracle(eps):
 
 
 @pytest.mark.parametrize("nc,tuning", [
-    (11, None),                                   # register tile 4x8x16, coil groups of 8 and 3
-    (8, Tuning(threads=128)),                     # register tile 4x4x16
+    (11, None),                                   # default: cube kernel on 8^3 tiles, coil groups of 8 and 3
+    (11, Tuning(spread_variant=1)),               # register rows, tile 4x8x16, coil groups of 8 and 3
+    (8, Tuning(threads=128, spread_variant=1)),   # register rows, tile 4x4x16
     (4, None),                                    # register tile 4x8x32, 4 coils per block
     (8, Tuning(spread_tile=(8, 8, 32))),          # shared-memory tile kernel
     (8, Tuning(max_subproblem=64)),               # many split tiles (global-atomic flush)
