@@ -874,6 +874,41 @@ def cpu_baseline_subprocess(wl):
                 "sample": "reference-arm subprocess failed: %s" % str(exc)[:200]}
 
 
+def step_kernels(torch, wl, coords, tuning, reps=3):
+    """The NUFFT step alone (type-2 then type-1 over every instance, eager launches), run
+    ``reps`` times after one warm-up, with each stage's CUDA-event time: the entry point for
+    profiling the step's kernels without the rest of the benchmark."""
+    from mripy_gb300 import _native as N
+    from mripy_gb300.plan import NufftPlan
+    dev = torch.device("cuda")
+    plan = NufftPlan(wl.dim, wl.shape, n_coil=wl.n_coil, n_traj=wl.n_traj, eps=wl.eps, max_nspread=wl.max_nspread,
+                     tuning=tuning)
+    plan.set_points(coords, traj_offsets=wl.offsets)
+    img = torch.from_numpy(np.ascontiguousarray(wl.imgs)).to(dev)
+    samples = torch.empty((wl.M, wl.n_coil), dtype=torch.complex64, device=dev)
+    out = torch.empty_like(img)
+    grid = plan.grid()
+    stream = torch.cuda.current_stream()
+    stages = {"pad_deapod": lambda: plan.pad_deapod(img, grid), "fft": lambda: plan.fft(grid, N.GBN_FFT_FORWARD),
+              "interp": lambda: plan.interp(grid, out=samples), "spread": lambda: plan.spread(samples, grid),
+              "fft_inverse": lambda: plan.fft(grid, N.GBN_FFT_INVERSE),
+              "crop_deapod": lambda: plan.crop_deapod(grid, out)}
+    for f in stages.values():
+        f()
+    torch.cuda.synchronize()
+    times = {k: [] for k in stages}
+    for _ in range(reps):
+        for k, f in stages.items():
+            t, _ = event_time(torch, f, 1, stream)
+            times[k].append(t)
+    plan.status()
+    info = plan.info()
+    return {"ms": {k: round(float(np.median(v)), 4) for k, v in times.items()}, "spread_tile": list(info["spread_tile"]),
+            "max_subproblem": info["max_subproblem"], "spread_kernels": info["spread_kernels"],
+            "launches_per_run": "pad, FFT (cuFFT), interp, spread (+ split-tile zeroing, dense-tile instance), "
+                                "inverse FFT, crop"}
+
+
 def run_solver_only(args, wl):
     import torch
     coords = [torch.from_numpy(c).cuda() for c in wl.coords]
@@ -882,6 +917,8 @@ def run_solver_only(args, wl):
         from mripy_gb300.tune import autotune
         tuning = autotune(wl.dim, wl.shape, coords, n_coil=wl.n_coil, n_traj=wl.n_traj, traj_offsets=wl.offsets,
                           eps=wl.eps, cache_file=args.tune_cache)
+    if args.part == "step":
+        return {"workload": wl.description, "part": "step", "step": step_kernels(torch, wl, coords, tuning)}
     if args.part == "autograd":
         return {"workload": wl.description, "part": "autograd", "autograd": autograd_time(torch, wl, tuning)}
     if args.part == "espirit":
@@ -905,14 +942,16 @@ def main():
     ap.add_argument("--tune-cache", default=None,
                     help="JSON file of autotuner results: read if it holds this workload's key, else "
                          "written; lets a profiler run reuse the tiling of an earlier run")
-    ap.add_argument("--part", default="all", choices=["all", "solver", "autograd", "espirit", "haar"],
-                    help="solver: only the solver timing of c2 (CG-SENSE) or c4 (IST); autograd: only "
+    ap.add_argument("--part", default="all", choices=["all", "step", "solver", "autograd", "espirit", "haar"],
+                    help="step: only the NUFFT step's stages, eager, 3 runs (for profiling); "
+                         "solver: only the solver timing of c2 (CG-SENSE) or c4 (IST); autograd: only "
                          "the differentiable step of c5; espirit: ESPIRiT maps from c2's or c4's coil "
                          "k-space; haar: the Haar transform and prox on c2's or c4's coil stack; one "
                          "JSON line with its figures (for profiling)")
     args = ap.parse_args()
     if args.part != "all":
-        ok = {"solver": ("c2", "c4"), "autograd": ("c5",), "espirit": ("c2", "c4"), "haar": ("c2", "c4")}[args.part]
+        ok = {"step": ("c1", "c2", "c3", "c4", "c5"), "solver": ("c2", "c4"), "autograd": ("c5",),
+              "espirit": ("c2", "c4"), "haar": ("c2", "c4")}[args.part]
         if args.workload not in ok or args.impl != "gb300":
             ap.error("--part %s takes --workload %s with the gb300 arm" % (args.part, " or ".join(ok)))
         from mripy_gb300 import build
