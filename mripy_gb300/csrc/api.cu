@@ -84,6 +84,7 @@ struct gbn_plan {
     int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256, interp_coil_group = 0;
     int interp_staging = 0;  // 0: tensor copies where the grid allows, 1: thread loads
     int spread_variant = 0;  // 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes
+    bool spread_items_interleaved = false;  // split tiles' work items interleave (cube kernel)
     int dense_min = kDenseDefault;  // 3-D spread tiles with this many samples use compensated sums (0: never)
     int64_t n_dense_sub = 0;
     int64_t n_split = 0;  // spread tiles covered by more than one subproblem (listed in split_tiles)
@@ -251,6 +252,17 @@ size_t smem_budget(const gbn_plan *p) {
 int dir_type1(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_FORWARD : GBN_FFT_INVERSE; }
 int dir_type2(const gbn_plan *p) { return p->desc.iflag < 0 ? GBN_FFT_INVERSE : GBN_FFT_FORWARD; }
 
+// coils per spread block: the plan's group, capped at the coil count and by shared memory
+int spread_cg(const gbn_plan *p) {
+    int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
+    while (cg > 1 && spread_smem_bytes(p->gs, cg) > smem_budget(p)) cg /= 2;
+    return cg;
+}
+
+// the 3-D cube kernel runs this plan's spreads; it alone reads interleaved work items, so
+// set_points builds them exactly when this holds
+bool spread_interleaved(const gbn_plan *p) { return spread_cube_applies(p->gs, spread_cg(p), p->spread_variant); }
+
 int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, float2 *grid, cudaStream_t s) {
     NvtxRange range("gbn spread");
     // tiles covered by several work items start from zero; when they are most of the grid
@@ -273,10 +285,11 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
     a.any_dense = p->n_dense_sub > 0 ? 1 : 0;
     a.variant = p->spread_variant;
     a.status = p->kstatus;
-    int cg = std::min(p->coil_group, pow2_floor(std::max(1, (int)p->desc.n_coil)));
-    while (cg > 1 && spread_smem_bytes(p->gs, cg) > smem_budget(p)) cg /= 2;
+    const int cg = spread_cg(p);
     if (spread_smem_bytes(p->gs, cg) > (size_t)p->smem_optin)
         return fail(GBN_ERR_CAPACITY, "spread tile does not fit in shared memory");
+    if (p->spread_items_interleaved != spread_interleaved(p))
+        return fail(GBN_ERR_INTERNAL, "spread work items do not match the spread kernel");
     GBN_CUDA(launch_spread(a, p->n_spread_sub, cg, p->threads, s));
     p->spread_kernels = (!memset_grid && p->n_split > 0 ? 1 : 0) + spread_kernel_count(a, p->n_spread_sub, cg, p->threads);
     return GBN_OK;
@@ -439,6 +452,7 @@ struct SubsJob {
     int every_tile, max_sub;
     uint32_t dense_min;
     uint32_t *n_dense, *n_split;  // device counters (may be null)
+    int interleave = 0;           // split tiles' items take every s-th entry
     int64_t T = 0;
 };
 
@@ -469,7 +483,8 @@ int subs_build(gbn_plan *p, const SubsJob &j, const uint32_t last[2], DevBuf &su
     if (n_sub > 0x7FFFFFFF) return fail(GBN_ERR_CAPACITY, "too many subproblems");
     GBN_TRY(ensure(p, subs, sizeof(int4) * (size_t)std::max<int64_t>(n_sub, 1)));
     GBN_CUDA(launch_build_subs(j.count, j.tile_off->as<uint32_t>(), j.sub_off->as<uint32_t>(), j.T, j.max_sub,
-                               j.every_tile, j.dense_min, split_list, split_cursor, subs.as<int4>(), s));
+                               j.every_tile, j.dense_min, j.interleave, split_list, split_cursor, subs.as<int4>(),
+                               s));
     *n_sub_out = n_sub;
     return GBN_OK;
 }
@@ -562,6 +577,8 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
                                    : p->max_sub;
     SubsJob js{&p->gs, scount, &p->spread_tile_off, &p->nsub, &p->sub_off, 1, p->max_sub, dense_min,
                p->kstatus + 1, p->kstatus + 2};
+    js.interleave = spread_interleaved(p) ? 1 : 0;
+    p->spread_items_interleaved = js.interleave != 0;
     SubsJob ji{&p->gi, home_count, &p->home_tile_off, &p->nsub_i, &p->sub_off_i, 0, interp_max_sub, 0u, nullptr,
                nullptr};
     uint32_t sizes[6] = {0, 0, 0, 0, 0, 0};  // spread last offset / count, interp ditto, dense, split

@@ -33,6 +33,7 @@ constexpr int kMaxW = 40;          // 2*nspread; nspread <= 20 (eps down to 1e-3
 constexpr int kSplitFlag = 1;      // tile is covered by more than one subproblem
 constexpr int kFirstFlag = 2;      // first subproblem of its tile
 constexpr int kDenseFlag = 4;      // tile above the dense-sample threshold: compensated sums
+constexpr int kStrideShift = 8;    // flags >> kStrideShift: entry stride of an interleaved item (0: 1)
 // default dense threshold (samples per 3-D spread tile).  Measured on GB300 for the 8-coil
 // 20000 x 128 centre-out radial workload: 32768 flags 10% of the work items and costs 8% of
 // the spread time; 2048 flags 41% and costs 27%.
@@ -109,8 +110,9 @@ cudaError_t launch_gather_pts(const float4 *pts, const uint32_t *idx, int64_t n,
 // dense_min > 0: subproblems of tiles with at least dense_min samples get kDenseFlag.
 // split_list (may be null): the indices of the tiles covered by more than one subproblem
 // are appended at *split_cursor (zeroed by the caller).
+// interleave: split tiles' items take every s-th entry (only for the 3-D cube spread)
 cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
-                              int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min,
+                              int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min, int interleave,
                               uint32_t *split_list, uint32_t *split_cursor, int4 *subs, cudaStream_t s);
 // work items per tile; n_dense (may be null) accumulates the items of tiles with at least
 // dense_min samples, n_split (may be null) the tiles split over several items
@@ -156,6 +158,8 @@ cudaError_t launch_zero_split(const Geom &g, const uint32_t *split_tiles, int64_
                               cudaStream_t s);
 cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads,
                           cudaStream_t s);
+// the 3-D cube spread runs these arguments (the kernel that reads interleaved work items)
+bool spread_cube_applies(const Geom &g, int coil_group, int variant);
 // kernels launch_spread runs for these arguments (the 3-D register path adds a Kahan instance)
 int spread_kernel_count(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads);
 cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, int threads,

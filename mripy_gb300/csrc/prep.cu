@@ -154,9 +154,12 @@ __global__ void k_count_subs(const uint32_t *__restrict__ count, int64_t n, int 
     if (n_split && s > 1) atomicAdd(n_split, 1u);
 }
 
+// interleave: the s > 1 items of a split tile take every s-th entry (item k: entries k,
+// k + s, k + 2s, ...; stride s in the flags above kStrideShift) instead of consecutive runs,
+// so that each item holds a spatially even share of the tile's samples
 __global__ void k_build_subs(const uint32_t *__restrict__ count, const uint32_t *__restrict__ tile_off,
                              const uint32_t *__restrict__ sub_off, int64_t n, int max_sub, int every_tile,
-                             uint32_t dense_min, uint32_t *__restrict__ split_list,
+                             uint32_t dense_min, int interleave, uint32_t *__restrict__ split_list,
                              uint32_t *__restrict__ split_cursor, int4 *__restrict__ subs) {
     int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -167,10 +170,15 @@ __global__ void k_build_subs(const uint32_t *__restrict__ count, const uint32_t 
     const bool dense = dense_min > 0 && c >= dense_min;
     if (s > 1 && split_list) split_list[atomicAdd(split_cursor, 1u)] = (uint32_t)t;  // order is irrelevant
     for (uint32_t k = 0; k < s; ++k) {
-        uint32_t start = k * (uint32_t)max_sub;
-        uint32_t len = c > start ? min((uint32_t)max_sub, c - start) : 0u;
         int flags = (s > 1 ? kSplitFlag : 0) | (k == 0 ? kFirstFlag : 0) | (dense ? kDenseFlag : 0);
-        subs[o + k] = make_int4((int)t, (int)(tile_off[t] + start), (int)len, flags);
+        if (interleave && s > 1) {
+            const uint32_t len = (c - k + s - 1) / s;  // entries k, k + s, ... below c
+            subs[o + k] = make_int4((int)t, (int)(tile_off[t] + k), (int)len, flags | (int)(s << kStrideShift));
+        } else {
+            uint32_t start = k * (uint32_t)max_sub;
+            uint32_t len = c > start ? min((uint32_t)max_sub, c - start) : 0u;
+            subs[o + k] = make_int4((int)t, (int)(tile_off[t] + start), (int)len, flags);
+        }
     }
 }
 
@@ -221,12 +229,12 @@ cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int
 }
 
 cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
-                              int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min,
+                              int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min, int interleave,
                               uint32_t *split_list, uint32_t *split_cursor, int4 *subs, cudaStream_t s) {
     if (ntiles_total == 0) return cudaSuccess;
     k_build_subs<<<blocks_for(ntiles_total, 256), 256, 0, s>>>(count, tile_off, sub_off, ntiles_total, max_sub,
-                                                               every_tile, dense_min, split_list, split_cursor,
-                                                               subs);
+                                                               every_tile, dense_min, interleave, split_list,
+                                                               split_cursor, subs);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,8 @@ static int cube_path(const Geom &g, int coil_group, int variant) {
     return 0;
 }
 
+bool spread_cube_applies(const Geom &g, int coil_group, int variant) { return cube_path(g, coil_group, variant) != 0; }
+
 int spread_kernel_count(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads) {
     if (n_sub == 0) return 0;
     const bool two = cube_path(a.g, coil_group, a.variant) || reg3d_path(a.g, coil_group, threads);

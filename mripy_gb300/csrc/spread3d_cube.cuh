@@ -132,6 +132,7 @@ __global__ void __launch_bounds__((NWC + kCubeProducers) * 32, (KAHAN || NWC > 8
             if (!cube_unit(a.subs, unit, n_cg, KAHAN, sub)) continue;
             const int nb = (sub.z + B - 1) / B;
             const int cg0 = (int)(unit % n_cg) * CG;
+            const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
             int o[3], e[3];
             tile_coords<3>(g, sub.x % g.ntiles, o, e);
             // this producer's batches of the unit: t + k with (t + k) % kCubeProducers == p
@@ -144,8 +145,9 @@ __global__ void __launch_bounds__((NWC + kCubeProducers) * 32, (KAHAN || NWC > 8
                 float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
                 uint32_t j = 0;
                 if (ok) {
-                    pt = a.pts[(int64_t)sub.y + k * B + lane];
-                    j = a.idx[(int64_t)sub.y + k * B + lane];
+                    const int64_t ent = (int64_t)sub.y + (int64_t)(k * B + lane) * stride;
+                    pt = a.pts[ent];
+                    j = a.idx[ent];
                 }
                 float2 v[CG];
                 float sw = 1.f;
