@@ -277,6 +277,7 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
     a.subs = p->spread_subs.as<int4>();
     a.pts = p->dup_pts.as<float4>();
     a.idx = p->dup_idx.as<uint32_t>();
+    a.pts_by_sample = p->pts.as<float4>();
     a.c = (const float2 *)c;
     a.c_elem = L.elem_stride;
     a.c_coil = L.coil_stride;

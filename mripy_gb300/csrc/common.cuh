@@ -125,6 +125,8 @@ struct SpreadArgs {
     const int4 *subs;
     const float4 *pts;        // dup-list order
     const uint32_t *idx;      // dup-list sample index
+    const float4 *pts_by_sample;  // the same records in the caller's sample order (41 MB for
+                                  // 2.56 M samples: stays in L2), read through idx
     const float2 *c;          // samples
     int64_t c_elem, c_coil;   // strides (complex elements)
     const float *weight;      // per sample (original index) or null: density compensation

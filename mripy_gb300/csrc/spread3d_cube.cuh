@@ -14,7 +14,7 @@
 // item, coil group) units -- block b takes units b, b + gridDim.x, ...; the launcher gives
 // one unit per block -- and numbers their 32-sample batches consecutively.  Batch t goes to
 // slot t % kCubeSlots of a ring in shared memory and is filled by producer warp
-// t % kCubeProducers: sample records, the separable
+// t % kCubeProducers: sample records (read by sample index), the separable
 // weights of every tile plane / row / column in FP32, the 8 coil values times the optional
 // density weight, and for every consumer warp the ordered list of the batch's samples whose
 // stencil reaches its cube, built by ballots.  The producer waits on the slot's `empty`
@@ -145,9 +145,11 @@ __global__ void __launch_bounds__((NWC + kCubeProducers) * 32, (KAHAN || NWC > 8
                 float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
                 uint32_t j = 0;
                 if (ok) {
-                    const int64_t ent = (int64_t)sub.y + (int64_t)(k * B + lane) * stride;
-                    pt = a.pts[ent];
-                    j = a.idx[ent];
+                    // the record by sample index: the 16-byte copies of the dup list would
+                    // be read once per (sample, tile) pair from DRAM; the sample-order array
+                    // stays in L2
+                    j = a.idx[(int64_t)sub.y + (int64_t)(k * B + lane) * stride];
+                    pt = a.pts_by_sample[j];
                 }
                 float2 v[CG];
                 float sw = 1.f;
