@@ -83,7 +83,7 @@ typedef struct {
                                    (cubes on the default 8^3 tile, warp rows on a caller's
                                    tile), 1 = warp rows (tile (4 x warps / TY, TY, 16)),
                                    2 = 4^3-cell cubes fed by producer warps (tile of 8 or 16
-                                   cubes; default work items of 4096 samples) */
+                                   cubes; default work items of 2048 samples) */
 } gbn_plan_desc;
 
 typedef struct {

@@ -748,8 +748,8 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         }
     }
     // 3-D with 8 coils per block: the cube kernel on 8^3-cell tiles (2 x 2 x 2 cubes of 4^3)
-    // with 4096-sample work items, unless the caller chose a tile or warp rows.  Measured on
-    // GB300 (8 coils, 2.56 M centre-out radial samples, 256^3 grid): 12.2 ms against 13.9 ms
+    // with 2048-sample work items, unless the caller chose a tile or warp rows.  Measured on
+    // GB300 (8 coils, 2.56 M centre-out radial samples, 256^3 grid): 11.3 ms against 13.9 ms
     // for the warp rows' best tiling.  Otherwise (4 coils per block, or warp rows) the
     // register rows: (x, y) rows of 4 per warp, tile (TX, TY, 4 x 32/coils), TX*TY = 4 x warps.
     const bool tile_given = desc->spread_tile[0] > 0 || desc->spread_tile[1] > 0 || desc->spread_tile[2] > 0;
@@ -765,7 +765,7 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     }
     const bool cube = p->dim == 3 && cg_eff == 8 && p->spread_variant == 2;
     p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem
-                                          : (cube ? 4096 : (reg_spread && p->dim == 2 ? 128 : 256));
+                                          : (cube ? 2048 : (reg_spread && p->dim == 2 ? 128 : 256));
     make_geom(p, ts, p->gs);
     make_geom(p, ti, p->gi);
 

@@ -23,7 +23,7 @@
 // run their own list, arrive on `empty`; after a unit's last batch they write their cube
 // and start the next unit from zero.  No block-wide barrier runs after the set-up: a
 // consumer warp with a long list in one batch is evened out by short lists in the next
-// seven.  (Cubes of one tile also get unequal shares of its samples over a whole unit -- a
+// fifteen.  (Cubes of one tile also get unequal shares of its samples over a whole unit -- a
 // tile's samples cluster on one side -- which the ring cannot absorb; on the 3-D radial
 // workload the cube warps' work per tile is 84 % balanced.)
 //
@@ -44,8 +44,14 @@
 
 namespace gbn {
 
-constexpr int kCubeSlots = 8;                 // ring depth (batches)
-constexpr int kCubeProducers = 4;             // producer warps; producer p fills slots p, p + 4
+#ifndef GBN_CUBE_SLOTS
+#define GBN_CUBE_SLOTS 16
+#endif
+// ring depth (batches), a multiple of kCubeProducers: a fast consumer warp may run up to 15
+// batches ahead of the slowest (measured on the 3-D radial workload: 8 slots 11.93 ms,
+// 12 slots 11.68 ms, 16 slots 11.32 ms, with 2048-sample work items)
+constexpr int kCubeSlots = GBN_CUBE_SLOTS;
+constexpr int kCubeProducers = 4;             // producer warps; producer p fills slots p, p + 4, ...
 constexpr int kCubeBatch = 32;                // samples per batch
 constexpr uint32_t kStatusSpreadTimeout = 4u; // status-word bit: a spread ring wait gave up
 

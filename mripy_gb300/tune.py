@@ -150,9 +150,9 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
     best_s = best_i = None
     # spread tiling (interp at default), then interp tiling (spread at the winner)
     for tile, th, cg, var in _spread_candidates(dim, n_coil):
-        # the cube kernel needs long work items to keep its ring full: time it at 4096
+        # the cube kernel needs long work items to keep its ring full: time it at 2048
         tu = Tuning(spread_tile=tile, threads=th, coil_group=cg, spread_variant=var,
-                    max_subproblem=4096 if var == 2 else 0)
+                    max_subproblem=2048 if var == 2 else 0)
         try:
             t_s, _ = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
         except Exception:
