@@ -80,10 +80,12 @@ typedef struct {
                                    k-space centre of radial data) accumulate with Kahan-
                                    compensated FP32 sums; 0 = 32768, negative = never */
     int32_t spread_variant;     /* 3-D spread with 8 coils per block: 0 = library choice
-                                   (cubes on the default 8^3 tile, warp rows on a caller's
-                                   tile), 1 = warp rows (tile (4 x warps / TY, TY, 16)),
+                                   (tensor cores on the default 4 x 8 x 16 tile, warp rows
+                                   on a caller's tile), 1 = warp rows (tile (4 x warps / TY, TY, 16)),
                                    2 = 4^3-cell cubes fed by producer warps (tile of 8 or 16
-                                   cubes; default work items of 2048 samples) */
+                                   cubes; default work items of 2048 samples),
+                                   3 = tensor cores (tcgen05 TF32 MMAs, 3-term split; tile
+                                   4 x 8 x 16; dense items on the compensated cubes) */
 } gbn_plan_desc;
 
 typedef struct {

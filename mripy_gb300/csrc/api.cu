@@ -83,7 +83,7 @@ struct gbn_plan {
     Geom gs{}, gi{};
     int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256, interp_coil_group = 0;
     int interp_staging = 0;  // 0: tensor copies where the grid allows, 1: thread loads
-    int spread_variant = 0;  // 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes
+    int spread_variant = 0;  // 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes, 3 tensor cores
     bool spread_items_interleaved = false;  // split tiles' work items interleave (cube kernel)
     int dense_min = kDenseDefault;  // 3-D spread tiles with this many samples use compensated sums (0: never)
     int64_t n_dense_sub = 0;
@@ -719,9 +719,9 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         return fail(GBN_ERR_ARG, "interp_staging must be 0 or 1");
     }
     p->interp_staging = desc->interp_staging;
-    if (desc->spread_variant < 0 || desc->spread_variant > 2) {
+    if (desc->spread_variant < 0 || desc->spread_variant > 3) {
         delete p;
-        return fail(GBN_ERR_ARG, "spread_variant must be 0, 1 or 2");
+        return fail(GBN_ERR_ARG, "spread_variant must be 0, 1, 2 or 3");
     }
     p->spread_variant = desc->spread_variant;
     p->dense_min = desc->dense_tile_samples > 0 ? desc->dense_tile_samples
@@ -747,15 +747,21 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
             reg_spread = true;
         }
     }
-    // 3-D with 8 coils per block: the cube kernel on 8^3-cell tiles (2 x 2 x 2 cubes of 4^3)
-    // with 2048-sample work items, unless the caller chose a tile or warp rows.  Measured on
-    // GB300 (8 coils, 2.56 M centre-out radial samples, 256^3 grid): 11.3 ms against 13.9 ms
-    // for the warp rows' best tiling.  Otherwise (4 coils per block, or warp rows) the
-    // register rows: (x, y) rows of 4 per warp, tile (TX, TY, 4 x 32/coils), TX*TY = 4 x warps.
+    // 3-D with 8 coils per block, unless the caller chose a tile: the tensor-core kernel on
+    // 4 x 8 x 16 tiles (variant 0 or 3), or the cube kernel on 8^3-cell tiles (2 x 2 x 2 cubes
+    // of 4^3, variant 2), with 2048-sample work items.  Measured on GB300 (8 coils, 2.56 M
+    // centre-out radial samples, 256^3 grid), with the dense centre tiles on the compensated
+    // cubes: 7.8 ms (tensor cores), 11.3 ms (cubes), 13.9 ms (the warp rows' best tiling).
+    // Otherwise (4 coils per block, or warp rows) the register rows: (x, y) rows of 4 per
+    // warp, tile (TX, TY, 4 x 32/coils), TX*TY = 4 x warps.
     const bool tile_given = desc->spread_tile[0] > 0 || desc->spread_tile[1] > 0 || desc->spread_tile[2] > 0;
-    if (p->dim == 3 && !tile_given && cg_eff == 8 && p->spread_variant != 1) {
+    if (p->dim == 3 && !tile_given && cg_eff == 8 && (p->spread_variant == 3 || p->spread_variant == 0)) {
+        ts[0] = 4;  // the tensor-core kernel's tile: (y, z) = 128 cells, one TMEM lane each
+        ts[1] = 8;
+        ts[2] = 16;
+        p->spread_variant = 3;
+    } else if (p->dim == 3 && !tile_given && cg_eff == 8 && p->spread_variant == 2) {
         ts[0] = ts[1] = ts[2] = 8;
-        p->spread_variant = 2;
     } else if (p->dim == 3 && !tile_given && cg_eff >= 4 && p->threads <= 256) {
         const int rows = 4 * (p->threads / 32);
         ts[1] = rows >= 32 ? 8 : 4;
@@ -763,7 +769,7 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         ts[2] = 4 * (32 / cg_eff);
         reg_spread = true;
     }
-    const bool cube = p->dim == 3 && cg_eff == 8 && p->spread_variant == 2;
+    const bool cube = p->dim == 3 && cg_eff == 8 && (p->spread_variant == 2 || p->spread_variant == 3);
     p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem
                                           : (cube ? 2048 : (reg_spread && p->dim == 2 ? 128 : 256));
     make_geom(p, ts, p->gs);

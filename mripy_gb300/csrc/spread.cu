@@ -4,10 +4,14 @@
 // they are built for: k_spread2d_reg / k_spread3d_reg (accumulators in registers).
 // Other 2-D / 3-D tiles: k_spread2d / k_spread3d (warp-owned shared-memory rows, no atomics).
 // Otherwise (1-D, wide stencils, small grids): k_spread (shared-memory atomics).
+// 3-D with 8 coils per block also: k_spread3d_mma (tensor cores, 4 x 8 x 16 tiles) and
+// k_spread3d_cube (register cubes), each followed by the compensated cube instance for the
+// dense work items.
 #include "dispatch.cuh"
 #include "grid2d_kernels.cuh"
 #include "grid3d_kernels.cuh"
 #include "spread3d_cube.cuh"
+#include "spread3d_mma.cuh"
 
 #include <algorithm>
 
@@ -53,11 +57,21 @@ static int cube_path(const Geom &g, int coil_group, int variant) {
     return 0;
 }
 
-bool spread_cube_applies(const Geom &g, int coil_group, int variant) { return cube_path(g, coil_group, variant) != 0; }
+// the tensor-core kernel applies: 3-D, 8 coils per block, its 4 x 8 x 16 tile, variant 3
+static bool mma_path(const Geom &g, int coil_group, int variant) {
+    return variant == 3 && grid3d_applies(g) && coil_group == 8 && g.tile[0] == kMmaTX && g.tile[1] == kMmaTY &&
+           g.tile[2] == kMmaTZ;
+}
+
+// the cube and tensor-core kernels read interleaved work items
+bool spread_cube_applies(const Geom &g, int coil_group, int variant) {
+    return cube_path(g, coil_group, variant) != 0 || mma_path(g, coil_group, variant);
+}
 
 int spread_kernel_count(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads) {
     if (n_sub == 0) return 0;
-    const bool two = cube_path(a.g, coil_group, a.variant) || reg3d_path(a.g, coil_group, threads);
+    const bool two = cube_path(a.g, coil_group, a.variant) || mma_path(a.g, coil_group, a.variant) ||
+                     reg3d_path(a.g, coil_group, threads);
     return (two && a.any_dense) ? 2 : 1;
 }
 
@@ -91,6 +105,21 @@ static cudaError_t launch_cube(const SpreadArgs &a, int64_t n_sub, cudaStream_t 
     return e;
 }
 
+// tensor-core kernel (one unit per block), then the compensated cube instance for the dense
+// units on the same tiles (4 x 8 x 16 = 8 cubes of 4^3)
+template <int WT>
+static cudaError_t launch_mma(const SpreadArgs &a, int64_t n_sub, cudaStream_t s) {
+    const int n_cg = (a.g.n_coil + 7) / 8;
+    const int64_t n_units = n_sub * n_cg;
+    auto kern = k_spread3d_mma<WT>;
+    cudaError_t e = set_smem(kern, kMmaSmemBytes);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)n_units, kMmaThreads, kMmaSmemBytes, s>>>(a, a.status, n_cg);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && a.any_dense) e = launch_cube_instance<WT, 8, true>(a, n_units, n_cg, s);
+    return e;
+}
+
 cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads, cudaStream_t s) {
     if (n_sub == 0) return cudaSuccess;
     const size_t smem = spread_smem_bytes(a.g, coil_group);
@@ -120,6 +149,11 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
                 err = cudaGetLastError();
             }
         }));
+        return err;
+    }
+    // 3-D tensor-core kernel (8 coils per block), then compensated cube sums for dense units
+    if (mma_path(a.g, coil_group, a.variant)) {
+        GBN_DISPATCH_W(a.g.W, { err = launch_mma<WT>(a, n_sub, s); });
         return err;
     }
     // 3-D cube kernel (8 coils per block): plain sums, then (if any) compensated ones

@@ -1,0 +1,348 @@
+// 3-D spread (type-1 gridding) of 8 coils on the tensor cores.
+//
+// The adjoint gridding of one tile is a sum of outer products over its samples s:
+//     G[x, y, z, c] = sum_s wx_s[x] wy_s[y] wz_s[z] v_s[c]
+// and with the separable weights split between the two operands it is a GEMM with the
+// samples as its K dimension:
+//     D[(y, z), (x, c, re/im)] = sum_s A[(y, z), s] * B[s, (x, c, re/im)]
+//     A[(y, z), s] = wy_s[y] wz_s[z]                      (M = 8 x 16 = 128 cells)
+//     B[s, (x, c, ri)] = wx_s[x] * (re, im)(v_s[c])       (N = 4 x 8 x 2 = 64)
+// on tiles of 4 x 8 x 16 cells.  The accumulator D lives in tensor memory (TMEM); A is built
+// in TMEM (tcgen05.st), B in shared memory (K-major, 128-byte swizzle); one
+// tcgen05.mma.kind::tf32 covers 8 samples.  Each FP32 operand is split as x = hi + lo with
+// hi on the TF32 grid, and three MMAs (hi*hi + hi*lo + lo*hi) give products within ~1e-6 of
+// FP32 (the lo*lo term, below 2^-22 relative, is left out).  The tensor core evaluates the
+// whole tile for every sample (a 12-tap stencil covers ~22 % of a 4 x 8 x 16 tile on
+// average) but needs no per-cell instruction: the CUDA cores build 192 operand values per
+// (sample, tile) pair instead of issuing the stencil's FMAs.
+//
+// One (work item, coil group) unit per block, 13 warps:
+// * 4 loader warps fill a ring of kMmaSlots 32-sample batches (loader l: batches l, l + 4,
+//   ...): sample records by sample index, the tile's separable FP32 weights per sample
+//   (stored [tap][sample]), the 8 coil values times the optional density weight
+//   ([coil][sample]); `full` / `empty` mbarriers per slot.
+// * 8 builder warps turn a batch into the MMA operands: warp b writes A's hi and lo parts
+//   for the 32 TMEM lanes of its quarter (b % 4) and 16 of the 32 samples (b / 4), and 8 of
+//   B's 64 rows into shared memory; two operand buffers, the one of batch t reused by batch
+//   t + 2 after the MMAs of batch t completed (`done` mbarrier, signalled by tcgen05.commit).
+//   After the last batch they read D back (tcgen05.ld) and write the tile.
+// * 1 MMA warp: allocates TMEM, and its lane 0 issues 12 MMAs per batch once the builders
+//   arrived on the buffer's `ops` mbarrier, then commits to the buffer's `done` mbarrier.
+// Summation: the tensor core's FP32 accumulation rounds less carefully than FP32 adds (its
+// error grew with the number of accumulated MMAs: 1.6e-6 relative to the FP32 kernel with
+// 1024-sample work items, 4.9e-6 with 8192, on the 3-D radial workload), so it sums groups
+// of kMmaGroup batches (256 samples, 96 MMAs) only; the builders then add the accumulator
+// into a running sum S in TMEM with FP32 adds before the next group's first MMA overwrites
+// it.  The order is fixed for a given trajectory and tiling.
+//
+// Every wait is bounded (kTmaWaitLimit probes); one that gives up sets kStatusSpreadTimeout
+// in the plan's status word and goes on, so no launch can hang.  Only the units without the
+// dense flag run here: dense (k-space centre) units take the Kahan-compensated cube kernel.
+#pragma once
+
+#include "common.cuh"
+#include "grid2d_kernels.cuh"
+#include "grid3d_kernels.cuh"
+#include "spread3d_cube.cuh"
+#include "tc.cuh"
+
+namespace gbn {
+
+constexpr int kMmaTX = 4, kMmaTY = 8, kMmaTZ = 16;  // the tile this kernel takes
+constexpr int kMmaM = kMmaTY * kMmaTZ;              // 128 cells (y, z): one TMEM lane each
+constexpr int kMmaN = kMmaTX * 16;                  // 64 columns (x, coil, re/im)
+constexpr int kMmaBatch = 32;                       // samples per batch: one 128-byte K row
+constexpr int kMmaSlots = 8;                        // staged batches
+constexpr int kMmaLoaders = 4;
+constexpr int kMmaBuilders = 8;
+constexpr int kMmaWarp = kMmaBuilders + kMmaLoaders;  // the MMA warp's index
+constexpr int kMmaThreads = 32 * (kMmaWarp + 1);
+constexpr uint32_t kMmaTmemCols = 256;              // A (hi, lo) x 2 buffers: 0..127; D, S: 128..255
+constexpr uint32_t kMmaColD = 128;                  // the MMAs' accumulator
+constexpr uint32_t kMmaColS = 192;                  // the running sum of the drained accumulators
+constexpr int kMmaGroup = 8;                        // batches the tensor core sums before a drain
+constexpr int kMmaWS = 36;  // floats per staged [tap] row of 32 samples: 16-byte aligned, 4-bank skew
+
+// shared memory, bytes from a 1024-byte aligned base
+constexpr uint32_t kMmaBOp = kMmaN * 128;                               // one B operand: 64 rows x 128 B
+constexpr uint32_t kMmaStWx = 0;                                        // [TX][kMmaWS] floats
+constexpr uint32_t kMmaStWy = kMmaStWx + 4 * kMmaTX * kMmaWS;           // [TY][kMmaWS]
+constexpr uint32_t kMmaStWz = kMmaStWy + 4 * kMmaTY * kMmaWS;           // [TZ][kMmaWS]
+constexpr uint32_t kMmaStV = kMmaStWz + 4 * kMmaTZ * kMmaWS;            // [8 coils][32] float2
+constexpr uint32_t kMmaSlotBytes = kMmaStV + 8 * 8 * kMmaBatch;
+constexpr uint32_t kMmaStageOff = 4 * kMmaBOp;                          // after B (hi, lo) x 2 buffers
+constexpr uint32_t kMmaBarOff = kMmaStageOff + kMmaSlots * kMmaSlotBytes;
+constexpr uint32_t kMmaBars = 2 * kMmaSlots + 4;                        // full, empty, ops[2], done[2]
+// + the TMEM address word and the alignment slack.  Above a third of the SM's 228 KB, so at
+// most two blocks (2 x 256 TMEM columns) share an SM and tcgen05.alloc never waits.
+constexpr size_t kMmaSmemBytes = kMmaBarOff + 8 * kMmaBars + 16 + 1024;
+static_assert(kMmaSmemBytes > 228 * 1024 / 3, "two blocks per SM at most");
+static_assert(kMmaStV % 16 == 0 && kMmaSlotBytes % 16 == 0, "16-byte aligned staging");
+
+// x = hi + lo: hi rounded to the TF32 grid (ties away from zero, by integer arithmetic on the
+// bit pattern), lo = x - hi exactly; the tensor core reads lo's top 11 significant bits
+__device__ __forceinline__ void tf32_split_fast(float x, float &hi, float &lo) {
+    hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+    lo = x - hi;
+}
+
+// S (+)= D over this thread's lane and the 32 columns of half hk; `first`: S = D
+__device__ __forceinline__ void mma_drain(uint32_t tl, int hk, bool first) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t col = 32u * hk + 16u * h;
+        float d[16], s[16];
+        tmem_ld_x16(tl + kMmaColD + col, d);
+        if (!first) {
+            tmem_ld_x16(tl + kMmaColS + col, s);
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) d[i] += s[i];
+        } else {
+            tmem_wait_ld();
+        }
+        tmem_st_x16(tl + kMmaColS + col, d);
+    }
+}
+
+template <int WT>
+__global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, uint32_t *status, int n_cg) {
+    constexpr int B = kMmaBatch;
+    constexpr int CG = 8;
+    extern __shared__ unsigned char smem_mma_raw[];
+    unsigned char *sm = smem_mma_raw + ((1024u - (smem_addr(smem_mma_raw) & 1023u)) & 1023u);
+    unsigned char *opB = sm;  // [buf][hi, lo][64 rows x 128 B], SW128
+    unsigned char *stage = sm + kMmaStageOff;
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + kMmaBarOff);
+    uint64_t *empty = full + kMmaSlots;
+    uint64_t *ops = empty + kMmaSlots;
+    uint64_t *done = ops + 2;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 2);
+
+    const Geom &g = a.g;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int W = WT ? WT : g.W;
+
+    if (warp == kMmaWarp) {
+        tmem_alloc(tslot, kMmaTmemCols);
+        tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kMmaSlots; ++k) {
+            mbar_init(&full[k], 32);                  // the loader warp, every lane
+            mbar_init(&empty[k], kMmaBuilders * 32);  // every builder lane
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&ops[b], kMmaBuilders * 32);
+            mbar_init(&done[b], 1);                   // tcgen05.commit
+        }
+        fence_barrier_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tslot;
+
+    const int64_t unit = blockIdx.x;
+    int4 sub;
+    if (cube_unit(a.subs, unit, n_cg, false, sub)) {
+        const int nb = (sub.z + B - 1) / B;
+        const int cg0 = (int)(unit % n_cg) * CG;
+        int o[3], e[3];
+        tile_coords<3>(g, sub.x % g.ntiles, o, e);
+
+        if (warp >= kMmaBuilders && warp < kMmaWarp) {
+            // ------------------------------------------------------------ loader warp
+            const int lw = warp - kMmaBuilders;
+            const int ns = g.ns;
+            const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
+            for (int k = lw; k < nb; k += kMmaLoaders) {
+                const int slot = k % kMmaSlots;
+                const int n = min(B, sub.z - k * B);
+                const bool ok = lane < n;
+                float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
+                uint32_t j = 0;
+                if (ok) {
+                    j = a.idx[(int64_t)sub.y + (int64_t)(k * B + lane) * stride];
+                    pt = a.pts_by_sample[j];
+                }
+                float sw = 1.f;
+                if (ok && a.weight) sw = a.weight[j];
+                float2 v[CG];
+#pragma unroll
+                for (int cc = 0; cc < CG; ++cc) {
+                    v[cc] = make_float2(0.f, 0.f);
+                    if (ok && cg0 + cc < g.n_coil) {
+                        const float2 tv = a.c[(int64_t)j * a.c_elem + (int64_t)(cg0 + cc) * a.c_coil];
+                        v[cc] = make_float2(tv.x * sw, tv.y * sw);
+                    }
+                }
+                int r[3] = {0, 0, 0};
+                if (ok) {
+                    int c0[3];
+                    unpack_cells(3, __float_as_uint(pt.w), c0[0], c0[1], c0[2]);
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        int rr = c0[d] - o[d];
+                        rr += rr < 0 ? g.nf[d] : 0;
+                        rr -= rr > g.nf[d] - W ? g.nf[d] : 0;
+                        r[d] = rr;
+                    }
+                }
+                // the slot's previous batch must be released by every builder lane
+                if (k >= kMmaSlots &&
+                    !mbar_wait_bounded(&empty[slot], (uint32_t)((k / kMmaSlots - 1) & 1)) && lane == 0)
+                    atomicOr(status, kStatusSpreadTimeout);
+                unsigned char *sl = stage + (size_t)slot * kMmaSlotBytes;
+                float *wx = reinterpret_cast<float *>(sl + kMmaStWx);
+                float *wy = reinterpret_cast<float *>(sl + kMmaStWy);
+                float *wz = reinterpret_cast<float *>(sl + kMmaStWz);
+#pragma unroll
+                for (int t = 0; t < kMmaTX; ++t) wx[t * kMmaWS + lane] = tap_weight(ok, t - r[0], W, pt.x, ns, g.beta2[0]);
+#pragma unroll
+                for (int t = 0; t < kMmaTY; ++t) wy[t * kMmaWS + lane] = tap_weight(ok, t - r[1], W, pt.y, ns, g.beta2[1]);
+#pragma unroll
+                for (int t = 0; t < kMmaTZ; ++t) wz[t * kMmaWS + lane] = tap_weight(ok, t - r[2], W, pt.z, ns, g.beta2[2]);
+                float2 *vs = reinterpret_cast<float2 *>(sl + kMmaStV);
+#pragma unroll
+                for (int cc = 0; cc < CG; ++cc) vs[cc * B + lane] = v[cc];
+                mbar_arrive(&full[slot]);
+            }
+        } else if (warp == kMmaWarp) {
+            // ------------------------------------------------------------ MMA warp
+            if (lane == 0) {
+                constexpr uint32_t idesc = tc_idesc_tf32(kMmaM, kMmaN);
+                const uint32_t b0 = smem_addr(opB);
+                for (int k = 0; k < nb; ++k) {
+                    const int buf = k & 1;
+                    if (!mbar_wait_bounded(&ops[buf], (uint32_t)((k >> 1) & 1))) atomicOr(status, kStatusSpreadTimeout);
+                    tc_fence_after();
+                    const uint32_t ah = tbase + 64u * buf, al = ah + 32u, d = tbase + kMmaColD;
+                    const uint32_t bh = b0 + 2u * buf * kMmaBOp, bl = bh + kMmaBOp;
+#pragma unroll
+                    for (int jk = 0; jk < B / 8; ++jk) {
+                        tc_mma_tf32_ts(d, ah + 8u * jk, tc_desc_sw128(bh + 32u * jk), idesc,
+                                       (k % kMmaGroup) != 0 || jk != 0);
+                        tc_mma_tf32_ts(d, ah + 8u * jk, tc_desc_sw128(bl + 32u * jk), idesc, 1u);
+                        tc_mma_tf32_ts(d, al + 8u * jk, tc_desc_sw128(bh + 32u * jk), idesc, 1u);
+                    }
+                    tc_commit(&done[buf]);
+                }
+            }
+            __syncwarp();
+        } else {
+            // ------------------------------------------------------------ builder warp
+            const int q = warp & 3, hk = warp >> 2;  // TMEM quarter; half of the batch's samples
+            const int m = 32 * q + lane, y = m >> 4, z = m & 15;
+            const int bx = warp >> 1, bc0 = 4 * (warp & 1);  // B rows: x = bx, coils bc0 .. bc0 + 3
+            const uint32_t tl = tmem_lane_base(tbase, q);
+            for (int k = 0; k < nb; ++k) {
+                const int slot = k % kMmaSlots, buf = k & 1;
+                if (!mbar_wait_bounded(&full[slot], (uint32_t)((k / kMmaSlots) & 1)) && lane == 0)
+                    atomicOr(status, kStatusSpreadTimeout);
+                // the MMAs of batch k - 2 (same operand buffer) have completed
+                if (k >= 2 && !mbar_wait_bounded(&done[buf], (uint32_t)(((k >> 1) - 1) & 1)) && lane == 0)
+                    atomicOr(status, kStatusSpreadTimeout);
+                const unsigned char *sl = stage + (size_t)slot * kMmaSlotBytes;
+                // A: cells (y, z) of this lane, samples 16 hk .. 16 hk + 15
+                const float4 *wy4 = reinterpret_cast<const float4 *>(sl + kMmaStWy) + (y * kMmaWS + 16 * hk) / 4;
+                const float4 *wz4 = reinterpret_cast<const float4 *>(sl + kMmaStWz) + (z * kMmaWS + 16 * hk) / 4;
+                float hi[16], lo[16];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float4 p = wy4[i], s = wz4[i];
+                    tf32_split_fast(p.x * s.x, hi[4 * i], lo[4 * i]);
+                    tf32_split_fast(p.y * s.y, hi[4 * i + 1], lo[4 * i + 1]);
+                    tf32_split_fast(p.z * s.z, hi[4 * i + 2], lo[4 * i + 2]);
+                    tf32_split_fast(p.w * s.w, hi[4 * i + 3], lo[4 * i + 3]);
+                }
+                tmem_st_x16(tl + 64u * buf + 16u * hk, hi);
+                tmem_st_x16(tl + 64u * buf + 32u + 16u * hk, lo);
+                // B: rows (bx, coil, re/im) for sample `lane`
+                const float wxk = reinterpret_cast<const float *>(sl + kMmaStWx)[bx * kMmaWS + lane];
+                const float2 *vs = reinterpret_cast<const float2 *>(sl + kMmaStV);
+                unsigned char *bh = opB + (size_t)(2 * buf) * kMmaBOp, *bl = bh + kMmaBOp;
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) {
+                    const float2 vv = vs[(bc0 + cc) * B + lane];
+                    const int nre = bx * 16 + (bc0 + cc) * 2;
+                    float h, l;
+                    tf32_split_fast(wxk * vv.x, h, l);
+                    *reinterpret_cast<float *>(bh + sw128_offset(nre, lane)) = h;
+                    *reinterpret_cast<float *>(bl + sw128_offset(nre, lane)) = l;
+                    tf32_split_fast(wxk * vv.y, h, l);
+                    *reinterpret_cast<float *>(bh + sw128_offset(nre + 1, lane)) = h;
+                    *reinterpret_cast<float *>(bl + sw128_offset(nre + 1, lane)) = l;
+                }
+                mbar_arrive(&empty[slot]);
+                if (k % kMmaGroup == 0 && k > 0) {
+                    // batch k starts a new group: once the previous group's MMAs are done,
+                    // add its accumulator into S (the same phase is waited for again at
+                    // k + 1, which returns at once)
+                    if (!mbar_wait_bounded(&done[(k - 1) & 1], (uint32_t)(((k - 1) >> 1) & 1)) && lane == 0)
+                        atomicOr(status, kStatusSpreadTimeout);
+                    tc_fence_after();
+                    mma_drain(tl, hk, k == kMmaGroup);
+                }
+                // operands visible to the tensor core before the MMA warp proceeds
+                tmem_wait_st();
+                fence_proxy_async_smem();
+                tc_fence_before();
+                mbar_arrive(&ops[buf]);
+            }
+
+            // ---------------------------------------------------------------- epilogue
+            // this warp: lanes of quarter q, columns 32 hk .. 32 hk + 31 (x = 2 hk, 2 hk + 1)
+            if (nb > 0) {
+                const int kl = nb - 1;
+                if (!mbar_wait_bounded(&done[kl & 1], (uint32_t)((kl >> 1) & 1)) && lane == 0)
+                    atomicOr(status, kStatusSpreadTimeout);
+                tc_fence_after();
+            }
+            const int grp = sub.x / g.ntiles;
+            const bool split = (sub.w & kSplitFlag) != 0;
+            const bool inside = y < e[1] && z < e[2];
+            const int64_t cell_yz = (int64_t)(o[1] + y) * g.nf[2] + (o[2] + z);
+#pragma unroll
+            for (int xi = 0; xi < 2; ++xi) {
+                // columns 32 hk + 16 xi ..: cell x = 2 hk + xi, (coil, re/im) pairs
+                float dv[16];
+                if (nb > 0) {
+                    tmem_ld_x16(tl + kMmaColD + 32u * hk + 16u * xi, dv);
+                    if (nb > kMmaGroup) {  // plus the drained groups
+                        float sv[16];
+                        tmem_ld_x16(tl + kMmaColS + 32u * hk + 16u * xi, sv);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) dv[i] += sv[i];
+                    } else {
+                        tmem_wait_ld();
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) dv[i] = 0.f;
+                }
+                const int x = 2 * hk + xi;
+                if (!inside || x >= e[0]) continue;
+                const int64_t cell = (int64_t)(o[0] + x) * g.nf[1] * g.nf[2] + cell_yz;
+#pragma unroll
+                for (int c = 0; c < CG; ++c) {
+                    if (cg0 + c >= g.n_coil) break;
+                    float2 *dst = a.grid + ((int64_t)grp * g.n_coil + cg0 + c) * g.G + cell;
+                    if (split) {
+                        atomicAdd(&dst->x, dv[2 * c]);
+                        atomicAdd(&dst->y, dv[2 * c + 1]);
+                    } else {
+                        *dst = make_float2(dv[2 * c], dv[2 * c + 1]);
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == kMmaWarp) tmem_dealloc(tbase, kMmaTmemCols);
+}
+
+}  // namespace gbn

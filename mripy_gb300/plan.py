@@ -68,7 +68,7 @@ class Tuning:
         self.interp_threads = interp_threads
         self.interp_coil_group = interp_coil_group
         self.interp_staging = interp_staging  # 0 tensor copies (TMA) where possible, 1 thread loads
-        self.spread_variant = spread_variant  # 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes
+        self.spread_variant = spread_variant  # 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes, 3 tensor cores
 
     def key(self):
         return (self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,

@@ -24,7 +24,8 @@ _CACHE = {}
 def _spread_candidates(dim, n_coil):
     """(tile, threads, coil_group, spread_variant) tuples: the register-tile kernels' own
     tiles (rows of 4 per warp, 4 columns per lane) for 4 and 8 coils per block, in 3-D with 8
-    coils also the cube kernel's tiles (8 or 16 cubes of 4^3 cells), plus shared-memory tiles."""
+    coils also the tensor-core kernel's 4 x 8 x 16 tile and the cube kernel's tiles (8 or 16
+    cubes of 4^3 cells), plus shared-memory tiles."""
     out = []
     groups = [cg for cg in (8, 4) if n_coil >= cg]
     if dim == 2:
@@ -43,6 +44,7 @@ def _spread_candidates(dim, n_coil):
                     if rows % ty == 0:
                         out.append(((rows // ty, ty, 4 * 32 // cg), th, cg, 1 if cg == 8 else 0))
         if n_coil >= 8:
+            out.append(((4, 8, 16), 256, 8, 3))
             for tile in ((8, 8, 8), (4, 8, 16), (8, 8, 16), (16, 8, 8)):
                 out.append((tile, 256, 8, 2))
         out += [((8, 8, 32), 256, 8, 0)]
@@ -150,9 +152,10 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
     best_s = best_i = None
     # spread tiling (interp at default), then interp tiling (spread at the winner)
     for tile, th, cg, var in _spread_candidates(dim, n_coil):
-        # the cube kernel needs long work items to keep its ring full: time it at 2048
+        # the cube and tensor-core kernels need long work items to keep their rings full:
+        # time them at 2048
         tu = Tuning(spread_tile=tile, threads=th, coil_group=cg, spread_variant=var,
-                    max_subproblem=2048 if var == 2 else 0)
+                    max_subproblem=2048 if var >= 2 else 0)
         try:
             t_s, _ = _measure(dim, shape, coords, n_coil, n_traj, traj_offsets, eps, tu, reps)
         except Exception:
@@ -177,7 +180,7 @@ def autotune(dim, shape, coords, n_coil=1, n_traj=1, traj_offsets=None, eps=5e-6
     if best_s is None or best_i is None:
         raise RuntimeError("no tuning candidate ran")
     best = None
-    for ms in ((1024, 2048, 4096, 8192) if best_s[4] == 2 else (64, 128, 256, 512, 1024)):
+    for ms in ((1024, 2048, 4096, 8192) if best_s[4] >= 2 else (64, 128, 256, 512, 1024)):
         tu = Tuning(spread_tile=best_s[1], threads=best_s[2], coil_group=best_s[3], interp_tile=best_i[1],
                     interp_threads=best_i[2], interp_coil_group=best_i[3], max_subproblem=ms,
                     spread_variant=best_s[4])

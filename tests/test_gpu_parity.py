@@ -253,7 +253,8 @@ def test_3d_warp_kernels_against_oracle(eps):
 
 
 @pytest.mark.parametrize("nc,tuning", [
-    (11, None),                                   # default: cube kernel on 8^3 tiles, coil groups of 8 and 3
+    (11, None),                                   # default: tensor cores on 4x8x16 tiles, coil groups of 8 and 3
+    (11, Tuning(spread_variant=2)),               # cube kernel on 8^3 tiles, coil groups of 8 and 3
     (11, Tuning(spread_variant=1)),               # register rows, tile 4x8x16, coil groups of 8 and 3
     (8, Tuning(threads=128, spread_variant=1)),   # register rows, tile 4x4x16
     (4, None),                                    # register tile 4x8x32, 4 coils per block
