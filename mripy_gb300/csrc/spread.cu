@@ -105,18 +105,24 @@ static cudaError_t launch_cube(const SpreadArgs &a, int64_t n_sub, cudaStream_t 
     return e;
 }
 
-// tensor-core kernel (one unit per block), then the compensated cube instance for the dense
-// units on the same tiles (4 x 8 x 16 = 8 cubes of 4^3)
+// tensor-core kernel (one unit per block): plain instance, then the compensated one for the
+// dense units
+template <int WT, bool KAHAN>
+static cudaError_t launch_mma_instance(const SpreadArgs &a, int64_t n_units, int n_cg, cudaStream_t s) {
+    auto kern = k_spread3d_mma<WT, KAHAN>;
+    const size_t smem = KAHAN ? kMmaSmemBytesK : kMmaSmemBytes;
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)n_units, kMmaThreads, smem, s>>>(a, a.status, n_cg);
+    return cudaGetLastError();
+}
+
 template <int WT>
 static cudaError_t launch_mma(const SpreadArgs &a, int64_t n_sub, cudaStream_t s) {
     const int n_cg = (a.g.n_coil + 7) / 8;
     const int64_t n_units = n_sub * n_cg;
-    auto kern = k_spread3d_mma<WT>;
-    cudaError_t e = set_smem(kern, kMmaSmemBytes);
-    if (e != cudaSuccess) return e;
-    kern<<<(unsigned)n_units, kMmaThreads, kMmaSmemBytes, s>>>(a, a.status, n_cg);
-    e = cudaGetLastError();
-    if (e == cudaSuccess && a.any_dense) e = launch_cube_instance<WT, 8, true>(a, n_units, n_cg, s);
+    cudaError_t e = launch_mma_instance<WT, false>(a, n_units, n_cg, s);
+    if (e == cudaSuccess && a.any_dense) e = launch_mma_instance<WT, true>(a, n_units, n_cg, s);
     return e;
 }
 

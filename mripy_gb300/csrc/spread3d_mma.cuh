@@ -16,12 +16,14 @@
 // average) but needs no per-cell instruction: the CUDA cores build 192 operand values per
 // (sample, tile) pair instead of issuing the stencil's FMAs.
 //
-// One (work item, coil group) unit per block, 13 warps:
-// * 4 loader warps fill a ring of kMmaSlots 32-sample batches (loader l: batches l, l + 4,
-//   ...): sample records by sample index, the tile's separable FP32 weights per sample
-//   (stored [tap][sample]), the 8 coil values times the optional density weight
-//   ([coil][sample]); `full` / `empty` mbarriers per slot.
-// * 8 builder warps turn a batch into the MMA operands: warp b writes A's hi and lo parts
+// One (work item, coil group) unit per block, 12 warps:
+// * 3 loader warps fill a ring of kMmaSlots 32-sample batches (loader l: batches l, l + 3,
+//   ...): per sample and dimension the first tap's tile plane and the distance of plane 0,
+//   and the 8 coil values times the optional density weight ([coil][sample]); `full` /
+//   `empty` mbarriers per slot.
+// * 8 builder warps first compute the batch's 28 tile-plane weights per sample together
+//   (stored [plane][sample]; a named barrier among them), then turn the batch into the MMA
+//   operands: warp b writes A's hi and lo parts
 //   for the 32 TMEM lanes of its quarter (b % 4) and 16 of the 32 samples (b / 4), and 8 of
 //   B's 64 rows into shared memory; two operand buffers, the one of batch t reused by batch
 //   t + 2 after the MMAs of batch t completed (`done` mbarrier, signalled by tcgen05.commit).
@@ -53,13 +55,20 @@ constexpr int kMmaM = kMmaTY * kMmaTZ;              // 128 cells (y, z): one TME
 constexpr int kMmaN = kMmaTX * 16;                  // 64 columns (x, coil, re/im)
 constexpr int kMmaBatch = 32;                       // samples per batch: one 128-byte K row
 constexpr int kMmaSlots = 8;                        // staged batches
-constexpr int kMmaLoaders = 4;
+#ifndef GBN_MMA_LOADERS
+#define GBN_MMA_LOADERS 3
+#endif
+constexpr int kMmaLoaders = GBN_MMA_LOADERS;
 constexpr int kMmaBuilders = 8;
 constexpr int kMmaWarp = kMmaBuilders + kMmaLoaders;  // the MMA warp's index
 constexpr int kMmaThreads = 32 * (kMmaWarp + 1);
 constexpr uint32_t kMmaTmemCols = 256;              // A (hi, lo) x 2 buffers: 0..127; D, S: 128..255
 constexpr uint32_t kMmaColD = 128;                  // the MMAs' accumulator
 constexpr uint32_t kMmaColS = 192;                  // the running sum of the drained accumulators
+// the compensated instance: two accumulators D (batch k in D[k % 2]), the running sum S and
+// its Kahan compensation C; one block per SM
+constexpr uint32_t kMmaTmemColsK = 512;
+constexpr uint32_t kMmaColSK = 256, kMmaColCK = 320;
 constexpr int kMmaGroup = 8;                        // batches the tensor core sums before a drain
 constexpr int kMmaWS = 36;  // floats per staged [tap] row of 32 samples: 16-byte aligned, 4-bank skew
 
@@ -69,7 +78,9 @@ constexpr uint32_t kMmaStWx = 0;                                        // [TX][
 constexpr uint32_t kMmaStWy = kMmaStWx + 4 * kMmaTX * kMmaWS;           // [TY][kMmaWS]
 constexpr uint32_t kMmaStWz = kMmaStWy + 4 * kMmaTY * kMmaWS;           // [TZ][kMmaWS]
 constexpr uint32_t kMmaStV = kMmaStWz + 4 * kMmaTZ * kMmaWS;            // [8 coils][32] float2
-constexpr uint32_t kMmaSlotBytes = kMmaStV + 8 * 8 * kMmaBatch;
+constexpr uint32_t kMmaStD0 = kMmaStV + 8 * 8 * kMmaBatch;              // [3][32] float: d of tap 0
+constexpr uint32_t kMmaStR = kMmaStD0 + 4 * 3 * kMmaBatch;              // [3][32] int: first tap's cell
+constexpr uint32_t kMmaSlotBytes = kMmaStR + 4 * 3 * kMmaBatch;
 constexpr uint32_t kMmaStageOff = 4 * kMmaBOp;                          // after B (hi, lo) x 2 buffers
 constexpr uint32_t kMmaBarOff = kMmaStageOff + kMmaSlots * kMmaSlotBytes;
 constexpr uint32_t kMmaBars = 2 * kMmaSlots + 4;                        // full, empty, ops[2], done[2]
@@ -77,13 +88,37 @@ constexpr uint32_t kMmaBars = 2 * kMmaSlots + 4;                        // full,
 // most two blocks (2 x 256 TMEM columns) share an SM and tcgen05.alloc never waits.
 constexpr size_t kMmaSmemBytes = kMmaBarOff + 8 * kMmaBars + 16 + 1024;
 static_assert(kMmaSmemBytes > 228 * 1024 / 3, "two blocks per SM at most");
+// the compensated instance asks for more than half the SM's shared memory: one block per SM
+// holds all 512 TMEM columns
+constexpr size_t kMmaSmemBytesK = 116 * 1024;
+static_assert(kMmaSmemBytesK > 228 * 1024 / 2 && kMmaSmemBytesK >= kMmaSmemBytes, "one block per SM");
 static_assert(kMmaStV % 16 == 0 && kMmaSlotBytes % 16 == 0, "16-byte aligned staging");
+constexpr int kMmaTaps = kMmaTX + kMmaTY + kMmaTZ;  // 28 tile-plane weights per sample
 
-// x = hi + lo: hi rounded to the TF32 grid (ties away from zero, by integer arithmetic on the
-// bit pattern), lo = x - hi exactly; the tensor core reads lo's top 11 significant bits
-__device__ __forceinline__ void tf32_split_fast(float x, float &hi, float &lo) {
-    hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-    lo = x - hi;
+// 2^x (PTX ex2.approx, flushing subnormal results to zero: the Gaussian's smallest weight
+// inside the stencil is ~eps, far above the subnormal range)
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Two products x = a * b (one packed FP32x2 multiply) split as x = hi + lo: hi rounded to
+// the TF32 grid (11 significant bits; ties away from zero, by integer arithmetic on the bit
+// pattern), lo = x - hi exactly (one packed subtraction).  The tensor core reads lo's top 11
+// significant bits.  (Dekker's split t = x (2^13 + 1), hi = t - (t - x) in packed FP32x2
+// arithmetic was measured on GB300 to return hi = x, lo = 0, so it is not used.)
+__device__ __forceinline__ float tf32_round_bits(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+// (Rounding lo to the TF32 grid as well and adding the lo * lo MMA left the compensated
+// instance's centre-cell error unchanged, 3.9e-7 against 3.8e-7 on the 3-D radial test
+// data, and cost 0.09 ms of 6.0 on the 3-D radial workload: the tensor core's own FP32
+// accumulation within a batch dominates, so neither is done.)
+__device__ __forceinline__ void tf32_split2(float2 a, float2 b, float2 &hi, float2 &lo) {
+    const float2 x = __fmul2_rn(a, b);
+    hi = make_float2(tf32_round_bits(x.x), tf32_round_bits(x.y));
+    lo = __fadd2_rn(x, make_float2(-hi.x, -hi.y));
 }
 
 // S (+)= D over this thread's lane and the 32 columns of half hk; `first`: S = D
@@ -105,8 +140,39 @@ __device__ __forceinline__ void mma_drain(uint32_t tl, int hk, bool first) {
     }
 }
 
-template <int WT>
-__global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, uint32_t *status, int n_cg) {
+// S, C (+)= D[col_d] with Kahan compensation over this thread's lane and the 32 columns of
+// half hk (scalar FP32 operations); `first`: S = D, C = 0
+__device__ __forceinline__ void mma_drain_kahan(uint32_t tl, int hk, uint32_t col_d, bool first) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t col = 32u * hk + 16u * h;
+        float d[16], s[16], c[16];
+        tmem_ld_x16(tl + col_d + col, d);
+        if (first) {
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) c[i] = 0.f;
+            tmem_st_x16(tl + kMmaColSK + col, d);
+        } else {
+            tmem_ld_x16(tl + kMmaColSK + col, s);
+            tmem_ld_x16(tl + kMmaColCK + col, c);
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const float y = d[i] - c[i];
+                const float t = s[i] + y;
+                c[i] = (t - s[i]) - y;
+                s[i] = t;
+            }
+            tmem_st_x16(tl + kMmaColSK + col, s);
+        }
+        tmem_st_x16(tl + kMmaColCK + col, c);
+    }
+}
+
+template <int WT, bool KAHAN>
+__global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(SpreadArgs a, uint32_t *status, int n_cg) {
+    constexpr uint32_t kCols = KAHAN ? kMmaTmemColsK : kMmaTmemCols;
     constexpr int B = kMmaBatch;
     constexpr int CG = 8;
     extern __shared__ unsigned char smem_mma_raw[];
@@ -124,7 +190,7 @@ __global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, u
     const int W = WT ? WT : g.W;
 
     if (warp == kMmaWarp) {
-        tmem_alloc(tslot, kMmaTmemCols);
+        tmem_alloc(tslot, kCols);
         tmem_relinquish();
     }
     if (threadIdx.x == 0) {
@@ -145,14 +211,14 @@ __global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, u
 
     const int64_t unit = blockIdx.x;
     int4 sub;
-    if (cube_unit(a.subs, unit, n_cg, false, sub)) {
+    if (cube_unit(a.subs, unit, n_cg, KAHAN, sub)) {
         const int nb = (sub.z + B - 1) / B;
         const int cg0 = (int)(unit % n_cg) * CG;
-        int o[3], e[3];
-        tile_coords<3>(g, sub.x % g.ntiles, o, e);
 
         if (warp >= kMmaBuilders && warp < kMmaWarp) {
             // ------------------------------------------------------------ loader warp
+            int o[3], e[3];
+            tile_coords<3>(g, sub.x % g.ntiles, o, e);
             const int lw = warp - kMmaBuilders;
             const int ns = g.ns;
             const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
@@ -194,15 +260,17 @@ __global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, u
                     !mbar_wait_bounded(&empty[slot], (uint32_t)((k / kMmaSlots - 1) & 1)) && lane == 0)
                     atomicOr(status, kStatusSpreadTimeout);
                 unsigned char *sl = stage + (size_t)slot * kMmaSlotBytes;
-                float *wx = reinterpret_cast<float *>(sl + kMmaStWx);
-                float *wy = reinterpret_cast<float *>(sl + kMmaStWy);
-                float *wz = reinterpret_cast<float *>(sl + kMmaStWz);
-#pragma unroll
-                for (int t = 0; t < kMmaTX; ++t) wx[t * kMmaWS + lane] = tap_weight(ok, t - r[0], W, pt.x, ns, g.beta2[0]);
-#pragma unroll
-                for (int t = 0; t < kMmaTY; ++t) wy[t * kMmaWS + lane] = tap_weight(ok, t - r[1], W, pt.y, ns, g.beta2[1]);
-#pragma unroll
-                for (int t = 0; t < kMmaTZ; ++t) wz[t * kMmaWS + lane] = tap_weight(ok, t - r[2], W, pt.z, ns, g.beta2[2]);
+                // per dimension: the distance of tile plane 0 from the sample (plane t: d0 - t)
+                // and the plane of the first tap; a lane without a sample gets a first tap
+                // no plane reaches, so all its weights are 0
+                float *d0 = reinterpret_cast<float *>(sl + kMmaStD0);
+                int *rs = reinterpret_cast<int *>(sl + kMmaStR);
+                d0[lane] = pt.x + (float)(ns - 1 + r[0]);
+                d0[B + lane] = pt.y + (float)(ns - 1 + r[1]);
+                d0[2 * B + lane] = pt.z + (float)(ns - 1 + r[2]);
+                rs[lane] = ok ? r[0] : -(1 << 20);
+                rs[B + lane] = ok ? r[1] : -(1 << 20);
+                rs[2 * B + lane] = ok ? r[2] : -(1 << 20);
                 float2 *vs = reinterpret_cast<float2 *>(sl + kMmaStV);
 #pragma unroll
                 for (int cc = 0; cc < CG; ++cc) vs[cc * B + lane] = v[cc];
@@ -217,12 +285,14 @@ __global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, u
                     const int buf = k & 1;
                     if (!mbar_wait_bounded(&ops[buf], (uint32_t)((k >> 1) & 1))) atomicOr(status, kStatusSpreadTimeout);
                     tc_fence_after();
-                    const uint32_t ah = tbase + 64u * buf, al = ah + 32u, d = tbase + kMmaColD;
+                    const uint32_t ah = tbase + 64u * buf, al = ah + 32u;
+                    const uint32_t d = tbase + kMmaColD + (KAHAN ? 64u * buf : 0u);
                     const uint32_t bh = b0 + 2u * buf * kMmaBOp, bl = bh + kMmaBOp;
 #pragma unroll
                     for (int jk = 0; jk < B / 8; ++jk) {
+                        // plain: a group's first MMA starts D afresh; compensated: every batch's
                         tc_mma_tf32_ts(d, ah + 8u * jk, tc_desc_sw128(bh + 32u * jk), idesc,
-                                       (k % kMmaGroup) != 0 || jk != 0);
+                                       KAHAN ? jk != 0 : ((k % kMmaGroup) != 0 || jk != 0));
                         tc_mma_tf32_ts(d, ah + 8u * jk, tc_desc_sw128(bl + 32u * jk), idesc, 1u);
                         tc_mma_tf32_ts(d, al + 8u * jk, tc_desc_sw128(bh + 32u * jk), idesc, 1u);
                     }
@@ -240,24 +310,61 @@ __global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, u
                 const int slot = k % kMmaSlots, buf = k & 1;
                 if (!mbar_wait_bounded(&full[slot], (uint32_t)((k / kMmaSlots) & 1)) && lane == 0)
                     atomicOr(status, kStatusSpreadTimeout);
+                {
+                    // the batch's 28 plane weights per sample, shared by the builder warps:
+                    // warp b computes planes b, b + 8, b + 16, b + 24 of sample `lane`
+                    unsigned char *slw = stage + (size_t)slot * kMmaSlotBytes;
+                    const float *d0 = reinterpret_cast<const float *>(slw + kMmaStD0);
+                    const int *rs = reinterpret_cast<const int *>(slw + kMmaStR);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int jt = warp + 8 * i;
+                        if (jt >= kMmaTaps) break;
+                        const int dim = jt < kMmaTX ? 0 : (jt < kMmaTX + kMmaTY ? 1 : 2);
+                        const int t = jt - (dim == 0 ? 0 : (dim == 1 ? kMmaTX : kMmaTX + kMmaTY));
+                        const float d = d0[dim * B + lane] - (float)t;
+                        // (a parameter array indexed at run time would be copied to local memory)
+                        const float beta = dim == 0 ? g.beta2[0] : (dim == 1 ? g.beta2[1] : g.beta2[2]);
+                        const float wv = ex2_approx(-beta * d * d);
+                        const bool in = (unsigned)(t - rs[dim * B + lane]) < (unsigned)W;
+                        reinterpret_cast<float *>(slw + (dim == 0 ? kMmaStWx : (dim == 1 ? kMmaStWy : kMmaStWz)))
+                            [t * kMmaWS + lane] = in ? wv : 0.f;
+                    }
+                    asm volatile("bar.sync 1, %0;" ::"n"(kMmaBuilders * 32) : "memory");
+                }
                 // the MMAs of batch k - 2 (same operand buffer) have completed
                 if (k >= 2 && !mbar_wait_bounded(&done[buf], (uint32_t)(((k >> 1) - 1) & 1)) && lane == 0)
                     atomicOr(status, kStatusSpreadTimeout);
+                if (KAHAN && k >= 2) {
+                    // batch k - 2's accumulator D[k % 2] into S, C before batch k overwrites it
+                    tc_fence_after();
+                    mma_drain_kahan(tl, hk, kMmaColD + 64u * buf, k == 2);
+                }
                 const unsigned char *sl = stage + (size_t)slot * kMmaSlotBytes;
                 // A: cells (y, z) of this lane, samples 16 hk .. 16 hk + 15
                 const float4 *wy4 = reinterpret_cast<const float4 *>(sl + kMmaStWy) + (y * kMmaWS + 16 * hk) / 4;
                 const float4 *wz4 = reinterpret_cast<const float4 *>(sl + kMmaStWz) + (z * kMmaWS + 16 * hk) / 4;
-                float hi[16], lo[16];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const float4 p = wy4[i], s = wz4[i];
-                    tf32_split_fast(p.x * s.x, hi[4 * i], lo[4 * i]);
-                    tf32_split_fast(p.y * s.y, hi[4 * i + 1], lo[4 * i + 1]);
-                    tf32_split_fast(p.z * s.z, hi[4 * i + 2], lo[4 * i + 2]);
-                    tf32_split_fast(p.w * s.w, hi[4 * i + 3], lo[4 * i + 3]);
+                for (int h = 0; h < 2; ++h) {  // 8 samples at a time: fewer live registers
+                    float hi[8], lo[8];
+#pragma unroll
+                    for (int i = 0; i < 2; ++i) {
+                        const float4 p = wy4[2 * h + i], s = wz4[2 * h + i];
+                        float2 h0, l0, h1, l1;
+                        tf32_split2(make_float2(p.x, p.y), make_float2(s.x, s.y), h0, l0);
+                        tf32_split2(make_float2(p.z, p.w), make_float2(s.z, s.w), h1, l1);
+                        hi[4 * i] = h0.x;
+                        hi[4 * i + 1] = h0.y;
+                        hi[4 * i + 2] = h1.x;
+                        hi[4 * i + 3] = h1.y;
+                        lo[4 * i] = l0.x;
+                        lo[4 * i + 1] = l0.y;
+                        lo[4 * i + 2] = l1.x;
+                        lo[4 * i + 3] = l1.y;
+                    }
+                    tmem_st_x8(tl + 64u * buf + 16u * hk + 8u * h, hi);
+                    tmem_st_x8(tl + 64u * buf + 32u + 16u * hk + 8u * h, lo);
                 }
-                tmem_st_x16(tl + 64u * buf + 16u * hk, hi);
-                tmem_st_x16(tl + 64u * buf + 32u + 16u * hk, lo);
                 // B: rows (bx, coil, re/im) for sample `lane`
                 const float wxk = reinterpret_cast<const float *>(sl + kMmaStWx)[bx * kMmaWS + lane];
                 const float2 *vs = reinterpret_cast<const float2 *>(sl + kMmaStV);
@@ -266,16 +373,15 @@ __global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, u
                 for (int cc = 0; cc < 4; ++cc) {
                     const float2 vv = vs[(bc0 + cc) * B + lane];
                     const int nre = bx * 16 + (bc0 + cc) * 2;
-                    float h, l;
-                    tf32_split_fast(wxk * vv.x, h, l);
-                    *reinterpret_cast<float *>(bh + sw128_offset(nre, lane)) = h;
-                    *reinterpret_cast<float *>(bl + sw128_offset(nre, lane)) = l;
-                    tf32_split_fast(wxk * vv.y, h, l);
-                    *reinterpret_cast<float *>(bh + sw128_offset(nre + 1, lane)) = h;
-                    *reinterpret_cast<float *>(bl + sw128_offset(nre + 1, lane)) = l;
+                    float2 h, l;
+                    tf32_split2(make_float2(wxk, wxk), vv, h, l);
+                    *reinterpret_cast<float *>(bh + sw128_offset(nre, lane)) = h.x;
+                    *reinterpret_cast<float *>(bl + sw128_offset(nre, lane)) = l.x;
+                    *reinterpret_cast<float *>(bh + sw128_offset(nre + 1, lane)) = h.y;
+                    *reinterpret_cast<float *>(bl + sw128_offset(nre + 1, lane)) = l.y;
                 }
                 mbar_arrive(&empty[slot]);
-                if (k % kMmaGroup == 0 && k > 0) {
+                if (!KAHAN && k % kMmaGroup == 0 && k > 0) {
                     // batch k starts a new group: once the previous group's MMAs are done,
                     // add its accumulator into S (the same phase is waited for again at
                     // k + 1, which returns at once)
@@ -298,16 +404,34 @@ __global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, u
                 if (!mbar_wait_bounded(&done[kl & 1], (uint32_t)((kl >> 1) & 1)) && lane == 0)
                     atomicOr(status, kStatusSpreadTimeout);
                 tc_fence_after();
+                if constexpr (KAHAN) {
+                    // the last two batches' accumulators, in order
+                    for (int j = max(0, nb - 2); j < nb; ++j) {
+                        mma_drain_kahan(tl, hk, kMmaColD + 64u * (j & 1), j == 0);
+                        tmem_wait_st();  // S and C stored before the next drain reads them
+                    }
+                }
             }
-            const int grp = sub.x / g.ntiles;
-            const bool split = (sub.w & kSplitFlag) != 0;
+            // the unit's tile, read again here rather than kept in registers through the loop
+            const int4 su = a.subs[unit / n_cg];
+            int o[3], e[3];
+            tile_coords<3>(g, su.x % g.ntiles, o, e);
+            const int grp = su.x / g.ntiles;
+            const bool split = (su.w & kSplitFlag) != 0;
             const bool inside = y < e[1] && z < e[2];
             const int64_t cell_yz = (int64_t)(o[1] + y) * g.nf[2] + (o[2] + z);
 #pragma unroll
             for (int xi = 0; xi < 2; ++xi) {
                 // columns 32 hk + 16 xi ..: cell x = 2 hk + xi, (coil, re/im) pairs
                 float dv[16];
-                if (nb > 0) {
+                if (nb > 0 && KAHAN) {
+                    float cv[16];
+                    tmem_ld_x16(tl + kMmaColSK + 32u * hk + 16u * xi, dv);
+                    tmem_ld_x16(tl + kMmaColCK + 32u * hk + 16u * xi, cv);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) dv[i] -= cv[i];
+                } else if (nb > 0) {
                     tmem_ld_x16(tl + kMmaColD + 32u * hk + 16u * xi, dv);
                     if (nb > kMmaGroup) {  // plus the drained groups
                         float sv[16];
@@ -342,7 +466,7 @@ __global__ void __launch_bounds__(kMmaThreads, 2) k_spread3d_mma(SpreadArgs a, u
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == kMmaWarp) tmem_dealloc(tbase, kMmaTmemCols);
+    if (warp == kMmaWarp) tmem_dealloc(tbase, kCols);
 }
 
 }  // namespace gbn
