@@ -92,6 +92,16 @@ def _sm_max_mhz():
         return 2070.0
 
 
+def tf32_peak_tflops():
+    """TF32 tensor rate: half the measured cuBLAS BF16 burst rate (MEASURED_PEAKS.json), else
+    half the fallback 1.9 PFLOP/s."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["bf16_tflops"]) / 2
+    except Exception:
+        return 1900.0 / 2
+
+
 def fp32_peak_tflops():
     """Nominal FP32 CUDA-core peak: 152 SMs x 128 FMA lanes x 2 flop x max SM clock."""
     return 152 * 128 * 2 * _sm_max_mhz() * 1e6 / 1e12
@@ -435,6 +445,19 @@ def run_gpu(args, wl):
         "peaks": {"hbm_gbs": hbm, "fp32_tflops": round(fp32_peak, 1), "smem_tbs": round(smem_peak, 1)},
         "peak_note": "FP32 and shared-memory peaks are nominal (152 SMs x 128 FMA lanes, x 128 B/clk) at the "
                      "measured max SM clock"}
+    if info.get("spread_variant") == 3:
+        # the tensor-core spread: 3 TF32 MMAs (hi*hi, hi*lo, lo*hi) of M = 128 cells x N = 64
+        # (4 x-planes x 8 coils x re/im) per (sample, tile) pair; TF32 runs at half the BF16
+        # rate, so the reference is the measured cuBLAS BF16 burst / 2
+        mma_flop = info["spread_entries"] * 3 * 2 * 128 * 64
+        tf32_peak = tf32_peak_tflops()
+        result["roofline"]["spread_tensor"] = {
+            "kernel": "k_spread3d_mma", "mma_tflop_per_launch": round(mma_flop / 1e12, 3),
+            "achieved_tflops": round(mma_flop / (t_spread * 1e-3) / 1e12, 1), "peak_tflops": round(tf32_peak, 1),
+            "frac": round(mma_flop / (t_spread * 1e-3) / 1e12 / tf32_peak, 4),
+            "peak_source": "of measured (MEASURED_PEAKS.json bf16_tflops / 2: TF32 at half the BF16 rate)",
+            "stencil_fp32_tflops": round(fl / (t_spread * 1e-3) / 1e12, 2),
+            "stencil_fp32_frac": round(fl / (t_spread * 1e-3) / 1e12 / fp32_peak, 4)}
     result["kernels_ms"] = {"interp": round(t_interp, 4), "spread": round(t_spread, 4), "pad_deapod": round(t_pad, 4),
                             "fft": round(t_fft, 4), "crop_deapod": round(t_crop, 4)}
     # this library's kernels per step (cuFFT and memsets not counted): pad, interp, crop and

@@ -110,6 +110,8 @@ typedef struct {
     int32_t spread_kernels;    /* kernels the plan's last spread launched (0 before one) */
     int64_t split_tiles;       /* spread tiles shared by several work items (float atomics; 0 means
                                   the spread is bitwise reproducible run to run) */
+    int32_t spread_variant;    /* the 3-D spread kernel this plan runs with 8 coils per block:
+                                  1 warp rows, 2 cubes, 3 tensor cores; 0 for the others */
 } gbn_plan_info;
 
 /* element strides (in complex64 elements) of a strided complex array */

@@ -954,6 +954,7 @@ int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     o->dense_subproblems = p->n_dense_sub;
     o->spread_kernels = p->spread_kernels;
     o->split_tiles = p->n_split;
+    o->spread_variant = spread_path_kind(p->gs, spread_cg(p), p->spread_variant, p->threads);
     o->device_bytes = (int64_t)p->device_bytes;
     return GBN_OK;
 }

@@ -162,6 +162,8 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
                           cudaStream_t s);
 // the 3-D cube spread runs these arguments (the kernel that reads interleaved work items)
 bool spread_cube_applies(const Geom &g, int coil_group, int variant);
+// the 3-D 8-coil spread kernel launch_spread runs: 3 tensor cores, 2 cubes, 1 warp rows, 0 other
+int spread_path_kind(const Geom &g, int coil_group, int variant, int threads);
 // kernels launch_spread runs for these arguments (the 3-D register path adds a Kahan instance)
 int spread_kernel_count(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads);
 cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, int threads,

@@ -68,6 +68,13 @@ bool spread_cube_applies(const Geom &g, int coil_group, int variant) {
     return cube_path(g, coil_group, variant) != 0 || mma_path(g, coil_group, variant);
 }
 
+int spread_path_kind(const Geom &g, int coil_group, int variant, int threads) {
+    if (g.dim != 3 || coil_group != 8) return 0;
+    if (mma_path(g, coil_group, variant)) return 3;
+    if (cube_path(g, coil_group, variant)) return 2;
+    return reg3d_path(g, coil_group, threads) ? 1 : 0;
+}
+
 int spread_kernel_count(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads) {
     if (n_sub == 0) return 0;
     const bool two = cube_path(a.g, coil_group, a.variant) || mma_path(a.g, coil_group, a.variant) ||
