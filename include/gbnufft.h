@@ -85,7 +85,13 @@ typedef struct {
                                    2 = 4^3-cell cubes fed by producer warps (tile of 8 or 16
                                    cubes; default work items of 2048 samples),
                                    3 = tensor cores (tcgen05 TF32 MMAs, 3-term split; tile
-                                   4 x 8 x 16; dense items on the compensated cubes) */
+                                   4 x 8 x 16; dense items on a compensated instance) */
+    int32_t interp_variant;     /* 3-D interp with 8 coils per group: 0 = library choice (tensor
+                                   cores whenever the spread's tiles are the tensor-core
+                                   kernel's 4 x 8 x 16), 1 = the plane-streaming / window
+                                   kernels on the interp's own bins, 2 = tensor cores where
+                                   the spread's tiles allow (per tile a TF32 GEMM over the
+                                   tile's samples, partial sums added with float atomics) */
 } gbn_plan_desc;
 
 typedef struct {

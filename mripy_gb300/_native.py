@@ -43,7 +43,7 @@ class PlanDesc(ctypes.Structure):
         ("max_subproblem", ctypes.c_int32), ("coil_group", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("interp_threads", ctypes.c_int32), ("interp_coil_group", ctypes.c_int32),
         ("interp_staging", ctypes.c_int32), ("dense_tile_samples", ctypes.c_int32),
-        ("spread_variant", ctypes.c_int32),
+        ("spread_variant", ctypes.c_int32), ("interp_variant", ctypes.c_int32),
     ]
 
 

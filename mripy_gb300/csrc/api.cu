@@ -83,6 +83,7 @@ struct gbn_plan {
     Geom gs{}, gi{};
     int coil_group = 1, threads = 256, interp_threads = 256, max_sub = 256, interp_coil_group = 0;
     int interp_staging = 0;  // 0: tensor copies where the grid allows, 1: thread loads
+    int interp_variant = 0;  // 3-D, 8 coils: 0 library choice, 1 interp bins, 2 tensor cores
     int spread_variant = 0;  // 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes, 3 tensor cores
     bool spread_items_interleaved = false;  // split tiles' work items interleave (cube kernel)
     int dense_min = kDenseDefault;  // 3-D spread tiles with this many samples use compensated sums (0: never)
@@ -391,8 +392,28 @@ bool grid_tensor_map3d(gbn_plan *p, const float2 *grid, int cg, int BY, int BZ) 
     return true;
 }
 
+// the tensor-core interp runs this plan's interps (on the spread's tiles and work lists)
+bool interp_on_tensor_cores(const gbn_plan *p) {
+    return p->interp_variant != 1 && interp_mma_applies(p->gs, spread_cg(p));
+}
+
 int run_interp(gbn_plan *p, const float2 *grid, void *c, gbn_layout L, const float *weight, cudaStream_t s) {
     NvtxRange range("gbn interp");
+    if (interp_on_tensor_cores(p)) {
+        MmaInterpArgs m;
+        m.g = p->gs;
+        m.subs = p->spread_subs.as<int4>();
+        m.idx = p->dup_idx.as<uint32_t>();
+        m.pts_by_sample = p->pts.as<float4>();
+        m.grid = grid;
+        m.c = (float2 *)c;
+        m.c_elem = L.elem_stride;
+        m.c_coil = L.coil_stride;
+        m.weight = weight;
+        m.M = p->M;
+        GBN_CUDA(launch_interp3d_mma(m, p->n_spread_sub, p->kstatus, s));
+        return GBN_OK;
+    }
     InterpArgs a;
     a.g = p->gi;
     a.subs = p->interp_subs.as<int4>();
@@ -719,6 +740,11 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         return fail(GBN_ERR_ARG, "interp_staging must be 0 or 1");
     }
     p->interp_staging = desc->interp_staging;
+    if (desc->interp_variant < 0 || desc->interp_variant > 2) {
+        delete p;
+        return fail(GBN_ERR_ARG, "interp_variant must be 0, 1 or 2");
+    }
+    p->interp_variant = desc->interp_variant;
     if (desc->spread_variant < 0 || desc->spread_variant > 3) {
         delete p;
         return fail(GBN_ERR_ARG, "spread_variant must be 0, 1, 2 or 3");

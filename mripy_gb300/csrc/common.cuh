@@ -156,6 +156,21 @@ struct GradArgs {
     float *out;               // (M, dim)
     float scale;              // df
 };
+// the 3-D tensor-core interp: the spread's tiles and (sample, tile) work lists
+struct MmaInterpArgs {
+    Geom g;                       // the spread's geometry (4 x 8 x 16 tiles)
+    const int4 *subs;             // the spread's work items
+    const uint32_t *idx;          // (sample, tile) list: sample index per entry
+    const float4 *pts_by_sample;  // per sample: in-cell fractions, first-tap cells
+    const float2 *grid;
+    float2 *c;                    // output samples (zeroed by the launcher)
+    int64_t c_elem, c_coil;
+    const float *weight;          // per sample or null
+    int64_t M;                    // samples (all groups)
+};
+// whether the tensor-core interp takes this spread geometry and coil group
+bool interp_mma_applies(const Geom &gs, int coil_group);
+cudaError_t launch_interp3d_mma(const MmaInterpArgs &a, int64_t n_sub, uint32_t *status, cudaStream_t s);
 cudaError_t launch_zero_split(const Geom &g, const uint32_t *split_tiles, int64_t n_split, float2 *grid,
                               cudaStream_t s);
 cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads,

@@ -12,6 +12,7 @@
 #include "grid2d_kernels.cuh"
 #include "grid3d_kernels.cuh"
 #include "interp2d_tma.cuh"
+#include "interp3d_mma.cuh"
 
 namespace gbn {
 
@@ -107,6 +108,46 @@ cudaError_t launch_interp(const InterpArgs &a, int64_t n_sub, int coil_group, in
             err = cudaGetLastError();
         }
     })));
+    return err;
+}
+
+// ---------------------------------------------------------------- tensor-core 3-D interp
+
+bool interp_mma_applies(const Geom &gs, int coil_group) {
+    return gs.dim == 3 && coil_group == 8 && grid3d_applies(gs) && gs.tile[0] == kMmaTX && gs.tile[1] == kMmaTY &&
+           gs.tile[2] == kMmaTZ;
+}
+
+namespace {
+// the output samples start from zero: the kernel adds every (sample, tile) partial
+__global__ void k_zero_samples(float2 *c, int64_t M, int n_coil, int64_t c_elem, int64_t c_coil) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M * n_coil) return;
+    const int64_t j = i / n_coil, coil = i - j * n_coil;
+    c[j * c_elem + coil * c_coil] = make_float2(0.f, 0.f);
+}
+}  // namespace
+
+cudaError_t launch_interp3d_mma(const MmaInterpArgs &a, int64_t n_sub, uint32_t *status, cudaStream_t s) {
+    const int64_t n = a.M * a.g.n_coil;
+    if (n == 0) return cudaSuccess;
+    if (a.c_coil == 1 && a.c_elem == a.g.n_coil) {
+        cudaError_t e = cudaMemsetAsync(a.c, 0, sizeof(float2) * (size_t)n, s);
+        if (e != cudaSuccess) return e;
+    } else {
+        k_zero_samples<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.c, a.M, a.g.n_coil, a.c_elem, a.c_coil);
+    }
+    if (n_sub == 0) return cudaGetLastError();
+    const int n_cg = (a.g.n_coil + 7) / 8;
+    cudaError_t err = cudaSuccess;
+    GBN_DISPATCH_W(a.g.W, {
+        auto kern = k_interp3d_mma<WT>;
+        err = set_smem(kern, kImSmemBytes);
+        if (err == cudaSuccess) {
+            kern<<<(unsigned)(n_sub * n_cg), kImThreads, kImSmemBytes, s>>>(a, status, n_cg);
+            err = cudaGetLastError();
+        }
+    });
     return err;
 }
 

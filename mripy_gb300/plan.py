@@ -59,7 +59,7 @@ class Tuning:
     """Kernel tiling chosen by the autotuner (0 = library default)."""
 
     def __init__(self, spread_tile=(0, 0, 0), interp_tile=(0, 0, 0), max_subproblem=0, coil_group=0, threads=0,
-                 interp_threads=0, interp_coil_group=0, interp_staging=0, spread_variant=0):
+                 interp_threads=0, interp_coil_group=0, interp_staging=0, spread_variant=0, interp_variant=0):
         self.spread_tile = tuple(spread_tile) + (0,) * (3 - len(spread_tile))
         self.interp_tile = tuple(interp_tile) + (0,) * (3 - len(interp_tile))
         self.max_subproblem = max_subproblem
@@ -69,16 +69,20 @@ class Tuning:
         self.interp_coil_group = interp_coil_group
         self.interp_staging = interp_staging  # 0 tensor copies (TMA) where possible, 1 thread loads
         self.spread_variant = spread_variant  # 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes, 3 tensor cores
+        self.interp_variant = interp_variant  # 3-D, 8 coils: 0 library choice, 1 plane streaming, 2 tensor cores
 
     def key(self):
         return (self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
-                self.interp_threads, self.interp_coil_group, self.interp_staging, self.spread_variant)
+                self.interp_threads, self.interp_coil_group, self.interp_staging, self.spread_variant,
+                self.interp_variant)
 
     def __repr__(self):
         return ("Tuning(spread_tile=%s, interp_tile=%s, max_subproblem=%d, coil_group=%d, threads=%d, "
-                "interp_threads=%d, interp_coil_group=%d, interp_staging=%d, spread_variant=%d)" % (
+                "interp_threads=%d, interp_coil_group=%d, interp_staging=%d, spread_variant=%d, "
+                "interp_variant=%d)" % (
                     self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
-                    self.interp_threads, self.interp_coil_group, self.interp_staging, self.spread_variant))
+                    self.interp_threads, self.interp_coil_group, self.interp_staging, self.spread_variant,
+                    self.interp_variant))
 
 
 class Graph:
@@ -141,6 +145,7 @@ class NufftPlan:
         d.interp_staging = int(self.tuning.interp_staging)
         d.dense_tile_samples = int(dense_tile_samples)
         d.spread_variant = int(getattr(self.tuning, "spread_variant", 0))
+        d.interp_variant = int(getattr(self.tuning, "interp_variant", 0))
         self._lib = N.lib()
         h = ctypes.c_void_p()
         N.check(self._lib.gbn_plan_create(ctypes.byref(d), ctypes.byref(h)))
