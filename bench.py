@@ -445,6 +445,16 @@ def run_gpu(args, wl):
         "peaks": {"hbm_gbs": hbm, "fp32_tflops": round(fp32_peak, 1), "smem_tbs": round(smem_peak, 1)},
         "peak_note": "FP32 and shared-memory peaks are nominal (152 SMs x 128 FMA lanes, x 128 B/clk) at the "
                      "measured max SM clock"}
+    if info.get("interp_variant") == 2:
+        # the tensor-core interp: per (sample, tile) pair 3 TF32 MMAs' worth of M = 128
+        # samples x N = 64 over K = 128 (y, z) cells, as the spread
+        mma_flop_i = info["spread_entries"] * 3 * 2 * 128 * 64
+        result["roofline"]["interp_tensor"] = {
+            "kernel": "k_interp3d_mma", "mma_tflop_per_launch": round(mma_flop_i / 1e12, 3),
+            "achieved_tflops": round(mma_flop_i / (t_interp * 1e-3) / 1e12, 1),
+            "peak_tflops": round(tf32_peak_tflops(), 1),
+            "frac": round(mma_flop_i / (t_interp * 1e-3) / 1e12 / tf32_peak_tflops(), 4),
+            "peak_source": "of measured (MEASURED_PEAKS.json bf16_tflops / 2: TF32 at half the BF16 rate)"}
     if info.get("spread_variant") == 3:
         # the tensor-core spread: 3 TF32 MMAs (hi*hi, hi*lo, lo*hi) of M = 128 cells x N = 64
         # (4 x-planes x 8 coils x re/im) per (sample, tile) pair; TF32 runs at half the BF16

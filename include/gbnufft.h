@@ -118,6 +118,9 @@ typedef struct {
                                   the spread is bitwise reproducible run to run) */
     int32_t spread_variant;    /* the 3-D spread kernel this plan runs with 8 coils per block:
                                   1 warp rows, 2 cubes, 3 tensor cores; 0 for the others */
+    int32_t interp_variant;    /* 2 when the interp runs on the tensor cores (3-D, 8 coils per
+                                  group; partial sums added with float atomics, so the
+                                  samples agree run to run to rounding), else 1 */
 } gbn_plan_info;
 
 /* element strides (in complex64 elements) of a strided complex array */

@@ -57,6 +57,7 @@ class PlanInfo(ctypes.Structure):
         ("interp_threads", ctypes.c_int32), ("max_subproblem", ctypes.c_int32), ("device_bytes", ctypes.c_int64),
         ("interp_coil_group", ctypes.c_int32), ("dense_subproblems", ctypes.c_int64),
         ("spread_kernels", ctypes.c_int32), ("split_tiles", ctypes.c_int64), ("spread_variant", ctypes.c_int32),
+        ("interp_variant", ctypes.c_int32),
     ]
 
 

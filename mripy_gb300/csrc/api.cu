@@ -981,6 +981,7 @@ int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     o->spread_kernels = p->spread_kernels;
     o->split_tiles = p->n_split;
     o->spread_variant = spread_path_kind(p->gs, spread_cg(p), p->spread_variant, p->threads);
+    o->interp_variant = interp_on_tensor_cores(p) ? 2 : 1;
     o->device_bytes = (int64_t)p->device_bytes;
     return GBN_OK;
 }
@@ -1435,9 +1436,11 @@ int gbn_type2_host(gbn_plan *p, const void *h_img, void *h_c, gbn_stream_t strea
     if ((!h_c && p->M > 0) || !h_img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     const size_t cb = sizeof(float2) * (size_t)p->M * p->desc.n_coil, ib = sizeof(float2) * image_elems(p);
-    // pinned buffers: the pad reads the image and the interp writes the samples directly
+    // pinned buffers: the pad reads the image and the interp writes the samples directly --
+    // except the tensor-core interp, which zeroes its output and adds per-tile partials with
+    // atomics: it writes a device buffer that is copied back in bulk
     const void *src = mapped_host(h_img);
-    void *dst = p->M > 0 ? mapped_host(h_c) : nullptr;
+    void *dst = p->M > 0 && !interp_on_tensor_cores(p) ? mapped_host(h_c) : nullptr;
     if (!src) {
         GBN_TRY(ensure(p, p->stage_in, ib));
         GBN_CUDA(cudaMemcpyAsync(p->stage_in.p, h_img, ib, cudaMemcpyHostToDevice, s));

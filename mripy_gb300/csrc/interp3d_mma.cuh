@@ -157,17 +157,27 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
         float wxp[4] = {0.f, 0.f, 0.f, 0.f};
         uint32_t jp = 0;
         bool okp = false;
+        // records are read one batch ahead: the next batch's entry early in the batch, its
+        // sample record half way through, so neither load is waited for where it is used
+        uint32_t jn = 0;
+        bool okn = 32 * q + lane < sub.z;
+        float4 ptn = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (okn) {
+            jn = a.idx[(int64_t)sub.y + (int64_t)(32 * q + lane) * stride];
+            ptn = a.pts_by_sample[jn];
+        }
         for (int b = 0; b <= nb; ++b) {
             float wx[4] = {0.f, 0.f, 0.f, 0.f};
             uint32_t j = 0;
             bool ok = false;
             if (b < nb) {
-                const int i = b * B + 32 * q + lane;
-                ok = i < sub.z;
-                float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (ok) {
-                    j = a.idx[(int64_t)sub.y + (int64_t)i * stride];
-                    pt = a.pts_by_sample[j];
+                j = jn;
+                ok = okn;
+                const float4 pt = ptn;
+                {
+                    const int i = (b + 1) * B + 32 * q + lane;
+                    okn = i < sub.z;
+                    if (okn) jn = a.idx[(int64_t)sub.y + (int64_t)i * stride];
                 }
                 // per dimension the first tap's tile plane r and the distance of plane 0
                 int r[3] = {-(1 << 20), -(1 << 20), -(1 << 20)};
@@ -204,6 +214,7 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
                     // the MMAs of chunk gch - 2 (same buffer) have completed
                     if (gch >= 2 && !mbar_wait_bounded(&done[buf], (uint32_t)(((gch >> 1) - 1) & 1)) && lane == 0)
                         atomicOr(status, kStatusSpreadTimeout);
+                    if (ch == 1 && okn) ptn = a.pts_by_sample[jn];
                     const int y = 2 * ch + h;
                     const float dy = d0y - (float)y;
                     const float wyv = ex2_approx(-g.beta2[1] * dy * dy);

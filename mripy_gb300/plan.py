@@ -179,7 +179,7 @@ class NufftPlan:
             "device_bytes": inf.device_bytes, "interp_coil_group": inf.interp_coil_group,
             "dense_subproblems": inf.dense_subproblems,
             "spread_kernels": inf.spread_kernels, "split_tiles": inf.split_tiles,
-            "spread_variant": inf.spread_variant,
+            "spread_variant": inf.spread_variant, "interp_variant": inf.interp_variant,
         }
 
     def status(self, stream=None):

@@ -353,13 +353,15 @@ def test_tma_interp_matches_thread_staging(shape, nc, eps, tile, icg):
 def test_tma_planes_3d_match_thread_staging(nc, icg, tile):
     """3-D plane-streaming interp: planes staged by tensor copies (windows inside the grid in
     y and z) and by the threads (every window) feed the same arithmetic: equal bit for bit.
-    A 48^3 grid puts most 19-cell windows at an edge, so one launch mixes both paths."""
+    A 48^3 grid puts most 19-cell windows at an edge, so one launch mixes both paths.  (With
+    8 coils the library would choose the tensor-core interp: interp_variant 1 keeps the
+    plane kernel.)"""
     rng = np.random.default_rng(25)
     shape, M = (24, 24, 24), 30000
     xs = rng.uniform(-np.pi, np.pi, (3, M))
     xs[:, :12000] *= 0.2
     plans = [NufftPlan(3, shape, n_coil=nc, eps=1e-6, max_nspread=6,
-                       tuning=Tuning(interp_tile=tile, interp_coil_group=icg, interp_staging=st))
+                       tuning=Tuning(interp_tile=tile, interp_coil_group=icg, interp_staging=st, interp_variant=1))
              .set_points([cuda(v) for v in xs]) for st in (0, 1)]
     g = plans[0].grid()
     g.copy_(torch.randn(g.shape, dtype=torch.complex64, device="cuda"))
