@@ -79,13 +79,14 @@ typedef struct {
     int32_t dense_tile_samples; /* 3-D spread: tiles with at least this many samples (the
                                    k-space centre of radial data) accumulate with Kahan-
                                    compensated FP32 sums; 0 = 32768, negative = never */
-    int32_t spread_variant;     /* 3-D spread with 8 coils per block: 0 = library choice
+    int32_t spread_variant;     /* spread with 8 coils per block: 0 = library choice
                                    (tensor cores on the default 4 x 8 x 16 tile, warp rows
                                    on a caller's tile), 1 = warp rows (tile (4 x warps / TY, TY, 16)),
                                    2 = 4^3-cell cubes fed by producer warps (tile of 8 or 16
                                    cubes; default work items of 2048 samples),
                                    3 = tensor cores (tcgen05 TF32 MMAs, 3-term split; tile
-                                   4 x 8 x 16; dense items on a compensated instance) */
+                                   4 x 8 x 16, dense items on a compensated instance; in 2-D
+                                   tile 8 x 16, selectable, slower than the 2-D default) */
     int32_t interp_variant;     /* 3-D interp with 8 coils per group: 0 = library choice (tensor
                                    cores whenever the spread's tiles are the tensor-core
                                    kernel's 4 x 8 x 16), 1 = the plane-streaming / window
@@ -116,8 +117,8 @@ typedef struct {
     int32_t spread_kernels;    /* kernels the plan's last spread launched (0 before one) */
     int64_t split_tiles;       /* spread tiles shared by several work items (float atomics; 0 means
                                   the spread is bitwise reproducible run to run) */
-    int32_t spread_variant;    /* the 3-D spread kernel this plan runs with 8 coils per block:
-                                  1 warp rows, 2 cubes, 3 tensor cores; 0 for the others */
+    int32_t spread_variant;    /* the spread kernel this plan runs with 8 coils per block: 3 tensor
+                                  cores (2-D or 3-D); in 3-D 1 warp rows, 2 cubes; 0 others */
     int32_t interp_variant;    /* 2 when the interp runs on the tensor cores (3-D, 8 coils per
                                   group; partial sums added with float atomics, so the
                                   samples agree run to run to rounding), else 1 */

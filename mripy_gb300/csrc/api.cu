@@ -781,7 +781,10 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     // Otherwise (4 coils per block, or warp rows) the register rows: (x, y) rows of 4 per
     // warp, tile (TX, TY, 4 x 32/coils), TX*TY = 4 x warps.
     const bool tile_given = desc->spread_tile[0] > 0 || desc->spread_tile[1] > 0 || desc->spread_tile[2] > 0;
-    if (p->dim == 3 && !tile_given && cg_eff == 8 && (p->spread_variant == 3 || p->spread_variant == 0)) {
+    if (p->dim == 2 && !tile_given && cg_eff == 8 && p->spread_variant == 3) {
+        ts[0] = 8;  // the 2-D tensor-core kernel's tile: 128 cells, one TMEM lane each
+        ts[1] = 16;
+    } else if (p->dim == 3 && !tile_given && cg_eff == 8 && (p->spread_variant == 3 || p->spread_variant == 0)) {
         ts[0] = 4;  // the tensor-core kernel's tile: (y, z) = 128 cells, one TMEM lane each
         ts[1] = 8;
         ts[2] = 16;
@@ -795,7 +798,8 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         ts[2] = 4 * (32 / cg_eff);
         reg_spread = true;
     }
-    const bool cube = p->dim == 3 && cg_eff == 8 && (p->spread_variant == 2 || p->spread_variant == 3);
+    // the cube and tensor-core kernels keep a ring of batches full: long work items
+    const bool cube = cg_eff == 8 && ((p->dim == 3 && p->spread_variant == 2) || p->spread_variant == 3);
     p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem
                                           : (cube ? 2048 : (reg_spread && p->dim == 2 ? 128 : 256));
     make_geom(p, ts, p->gs);

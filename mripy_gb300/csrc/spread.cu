@@ -57,10 +57,13 @@ static int cube_path(const Geom &g, int coil_group, int variant) {
     return 0;
 }
 
-// the tensor-core kernel applies: 3-D, 8 coils per block, its 4 x 8 x 16 tile, variant 3
+// the tensor-core kernel applies: 8 coils per block, variant 3, its tile (3-D 4 x 8 x 16,
+// 2-D 8 x 16) on a grid of at least tile + stencil cells per axis
 static bool mma_path(const Geom &g, int coil_group, int variant) {
-    return variant == 3 && grid3d_applies(g) && coil_group == 8 && g.tile[0] == kMmaTX && g.tile[1] == kMmaTY &&
-           g.tile[2] == kMmaTZ;
+    if (variant != 3 || coil_group != 8) return false;
+    if (g.dim == 3)
+        return grid3d_applies(g) && g.tile[0] == kMmaTX && g.tile[1] == kMmaTY && g.tile[2] == kMmaTZ;
+    return use_2d_path(g) && g.tile[0] == kMmaTY && g.tile[1] == kMmaTZ;
 }
 
 // the cube and tensor-core kernels read interleaved work items
@@ -69,8 +72,8 @@ bool spread_cube_applies(const Geom &g, int coil_group, int variant) {
 }
 
 int spread_path_kind(const Geom &g, int coil_group, int variant, int threads) {
-    if (g.dim != 3 || coil_group != 8) return 0;
     if (mma_path(g, coil_group, variant)) return 3;
+    if (g.dim != 3 || coil_group != 8) return 0;
     if (cube_path(g, coil_group, variant)) return 2;
     return reg3d_path(g, coil_group, threads) ? 1 : 0;
 }
@@ -128,6 +131,13 @@ template <int WT>
 static cudaError_t launch_mma(const SpreadArgs &a, int64_t n_sub, cudaStream_t s) {
     const int n_cg = (a.g.n_coil + 7) / 8;
     const int64_t n_units = n_sub * n_cg;
+    if (a.g.dim == 2) {  // no dense tiles in 2-D
+        auto kern = k_spread2d_mma<WT>;
+        cudaError_t e = set_smem(kern, kMmaSmemBytes);
+        if (e != cudaSuccess) return e;
+        kern<<<(unsigned)n_units, kMmaThreads, kMmaSmemBytes, s>>>(a, a.status, n_cg);
+        return cudaGetLastError();
+    }
     cudaError_t e = launch_mma_instance<WT, false>(a, n_units, n_cg, s);
     if (e == cudaSuccess && a.any_dense) e = launch_mma_instance<WT, true>(a, n_units, n_cg, s);
     return e;
@@ -138,6 +148,11 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
     const size_t smem = spread_smem_bytes(a.g, coil_group);
     const dim3 grid((unsigned)n_sub, (unsigned)((a.g.n_coil + coil_group - 1) / coil_group));
     cudaError_t err = cudaSuccess;
+    // tensor-core kernel (8 coils per block; 3-D: then compensated sums for dense units)
+    if (mma_path(a.g, coil_group, a.variant)) {
+        GBN_DISPATCH_W(a.g.W, { err = launch_mma<WT>(a, n_sub, s); });
+        return err;
+    }
     // register-tile kernel: 4 or 8 coils per block and the tile it is built for
     if (use_2d_path(a.g) && (coil_group == 4 || coil_group == 8) && threads <= 256 &&
         a.g.tile[0] == kRegRows * (threads / 32) &&
@@ -162,11 +177,6 @@ cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, in
                 err = cudaGetLastError();
             }
         }));
-        return err;
-    }
-    // 3-D tensor-core kernel (8 coils per block), then compensated cube sums for dense units
-    if (mma_path(a.g, coil_group, a.variant)) {
-        GBN_DISPATCH_W(a.g.W, { err = launch_mma<WT>(a, n_sub, s); });
         return err;
     }
     // 3-D cube kernel (8 coils per block): plain sums, then (if any) compensated ones

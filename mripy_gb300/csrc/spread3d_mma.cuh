@@ -64,7 +64,7 @@ constexpr int kMmaWarp = kMmaBuilders + kMmaLoaders;  // the MMA warp's index
 constexpr int kMmaThreads = 32 * (kMmaWarp + 1);
 constexpr uint32_t kMmaTmemCols = 256;              // A (hi, lo) x 2 buffers: 0..127; D, S: 128..255
 constexpr uint32_t kMmaColD = 128;                  // the MMAs' accumulator
-constexpr uint32_t kMmaColS = 192;                  // the running sum of the drained accumulators
+constexpr uint32_t kMmaColS = 192;                  // the running sum of the drained accumulators (3-D)
 // the compensated instance: two accumulators D (batch k in D[k % 2]), the running sum S and
 // its Kahan compensation C; one block per SM
 constexpr uint32_t kMmaTmemColsK = 512;
@@ -95,6 +95,18 @@ static_assert(kMmaSmemBytesK > 228 * 1024 / 2 && kMmaSmemBytesK >= kMmaSmemBytes
 static_assert(kMmaStV % 16 == 0 && kMmaSlotBytes % 16 == 0, "16-byte aligned staging");
 constexpr int kMmaTaps = kMmaTX + kMmaTY + kMmaTZ;  // 28 tile-plane weights per sample
 
+// The tile of each dimension: M = TY x TZ = 128 cells of grid dimensions (DY, DZ), N = NX
+// planes along grid dimension 0 (3-D only) x 8 coils x re/im.  3-D: 4 x 8 x 16 cells,
+// N = 64.  2-D: 8 x 16 cells, N = 16 (no plane weight: B is the coil values themselves).
+template <int D> struct MmaTile;
+template <> struct MmaTile<3> {
+    static constexpr int NX = 4, DY = 1, DZ = 2, TAPS = kMmaTX + kMmaTY + kMmaTZ;
+};
+template <> struct MmaTile<2> {
+    static constexpr int NX = 1, DY = 0, DZ = 1, TAPS = kMmaTY + kMmaTZ;
+};
+template <int D> constexpr int mma_n() { return MmaTile<D>::NX * 16; }
+
 // 2^x (PTX ex2.approx, flushing subnormal results to zero: the Gaussian's smallest weight
 // inside the stencil is ~eps, far above the subnormal range)
 __device__ __forceinline__ float ex2_approx(float x) {
@@ -121,22 +133,41 @@ __device__ __forceinline__ void tf32_split2(float2 a, float2 b, float2 &hi, floa
     lo = __fadd2_rn(x, make_float2(-hi.x, -hi.y));
 }
 
-// S (+)= D over this thread's lane and the 32 columns of half hk; `first`: S = D
+// S (+)= D over this thread's lane and the N / 2 columns of half hk; `first`: S = D.  D is
+// at column kMmaColD, S right after it (N columns each).
+template <int N>
 __device__ __forceinline__ void mma_drain(uint32_t tl, int hk, bool first) {
+    constexpr uint32_t kColS = kMmaColD + N;
+    if constexpr (N == 64) {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const uint32_t col = 32u * hk + 16u * h;
-        float d[16], s[16];
-        tmem_ld_x16(tl + kMmaColD + col, d);
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t col = 32u * hk + 16u * h;
+            float d[16], s[16];
+            tmem_ld_x16(tl + kMmaColD + col, d);
+            if (!first) {
+                tmem_ld_x16(tl + kColS + col, s);
+                tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) d[i] += s[i];
+            } else {
+                tmem_wait_ld();
+            }
+            tmem_st_x16(tl + kColS + col, d);
+        }
+    } else {
+        static_assert(N == 16, "N is 64 (3-D) or 16 (2-D)");
+        const uint32_t col = 8u * hk;
+        float d[8], s[8];
+        tmem_ld_x8(tl + kMmaColD + col, d);
         if (!first) {
-            tmem_ld_x16(tl + kMmaColS + col, s);
+            tmem_ld_x8(tl + kColS + col, s);
             tmem_wait_ld();
 #pragma unroll
-            for (int i = 0; i < 16; ++i) d[i] += s[i];
+            for (int i = 0; i < 8; ++i) d[i] += s[i];
         } else {
             tmem_wait_ld();
         }
-        tmem_st_x16(tl + kMmaColS + col, d);
+        tmem_st_x8(tl + kColS + col, d);
     }
 }
 
@@ -170,14 +201,19 @@ __device__ __forceinline__ void mma_drain_kahan(uint32_t tl, int hk, uint32_t co
     }
 }
 
-template <int WT, bool KAHAN>
-__global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(SpreadArgs a, uint32_t *status, int n_cg) {
+// The kernel body for dimension D (3: 4 x 8 x 16 tiles, N = 64; 2: 8 x 16 tiles, N = 16).
+template <int D, int WT, bool KAHAN>
+__device__ __forceinline__ void spread_mma_body(const SpreadArgs &a, uint32_t *status, int n_cg) {
+    using T = MmaTile<D>;
+    constexpr int N = mma_n<D>();
+    constexpr uint32_t kBOp = N * 128;  // one B operand: N rows x 128 B
     constexpr uint32_t kCols = KAHAN ? kMmaTmemColsK : kMmaTmemCols;
     constexpr int B = kMmaBatch;
     constexpr int CG = 8;
+    static_assert(!KAHAN || D == 3, "dense tiles are a 3-D notion");
     extern __shared__ unsigned char smem_mma_raw[];
     unsigned char *sm = smem_mma_raw + ((1024u - (smem_addr(smem_mma_raw) & 1023u)) & 1023u);
-    unsigned char *opB = sm;  // [buf][hi, lo][64 rows x 128 B], SW128
+    unsigned char *opB = sm;  // [buf][hi, lo][N rows x 128 B], SW128
     unsigned char *stage = sm + kMmaStageOff;
     uint64_t *full = reinterpret_cast<uint64_t *>(sm + kMmaBarOff);
     uint64_t *empty = full + kMmaSlots;
@@ -218,7 +254,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
         if (warp >= kMmaBuilders && warp < kMmaWarp) {
             // ------------------------------------------------------------ loader warp
             int o[3], e[3];
-            tile_coords<3>(g, sub.x % g.ntiles, o, e);
+            tile_coords<D>(g, sub.x % g.ntiles, o, e);
             const int lw = warp - kMmaBuilders;
             const int ns = g.ns;
             const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
@@ -246,9 +282,9 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
                 int r[3] = {0, 0, 0};
                 if (ok) {
                     int c0[3];
-                    unpack_cells(3, __float_as_uint(pt.w), c0[0], c0[1], c0[2]);
+                    unpack_cells(D, __float_as_uint(pt.w), c0[0], c0[1], c0[2]);
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) {
+                    for (int d = 0; d < D; ++d) {
                         int rr = c0[d] - o[d];
                         rr += rr < 0 ? g.nf[d] : 0;
                         rr -= rr > g.nf[d] - W ? g.nf[d] : 0;
@@ -260,17 +296,19 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
                     !mbar_wait_bounded(&empty[slot], (uint32_t)((k / kMmaSlots - 1) & 1)) && lane == 0)
                     atomicOr(status, kStatusSpreadTimeout);
                 unsigned char *sl = stage + (size_t)slot * kMmaSlotBytes;
-                // per dimension: the distance of tile plane 0 from the sample (plane t: d0 - t)
-                // and the plane of the first tap; a lane without a sample gets a first tap
-                // no plane reaches, so all its weights are 0
+                // per grid dimension: the distance of tile plane 0 from the sample (plane t:
+                // d0 - t) and the plane of the first tap; a lane without a sample gets a first
+                // tap no plane reaches, so all its weights are 0
                 float *d0 = reinterpret_cast<float *>(sl + kMmaStD0);
                 int *rs = reinterpret_cast<int *>(sl + kMmaStR);
                 d0[lane] = pt.x + (float)(ns - 1 + r[0]);
                 d0[B + lane] = pt.y + (float)(ns - 1 + r[1]);
-                d0[2 * B + lane] = pt.z + (float)(ns - 1 + r[2]);
                 rs[lane] = ok ? r[0] : -(1 << 20);
                 rs[B + lane] = ok ? r[1] : -(1 << 20);
-                rs[2 * B + lane] = ok ? r[2] : -(1 << 20);
+                if constexpr (D == 3) {
+                    d0[2 * B + lane] = pt.z + (float)(ns - 1 + r[2]);
+                    rs[2 * B + lane] = ok ? r[2] : -(1 << 20);
+                }
                 float2 *vs = reinterpret_cast<float2 *>(sl + kMmaStV);
 #pragma unroll
                 for (int cc = 0; cc < CG; ++cc) vs[cc * B + lane] = v[cc];
@@ -279,7 +317,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
         } else if (warp == kMmaWarp) {
             // ------------------------------------------------------------ MMA warp
             if (lane == 0) {
-                constexpr uint32_t idesc = tc_idesc_tf32(kMmaM, kMmaN);
+                constexpr uint32_t idesc = tc_idesc_tf32(kMmaM, N);
                 const uint32_t b0 = smem_addr(opB);
                 for (int k = 0; k < nb; ++k) {
                     const int buf = k & 1;
@@ -287,7 +325,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
                     tc_fence_after();
                     const uint32_t ah = tbase + 64u * buf, al = ah + 32u;
                     const uint32_t d = tbase + kMmaColD + (KAHAN ? 64u * buf : 0u);
-                    const uint32_t bh = b0 + 2u * buf * kMmaBOp, bl = bh + kMmaBOp;
+                    const uint32_t bh = b0 + 2u * buf * kBOp, bl = bh + kBOp;
 #pragma unroll
                     for (int jk = 0; jk < B / 8; ++jk) {
                         // plain: a group's first MMA starts D afresh; compensated: every batch's
@@ -303,31 +341,32 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
         } else {
             // ------------------------------------------------------------ builder warp
             const int q = warp & 3, hk = warp >> 2;  // TMEM quarter; half of the batch's samples
-            const int m = 32 * q + lane, y = m >> 4, z = m & 15;
-            const int bx = warp >> 1, bc0 = 4 * (warp & 1);  // B rows: x = bx, coils bc0 .. bc0 + 3
+            const int m = 32 * q + lane, y = m >> 4, z = m & 15;  // tile cell (y, z) of TMEM lane m
             const uint32_t tl = tmem_lane_base(tbase, q);
             for (int k = 0; k < nb; ++k) {
                 const int slot = k % kMmaSlots, buf = k & 1;
                 if (!mbar_wait_bounded(&full[slot], (uint32_t)((k / kMmaSlots) & 1)) && lane == 0)
                     atomicOr(status, kStatusSpreadTimeout);
                 {
-                    // the batch's 28 plane weights per sample, shared by the builder warps:
-                    // warp b computes planes b, b + 8, b + 16, b + 24 of sample `lane`
+                    // the batch's tile-plane weights per sample (28 in 3-D, 24 in 2-D), shared
+                    // by the builder warps: warp b computes planes b, b + 8, ... of sample `lane`
                     unsigned char *slw = stage + (size_t)slot * kMmaSlotBytes;
                     const float *d0 = reinterpret_cast<const float *>(slw + kMmaStD0);
                     const int *rs = reinterpret_cast<const int *>(slw + kMmaStR);
+                    constexpr int XT = D == 3 ? kMmaTX : 0;  // planes along N's grid dimension
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
                         const int jt = warp + 8 * i;
-                        if (jt >= kMmaTaps) break;
-                        const int dim = jt < kMmaTX ? 0 : (jt < kMmaTX + kMmaTY ? 1 : 2);
-                        const int t = jt - (dim == 0 ? 0 : (dim == 1 ? kMmaTX : kMmaTX + kMmaTY));
-                        const float d = d0[dim * B + lane] - (float)t;
+                        if (jt >= T::TAPS) break;
+                        const int reg = jt < XT ? 0 : (jt < XT + kMmaTY ? 1 : 2);  // x, y or z planes
+                        const int t = jt - (reg == 0 ? 0 : (reg == 1 ? XT : XT + kMmaTY));
+                        const int gd = D == 3 ? reg : reg - 1;  // grid dimension (2-D: y, z planes only)
+                        const float d = d0[gd * B + lane] - (float)t;
                         // (a parameter array indexed at run time would be copied to local memory)
-                        const float beta = dim == 0 ? g.beta2[0] : (dim == 1 ? g.beta2[1] : g.beta2[2]);
+                        const float beta = gd == 0 ? g.beta2[0] : (gd == 1 ? g.beta2[1] : g.beta2[2]);
                         const float wv = ex2_approx(-beta * d * d);
-                        const bool in = (unsigned)(t - rs[dim * B + lane]) < (unsigned)W;
-                        reinterpret_cast<float *>(slw + (dim == 0 ? kMmaStWx : (dim == 1 ? kMmaStWy : kMmaStWz)))
+                        const bool in = (unsigned)(t - rs[gd * B + lane]) < (unsigned)W;
+                        reinterpret_cast<float *>(slw + (reg == 0 ? kMmaStWx : (reg == 1 ? kMmaStWy : kMmaStWz)))
                             [t * kMmaWS + lane] = in ? wv : 0.f;
                     }
                     asm volatile("bar.sync 1, %0;" ::"n"(kMmaBuilders * 32) : "memory");
@@ -335,10 +374,12 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
                 // the MMAs of batch k - 2 (same operand buffer) have completed
                 if (k >= 2 && !mbar_wait_bounded(&done[buf], (uint32_t)(((k >> 1) - 1) & 1)) && lane == 0)
                     atomicOr(status, kStatusSpreadTimeout);
-                if (KAHAN && k >= 2) {
-                    // batch k - 2's accumulator D[k % 2] into S, C before batch k overwrites it
-                    tc_fence_after();
-                    mma_drain_kahan(tl, hk, kMmaColD + 64u * buf, k == 2);
+                if constexpr (KAHAN) {
+                    if (k >= 2) {
+                        // batch k - 2's accumulator D[k % 2] into S, C before batch k overwrites it
+                        tc_fence_after();
+                        mma_drain_kahan(tl, hk, kMmaColD + 64u * buf, k == 2);
+                    }
                 }
                 const unsigned char *sl = stage + (size_t)slot * kMmaSlotBytes;
                 // A: cells (y, z) of this lane, samples 16 hk .. 16 hk + 15
@@ -365,20 +406,32 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
                     tmem_st_x8(tl + 64u * buf + 16u * hk + 8u * h, hi);
                     tmem_st_x8(tl + 64u * buf + 32u + 16u * hk + 8u * h, lo);
                 }
-                // B: rows (bx, coil, re/im) for sample `lane`
-                const float wxk = reinterpret_cast<const float *>(sl + kMmaStWx)[bx * kMmaWS + lane];
                 const float2 *vs = reinterpret_cast<const float2 *>(sl + kMmaStV);
-                unsigned char *bh = opB + (size_t)(2 * buf) * kMmaBOp, *bl = bh + kMmaBOp;
+                unsigned char *bh = opB + (size_t)(2 * buf) * kBOp, *bl = bh + kBOp;
+                if constexpr (D == 3) {
+                    // B: rows (x = bx, coils bc0 .. bc0 + 3, re/im) for sample `lane`
+                    const int bx = warp >> 1, bc0 = 4 * (warp & 1);
+                    const float wxk = reinterpret_cast<const float *>(sl + kMmaStWx)[bx * kMmaWS + lane];
 #pragma unroll
-                for (int cc = 0; cc < 4; ++cc) {
-                    const float2 vv = vs[(bc0 + cc) * B + lane];
-                    const int nre = bx * 16 + (bc0 + cc) * 2;
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const float2 vv = vs[(bc0 + cc) * B + lane];
+                        const int nre = bx * 16 + (bc0 + cc) * 2;
+                        float2 h, l;
+                        tf32_split2(make_float2(wxk, wxk), vv, h, l);
+                        *reinterpret_cast<float *>(bh + sw128_offset(nre, lane)) = h.x;
+                        *reinterpret_cast<float *>(bl + sw128_offset(nre, lane)) = l.x;
+                        *reinterpret_cast<float *>(bh + sw128_offset(nre + 1, lane)) = h.y;
+                        *reinterpret_cast<float *>(bl + sw128_offset(nre + 1, lane)) = l.y;
+                    }
+                } else {
+                    // B: rows (coil = warp, re/im) for sample `lane`: the coil value itself
+                    const float2 vv = vs[warp * B + lane];
                     float2 h, l;
-                    tf32_split2(make_float2(wxk, wxk), vv, h, l);
-                    *reinterpret_cast<float *>(bh + sw128_offset(nre, lane)) = h.x;
-                    *reinterpret_cast<float *>(bl + sw128_offset(nre, lane)) = l.x;
-                    *reinterpret_cast<float *>(bh + sw128_offset(nre + 1, lane)) = h.y;
-                    *reinterpret_cast<float *>(bl + sw128_offset(nre + 1, lane)) = l.y;
+                    tf32_split2(make_float2(1.f, 1.f), vv, h, l);
+                    *reinterpret_cast<float *>(bh + sw128_offset(2 * warp, lane)) = h.x;
+                    *reinterpret_cast<float *>(bl + sw128_offset(2 * warp, lane)) = l.x;
+                    *reinterpret_cast<float *>(bh + sw128_offset(2 * warp + 1, lane)) = h.y;
+                    *reinterpret_cast<float *>(bl + sw128_offset(2 * warp + 1, lane)) = l.y;
                 }
                 mbar_arrive(&empty[slot]);
                 if (!KAHAN && k % kMmaGroup == 0 && k > 0) {
@@ -388,7 +441,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
                     if (!mbar_wait_bounded(&done[(k - 1) & 1], (uint32_t)(((k - 1) >> 1) & 1)) && lane == 0)
                         atomicOr(status, kStatusSpreadTimeout);
                     tc_fence_after();
-                    mma_drain(tl, hk, k == kMmaGroup);
+                    mma_drain<N>(tl, hk, k == kMmaGroup);
                 }
                 // operands visible to the tensor core before the MMA warp proceeds
                 tmem_wait_st();
@@ -398,7 +451,6 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
             }
 
             // ---------------------------------------------------------------- epilogue
-            // this warp: lanes of quarter q, columns 32 hk .. 32 hk + 31 (x = 2 hk, 2 hk + 1)
             if (nb > 0) {
                 const int kl = nb - 1;
                 if (!mbar_wait_bounded(&done[kl & 1], (uint32_t)((kl >> 1) & 1)) && lane == 0)
@@ -415,49 +467,85 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
             // the unit's tile, read again here rather than kept in registers through the loop
             const int4 su = a.subs[unit / n_cg];
             int o[3], e[3];
-            tile_coords<3>(g, su.x % g.ntiles, o, e);
+            tile_coords<D>(g, su.x % g.ntiles, o, e);
             const int grp = su.x / g.ntiles;
             const bool split = (su.w & kSplitFlag) != 0;
-            const bool inside = y < e[1] && z < e[2];
-            const int64_t cell_yz = (int64_t)(o[1] + y) * g.nf[2] + (o[2] + z);
+            const bool inside = y < e[T::DY] && z < e[T::DZ];
+            if constexpr (D == 3) {
+                // this warp: lanes of quarter q, columns 32 hk .. 32 hk + 31 (x = 2 hk, 2 hk + 1)
+                const int64_t cell_yz = (int64_t)(o[1] + y) * g.nf[2] + (o[2] + z);
 #pragma unroll
-            for (int xi = 0; xi < 2; ++xi) {
-                // columns 32 hk + 16 xi ..: cell x = 2 hk + xi, (coil, re/im) pairs
-                float dv[16];
-                if (nb > 0 && KAHAN) {
-                    float cv[16];
-                    tmem_ld_x16(tl + kMmaColSK + 32u * hk + 16u * xi, dv);
-                    tmem_ld_x16(tl + kMmaColCK + 32u * hk + 16u * xi, cv);
-                    tmem_wait_ld();
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) dv[i] -= cv[i];
-                } else if (nb > 0) {
-                    tmem_ld_x16(tl + kMmaColD + 32u * hk + 16u * xi, dv);
-                    if (nb > kMmaGroup) {  // plus the drained groups
-                        float sv[16];
-                        tmem_ld_x16(tl + kMmaColS + 32u * hk + 16u * xi, sv);
+                for (int xi = 0; xi < 2; ++xi) {
+                    // columns 32 hk + 16 xi ..: cell x = 2 hk + xi, (coil, re/im) pairs
+                    float dv[16];
+                    if (nb > 0 && KAHAN) {
+                        float cv[16];
+                        tmem_ld_x16(tl + kMmaColSK + 32u * hk + 16u * xi, dv);
+                        tmem_ld_x16(tl + kMmaColCK + 32u * hk + 16u * xi, cv);
                         tmem_wait_ld();
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) dv[i] += sv[i];
+                        for (int i = 0; i < 16; ++i) dv[i] -= cv[i];
+                    } else if (nb > 0) {
+                        tmem_ld_x16(tl + kMmaColD + 32u * hk + 16u * xi, dv);
+                        if (nb > kMmaGroup) {  // plus the drained groups
+                            float sv[16];
+                            tmem_ld_x16(tl + kMmaColD + N + 32u * hk + 16u * xi, sv);
+                            tmem_wait_ld();
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) dv[i] += sv[i];
+                        } else {
+                            tmem_wait_ld();
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) dv[i] = 0.f;
+                    }
+                    const int x = 2 * hk + xi;
+                    if (!inside || x >= e[0]) continue;
+                    const int64_t cell = (int64_t)(o[0] + x) * g.nf[1] * g.nf[2] + cell_yz;
+#pragma unroll
+                    for (int c = 0; c < CG; ++c) {
+                        if (cg0 + c >= g.n_coil) break;
+                        float2 *dst = a.grid + ((int64_t)grp * g.n_coil + cg0 + c) * g.G + cell;
+                        if (split) {
+                            atomicAdd(&dst->x, dv[2 * c]);
+                            atomicAdd(&dst->y, dv[2 * c + 1]);
+                        } else {
+                            *dst = make_float2(dv[2 * c], dv[2 * c + 1]);
+                        }
+                    }
+                }
+            } else {
+                // this warp: lanes of quarter q, columns 8 hk .. 8 hk + 7 (coils 4 hk .. 4 hk + 3)
+                float dv[8];
+                if (nb > 0) {
+                    tmem_ld_x8(tl + kMmaColD + 8u * hk, dv);
+                    if (nb > kMmaGroup) {  // plus the drained groups
+                        float sv[8];
+                        tmem_ld_x8(tl + kMmaColD + N + 8u * hk, sv);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) dv[i] += sv[i];
                     } else {
                         tmem_wait_ld();
                     }
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) dv[i] = 0.f;
+                    for (int i = 0; i < 8; ++i) dv[i] = 0.f;
                 }
-                const int x = 2 * hk + xi;
-                if (!inside || x >= e[0]) continue;
-                const int64_t cell = (int64_t)(o[0] + x) * g.nf[1] * g.nf[2] + cell_yz;
+                if (inside) {
+                    const int64_t cell = (int64_t)(o[0] + y) * g.nf[1] + (o[1] + z);
 #pragma unroll
-                for (int c = 0; c < CG; ++c) {
-                    if (cg0 + c >= g.n_coil) break;
-                    float2 *dst = a.grid + ((int64_t)grp * g.n_coil + cg0 + c) * g.G + cell;
-                    if (split) {
-                        atomicAdd(&dst->x, dv[2 * c]);
-                        atomicAdd(&dst->y, dv[2 * c + 1]);
-                    } else {
-                        *dst = make_float2(dv[2 * c], dv[2 * c + 1]);
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const int c = 4 * hk + cc;
+                        if (cg0 + c >= g.n_coil) break;
+                        float2 *dst = a.grid + ((int64_t)grp * g.n_coil + cg0 + c) * g.G + cell;
+                        if (split) {
+                            atomicAdd(&dst->x, dv[2 * cc]);
+                            atomicAdd(&dst->y, dv[2 * cc + 1]);
+                        } else {
+                            *dst = make_float2(dv[2 * cc], dv[2 * cc + 1]);
+                        }
                     }
                 }
             }
@@ -467,6 +555,16 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(Spr
     __syncthreads();
     tc_fence_after();
     if (warp == kMmaWarp) tmem_dealloc(tbase, kCols);
+}
+
+template <int WT, bool KAHAN>
+__global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(SpreadArgs a, uint32_t *status, int n_cg) {
+    spread_mma_body<3, WT, KAHAN>(a, status, n_cg);
+}
+
+template <int WT>
+__global__ void __launch_bounds__(kMmaThreads, 2) k_spread2d_mma(SpreadArgs a, uint32_t *status, int n_cg) {
+    spread_mma_body<2, WT, false>(a, status, n_cg);
 }
 
 }  // namespace gbn
