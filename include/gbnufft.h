@@ -85,7 +85,8 @@ typedef struct {
                                    2 = 4^3-cell cubes fed by producer warps (tile of 8 or 16
                                    cubes; default work items of 2048 samples),
                                    3 = tensor cores (tcgen05 TF32 MMAs, 3-term split; tile
-                                   4 x 8 x 16, dense items on a compensated instance; in 2-D
+                                   4 x 8 x 16, default work items of 4096 samples, dense
+                                   items on a compensated instance; in 2-D
                                    tile 8 x 16, selectable, slower than the 2-D default) */
     int32_t interp_variant;     /* 3-D interp with 8 coils per group: 0 = library choice (tensor
                                    cores whenever the spread's tiles are the tensor-core

@@ -798,10 +798,13 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         ts[2] = 4 * (32 / cg_eff);
         reg_spread = true;
     }
-    // the cube and tensor-core kernels keep a ring of batches full: long work items
+    // the cube and tensor-core kernels keep a ring of batches full: long work items (the 3-D
+    // tensor-core spread and interp share the work items; measured on the 3-D radial
+    // workload: interp 3.75 ms at 4096 samples against 3.93 at 2048, spread even)
     const bool cube = cg_eff == 8 && ((p->dim == 3 && p->spread_variant == 2) || p->spread_variant == 3);
+    const bool mma3 = cube && p->dim == 3 && p->spread_variant == 3;
     p->max_sub = desc->max_subproblem > 0 ? desc->max_subproblem
-                                          : (cube ? 2048 : (reg_spread && p->dim == 2 ? 128 : 256));
+                                          : (mma3 ? 4096 : (cube ? 2048 : (reg_spread && p->dim == 2 ? 128 : 256)));
     make_geom(p, ts, p->gs);
     make_geom(p, ti, p->gi);
 
