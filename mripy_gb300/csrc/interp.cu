@@ -139,12 +139,15 @@ cudaError_t launch_interp3d_mma(const MmaInterpArgs &a, int64_t n_sub, uint32_t 
     }
     if (n_sub == 0) return cudaGetLastError();
     const int n_cg = (a.g.n_coil + 7) / 8;
+    // float4 atomics (two coils each) when the coils of a sample are adjacent and every
+    // coil group starts on a 16-byte boundary (8-coil groups: an even element stride)
+    const int vec = a.c_coil == 1 && a.c_elem % 2 == 0 && (uintptr_t)a.c % 16 == 0;
     cudaError_t err = cudaSuccess;
     GBN_DISPATCH_W(a.g.W, {
         auto kern = k_interp3d_mma<WT>;
         err = set_smem(kern, kImSmemBytes);
         if (err == cudaSuccess) {
-            kern<<<(unsigned)(n_sub * n_cg), kImThreads, kImSmemBytes, s>>>(a, status, n_cg);
+            kern<<<(unsigned)(n_sub * n_cg), kImThreads, kImSmemBytes, s>>>(a, status, n_cg, vec);
             err = cudaGetLastError();
         }
     });

@@ -55,7 +55,8 @@ __device__ __forceinline__ uint32_t im_b_offset(int n, int k) {
 }
 
 template <int WT>
-__global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a, uint32_t *status, int n_cg) {
+__global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a, uint32_t *status, int n_cg,
+                                                                 int vec_atomic) {
     constexpr int B = kImBatch;
     constexpr int CG = 8;
     extern __shared__ unsigned char smem_im_raw[];
@@ -94,21 +95,36 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
     // B: the tile's cells (x, y, z) of the 8 coils; cells past the grid edge and padded
     // coils are 0.  z fastest across threads: 128-byte runs of each (coil, x, y) row.
     // (Nothing to do for an empty work item.)
+    // Loads are issued 8 at a time before any is used, so a thread waits for one memory
+    // latency per 8 cells rather than per cell.
     if (nb > 0) {
+        constexpr int kCells = CG * kMmaTX * kMmaTY * kMmaTZ;
         const float2 *base = a.grid + (int64_t)grp * g.n_coil * g.G;
-        for (int i = threadIdx.x; i < CG * kMmaTX * kMmaTY * kMmaTZ; i += kImThreads) {
-            const int z = i & 15, y = (i >> 4) & 7, x = (i >> 7) & 3, c = i >> 9;
-            float2 v = make_float2(0.f, 0.f);
-            if (cg0 + c < g.n_coil && x < e[0] && y < e[1] && z < e[2])
-                v = base[(int64_t)(cg0 + c) * g.G + ((int64_t)(o[0] + x) * g.nf[1] + (o[1] + y)) * g.nf[2] + (o[2] + z)];
-            float2 h, l;
-            tf32_split2(v, make_float2(1.f, 1.f), h, l);
-            const int n = x * 16 + c * 2, k = y * 16 + z;
-            const uint32_t ore = im_b_offset(n, k), oim = im_b_offset(n + 1, k);
-            *reinterpret_cast<float *>(bh + ore) = h.x;
-            *reinterpret_cast<float *>(bl + ore) = l.x;
-            *reinterpret_cast<float *>(bh + oim) = h.y;
-            *reinterpret_cast<float *>(bl + oim) = l.y;
+        for (int r0 = threadIdx.x; r0 < kCells; r0 += 8 * kImThreads) {
+            float2 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = r0 + u * kImThreads;
+                const int z = i & 15, y = (i >> 4) & 7, x = (i >> 7) & 3, c = i >> 9;
+                v[u] = make_float2(0.f, 0.f);
+                if (i < kCells && cg0 + c < g.n_coil && x < e[0] && y < e[1] && z < e[2])
+                    v[u] = base[(int64_t)(cg0 + c) * g.G + ((int64_t)(o[0] + x) * g.nf[1] + (o[1] + y)) * g.nf[2] +
+                                (o[2] + z)];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = r0 + u * kImThreads;
+                if (i >= kCells) break;
+                const int z = i & 15, y = (i >> 4) & 7, x = (i >> 7) & 3, c = i >> 9;
+                float2 h, l;
+                tf32_split2(v[u], make_float2(1.f, 1.f), h, l);
+                const int n = x * 16 + c * 2, k = y * 16 + z;
+                const uint32_t ore = im_b_offset(n, k), oim = im_b_offset(n + 1, k);
+                *reinterpret_cast<float *>(bh + ore) = h.x;
+                *reinterpret_cast<float *>(bl + ore) = l.x;
+                *reinterpret_cast<float *>(bh + oim) = h.y;
+                *reinterpret_cast<float *>(bl + oim) = l.y;
+            }
         }
     }
     fence_proxy_async_smem();
@@ -255,17 +271,30 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
                 mbar_arrive(&tempty[tb]);
                 if (okp) {
                     const float sc = a.weight ? a.weight[jp] : 1.f;
+                    float pr[8];
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc) {
-                        const int coil = cg0 + 4 * h + cc;
-                        if (coil >= g.n_coil) break;
                         float re = 0.f, im = 0.f;
 #pragma unroll
                         for (int x = 0; x < 4; ++x) {
                             re = fmaf(wxp[x], tv[x][2 * cc], re);
                             im = fmaf(wxp[x], tv[x][2 * cc + 1], im);
                         }
-                        atomicAdd(a.c + (int64_t)jp * a.c_elem + (int64_t)coil * a.c_coil, make_float2(re * sc, im * sc));
+                        pr[2 * cc] = re * sc;
+                        pr[2 * cc + 1] = im * sc;
+                    }
+                    const int coil0 = cg0 + 4 * h;
+                    float2 *dst = a.c + (int64_t)jp * a.c_elem + (int64_t)coil0 * a.c_coil;
+                    if (vec_atomic && coil0 + 4 <= g.n_coil) {
+                        // coils adjacent and 16-byte aligned: two coils per atomic
+                        atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(pr[0], pr[1], pr[2], pr[3]));
+                        atomicAdd(reinterpret_cast<float4 *>(dst + 2), make_float4(pr[4], pr[5], pr[6], pr[7]));
+                    } else {
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc) {
+                            if (coil0 + cc >= g.n_coil) break;
+                            atomicAdd(dst + (int64_t)cc * a.c_coil, make_float2(pr[2 * cc], pr[2 * cc + 1]));
+                        }
                     }
                 }
             }
