@@ -462,7 +462,7 @@ def run_gpu(args, wl):
         mma_flop = info["spread_entries"] * 3 * 2 * 128 * 64
         tf32_peak = tf32_peak_tflops()
         result["roofline"]["spread_tensor"] = {
-            "kernel": "k_spread3d_mma", "mma_tflop_per_launch": round(mma_flop / 1e12, 3),
+            "kernel": "k_spread_mma<3, ...>", "mma_tflop_per_launch": round(mma_flop / 1e12, 3),
             "achieved_tflops": round(mma_flop / (t_spread * 1e-3) / 1e12, 1), "peak_tflops": round(tf32_peak, 1),
             "frac": round(mma_flop / (t_spread * 1e-3) / 1e12 / tf32_peak, 4),
             "peak_source": "of measured (MEASURED_PEAKS.json bf16_tflops / 2: TF32 at half the BF16 rate)",

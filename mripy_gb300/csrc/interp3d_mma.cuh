@@ -2,7 +2,7 @@
 //
 // The forward gridding of sample s is out[s, c] = sum_{x,y,z} wx_s[x] wy_s[y] wz_s[z] G[x,y,z,c].
 // Restricted to one tile of the spread's 4 x 8 x 16 tiling, with the separable weights
-// split the same way as in k_spread3d_mma, its (y, z) part is a GEMM with the samples as M:
+// split the same way as in k_spread_mma, its (y, z) part is a GEMM with the samples as M:
 //     T[s, (x, c, re/im)] = sum_{(y,z)} A[s, (y, z)] * B[(x, c, re/im), (y, z)]
 //     A[s, (y, z)] = wy_s[y] wz_s[z]          (M = 128 samples, K = 8 x 16 = 128 cells)
 //     B = the tile's grid values               (N = 4 x 8 x 2 = 64)

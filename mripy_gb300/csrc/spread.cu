@@ -4,7 +4,7 @@
 // they are built for: k_spread2d_reg / k_spread3d_reg (accumulators in registers).
 // Other 2-D / 3-D tiles: k_spread2d / k_spread3d (warp-owned shared-memory rows, no atomics).
 // Otherwise (1-D, wide stencils, small grids): k_spread (shared-memory atomics).
-// 3-D with 8 coils per block also: k_spread3d_mma (tensor cores, 4 x 8 x 16 tiles) and
+// 3-D with 8 coils per block also: k_spread_mma<3, ...> (tensor cores, 4 x 8 x 16 tiles) and
 // k_spread3d_cube (register cubes), each followed by the compensated cube instance for the
 // dense work items.
 #include "dispatch.cuh"
@@ -119,7 +119,7 @@ static cudaError_t launch_cube(const SpreadArgs &a, int64_t n_sub, cudaStream_t 
 // dense units
 template <int WT, bool KAHAN>
 static cudaError_t launch_mma_instance(const SpreadArgs &a, int64_t n_units, int n_cg, cudaStream_t s) {
-    auto kern = k_spread3d_mma<WT, KAHAN>;
+    auto kern = k_spread_mma<3, WT, KAHAN>;
     const size_t smem = KAHAN ? kMmaSmemBytesK : kMmaSmemBytes;
     cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
@@ -132,7 +132,7 @@ static cudaError_t launch_mma(const SpreadArgs &a, int64_t n_sub, cudaStream_t s
     const int n_cg = (a.g.n_coil + 7) / 8;
     const int64_t n_units = n_sub * n_cg;
     if (a.g.dim == 2) {  // no dense tiles in 2-D
-        auto kern = k_spread2d_mma<WT>;
+        auto kern = k_spread_mma<2, WT, false>;
         cudaError_t e = set_smem(kern, kMmaSmemBytes);
         if (e != cudaSuccess) return e;
         kern<<<(unsigned)n_units, kMmaThreads, kMmaSmemBytes, s>>>(a, a.status, n_cg);

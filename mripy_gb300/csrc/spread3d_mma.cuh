@@ -201,9 +201,11 @@ __device__ __forceinline__ void mma_drain_kahan(uint32_t tl, int hk, uint32_t co
     }
 }
 
-// The kernel body for dimension D (3: 4 x 8 x 16 tiles, N = 64; 2: 8 x 16 tiles, N = 16).
+// Dimension D (3: 4 x 8 x 16 tiles, N = 64; 2: 8 x 16 tiles, N = 16).  One kernel template
+// rather than a device function behind per-dimension kernels: the arguments stay in the
+// parameter space (an inlined copy of them cost registers and 4.5 % of the 3-D time).
 template <int D, int WT, bool KAHAN>
-__device__ __forceinline__ void spread_mma_body(const SpreadArgs &a, uint32_t *status, int n_cg) {
+__global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(SpreadArgs a, uint32_t *status, int n_cg) {
     using T = MmaTile<D>;
     constexpr int N = mma_n<D>();
     constexpr uint32_t kBOp = N * 128;  // one B operand: N rows x 128 B
@@ -342,6 +344,7 @@ __device__ __forceinline__ void spread_mma_body(const SpreadArgs &a, uint32_t *s
             // ------------------------------------------------------------ builder warp
             const int q = warp & 3, hk = warp >> 2;  // TMEM quarter; half of the batch's samples
             const int m = 32 * q + lane, y = m >> 4, z = m & 15;  // tile cell (y, z) of TMEM lane m
+            const int bx = warp >> 1, bc0 = 4 * (warp & 1);  // 3-D B rows: x = bx, coils bc0 .. bc0 + 3
             const uint32_t tl = tmem_lane_base(tbase, q);
             for (int k = 0; k < nb; ++k) {
                 const int slot = k % kMmaSlots, buf = k & 1;
@@ -410,7 +413,6 @@ __device__ __forceinline__ void spread_mma_body(const SpreadArgs &a, uint32_t *s
                 unsigned char *bh = opB + (size_t)(2 * buf) * kBOp, *bl = bh + kBOp;
                 if constexpr (D == 3) {
                     // B: rows (x = bx, coils bc0 .. bc0 + 3, re/im) for sample `lane`
-                    const int bx = warp >> 1, bc0 = 4 * (warp & 1);
                     const float wxk = reinterpret_cast<const float *>(sl + kMmaStWx)[bx * kMmaWS + lane];
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc) {
@@ -557,14 +559,5 @@ __device__ __forceinline__ void spread_mma_body(const SpreadArgs &a, uint32_t *s
     if (warp == kMmaWarp) tmem_dealloc(tbase, kCols);
 }
 
-template <int WT, bool KAHAN>
-__global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread3d_mma(SpreadArgs a, uint32_t *status, int n_cg) {
-    spread_mma_body<3, WT, KAHAN>(a, status, n_cg);
-}
-
-template <int WT>
-__global__ void __launch_bounds__(kMmaThreads, 2) k_spread2d_mma(SpreadArgs a, uint32_t *status, int n_cg) {
-    spread_mma_body<2, WT, false>(a, status, n_cg);
-}
 
 }  // namespace gbn

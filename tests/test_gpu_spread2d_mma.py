@@ -1,4 +1,4 @@
-"""The 2-D tensor-core spread (k_spread2d_mma: per 8 x 16 tile a TF32 GEMM over the tile's
+"""The 2-D tensor-core spread (k_spread_mma<2, ...>: per 8 x 16 tile a TF32 GEMM over the tile's
 samples, A = wx (x) wy in TMEM, B = the coil values in swizzled shared memory, N = 8 coils x
 re/im; `spread_variant` 3) against the FP64 oracle and the FP32 register kernel.
 

@@ -1,4 +1,4 @@
-"""The 3-D tensor-core spread (k_spread3d_mma: per 4 x 8 x 16 tile a TF32 GEMM over the
+"""The 3-D tensor-core spread (k_spread_mma<3, ...>: per 4 x 8 x 16 tile a TF32 GEMM over the
 tile's samples, operands split into hi + lo parts, A built in TMEM, B in swizzled shared
 memory, the accumulator in TMEM) against the FP64 oracle.
 
