@@ -123,7 +123,7 @@ static cudaError_t launch_mma_instance(const SpreadArgs &a, int64_t n_units, int
     const size_t smem = KAHAN ? kMmaSmemBytesK : kMmaSmemBytes;
     cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
-    kern<<<(unsigned)n_units, kMmaThreads, smem, s>>>(a, a.status, n_cg);
+    kern<<<(unsigned)n_units, mma_threads<KAHAN>(), smem, s>>>(a, a.status, n_cg);
     return cudaGetLastError();
 }
 
@@ -135,7 +135,7 @@ static cudaError_t launch_mma(const SpreadArgs &a, int64_t n_sub, cudaStream_t s
         auto kern = k_spread_mma<2, WT, false>;
         cudaError_t e = set_smem(kern, kMmaSmemBytes);
         if (e != cudaSuccess) return e;
-        kern<<<(unsigned)n_units, kMmaThreads, kMmaSmemBytes, s>>>(a, a.status, n_cg);
+        kern<<<(unsigned)n_units, mma_threads<false>(), kMmaSmemBytes, s>>>(a, a.status, n_cg);
         return cudaGetLastError();
     }
     cudaError_t e = launch_mma_instance<WT, false>(a, n_units, n_cg, s);

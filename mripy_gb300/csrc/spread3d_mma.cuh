@@ -59,9 +59,10 @@ constexpr int kMmaSlots = 8;                        // staged batches
 #define GBN_MMA_LOADERS 3
 #endif
 constexpr int kMmaLoaders = GBN_MMA_LOADERS;
-constexpr int kMmaBuilders = 8;
-constexpr int kMmaWarp = kMmaBuilders + kMmaLoaders;  // the MMA warp's index
-constexpr int kMmaThreads = 32 * (kMmaWarp + 1);
+// builder warps: 8 in the plain instance (two blocks per SM, registers), 16 in the
+// compensated one (one block per SM: more warps hide its latencies)
+template <bool KAHAN> constexpr int mma_builders() { return KAHAN ? 16 : 8; }
+template <bool KAHAN> constexpr int mma_threads() { return 32 * (mma_builders<KAHAN>() + kMmaLoaders + 1); }
 constexpr uint32_t kMmaTmemCols = 256;              // A (hi, lo) x 2 buffers: 0..127; D, S: 128..255
 constexpr uint32_t kMmaColD = 128;                  // the MMAs' accumulator
 constexpr uint32_t kMmaColS = 192;                  // the running sum of the drained accumulators (3-D)
@@ -171,12 +172,13 @@ __device__ __forceinline__ void mma_drain(uint32_t tl, int hk, bool first) {
     }
 }
 
-// S, C (+)= D[col_d] with Kahan compensation over this thread's lane and the 32 columns of
-// half hk (scalar FP32 operations); `first`: S = D, C = 0
-__device__ __forceinline__ void mma_drain_kahan(uint32_t tl, int hk, uint32_t col_d, bool first) {
+// S, C (+)= D[col_d] with Kahan compensation over this thread's lane and NCH 16-column
+// chunks from column col0 (scalar FP32 operations); `first`: S = D, C = 0
+template <int NCH>
+__device__ __forceinline__ void mma_drain_kahan(uint32_t tl, uint32_t col0, uint32_t col_d, bool first) {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const uint32_t col = 32u * hk + 16u * h;
+    for (int h = 0; h < NCH; ++h) {
+        const uint32_t col = col0 + 16u * h;
         float d[16], s[16], c[16];
         tmem_ld_x16(tl + col_d + col, d);
         if (first) {
@@ -205,7 +207,12 @@ __device__ __forceinline__ void mma_drain_kahan(uint32_t tl, int hk, uint32_t co
 // rather than a device function behind per-dimension kernels: the arguments stay in the
 // parameter space (an inlined copy of them cost registers and 4.5 % of the 3-D time).
 template <int D, int WT, bool KAHAN>
-__global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(SpreadArgs a, uint32_t *status, int n_cg) {
+__global__ void __launch_bounds__(mma_threads<KAHAN>(), KAHAN ? 1 : 2) k_spread_mma(SpreadArgs a, uint32_t *status, int n_cg) {
+    constexpr int NB = mma_builders<KAHAN>();  // builder warps
+    constexpr int WM = NB + kMmaLoaders;       // the MMA warp's index
+    constexpr int SPW = 128 / NB;              // A: samples of the batch per builder warp (16 or 8)
+    constexpr int RPW = mma_n<D>() / NB;       // B: rows per builder warp
+    constexpr int CPW = 256 / NB;              // accumulator columns per builder warp (3-D)
     using T = MmaTile<D>;
     constexpr int N = mma_n<D>();
     constexpr uint32_t kBOp = N * 128;  // one B operand: N rows x 128 B
@@ -227,17 +234,17 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int W = WT ? WT : g.W;
 
-    if (warp == kMmaWarp) {
+    if (warp == WM) {
         tmem_alloc(tslot, kCols);
         tmem_relinquish();
     }
     if (threadIdx.x == 0) {
         for (int k = 0; k < kMmaSlots; ++k) {
             mbar_init(&full[k], 32);                  // the loader warp, every lane
-            mbar_init(&empty[k], kMmaBuilders * 32);  // every builder lane
+            mbar_init(&empty[k], NB * 32);  // every builder lane
         }
         for (int b = 0; b < 2; ++b) {
-            mbar_init(&ops[b], kMmaBuilders * 32);
+            mbar_init(&ops[b], NB * 32);
             mbar_init(&done[b], 1);                   // tcgen05.commit
         }
         fence_barrier_init();
@@ -253,11 +260,11 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
         const int nb = (sub.z + B - 1) / B;
         const int cg0 = (int)(unit % n_cg) * CG;
 
-        if (warp >= kMmaBuilders && warp < kMmaWarp) {
+        if (warp >= NB && warp < WM) {
             // ------------------------------------------------------------ loader warp
             int o[3], e[3];
             tile_coords<D>(g, sub.x % g.ntiles, o, e);
-            const int lw = warp - kMmaBuilders;
+            const int lw = warp - NB;
             const int ns = g.ns;
             const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
             for (int k = lw; k < nb; k += kMmaLoaders) {
@@ -316,7 +323,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
                 for (int cc = 0; cc < CG; ++cc) vs[cc * B + lane] = v[cc];
                 mbar_arrive(&full[slot]);
             }
-        } else if (warp == kMmaWarp) {
+        } else if (warp == WM) {
             // ------------------------------------------------------------ MMA warp
             if (lane == 0) {
                 constexpr uint32_t idesc = tc_idesc_tf32(kMmaM, N);
@@ -342,9 +349,12 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
             __syncwarp();
         } else {
             // ------------------------------------------------------------ builder warp
-            const int q = warp & 3, hk = warp >> 2;  // TMEM quarter; half of the batch's samples
+            // warp (q, hk): TMEM quarter q; A for samples SPW hk .. SPW hk + SPW - 1 of a batch;
+            // B rows RPW warp .. (3-D: x plane bx, coils bc0 .. bc0 + RPW / 2 - 1); the
+            // accumulator's columns CPW hk .. (3-D)
+            const int q = warp & 3, hk = warp >> 2;
             const int m = 32 * q + lane, y = m >> 4, z = m & 15;  // tile cell (y, z) of TMEM lane m
-            const int bx = warp >> 1, bc0 = 4 * (warp & 1);  // 3-D B rows: x = bx, coils bc0 .. bc0 + 3
+            const int bx = (RPW * warp) >> 4, bc0 = ((RPW * warp) & 15) >> 1;
             const uint32_t tl = tmem_lane_base(tbase, q);
             for (int k = 0; k < nb; ++k) {
                 const int slot = k % kMmaSlots, buf = k & 1;
@@ -358,8 +368,8 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
                     const int *rs = reinterpret_cast<const int *>(slw + kMmaStR);
                     constexpr int XT = D == 3 ? kMmaTX : 0;  // planes along N's grid dimension
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const int jt = warp + 8 * i;
+                    for (int i = 0; i < (T::TAPS + NB - 1) / NB; ++i) {
+                        const int jt = warp + NB * i;
                         if (jt >= T::TAPS) break;
                         const int reg = jt < XT ? 0 : (jt < XT + kMmaTY ? 1 : 2);  // x, y or z planes
                         const int t = jt - (reg == 0 ? 0 : (reg == 1 ? XT : XT + kMmaTY));
@@ -372,7 +382,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
                         reinterpret_cast<float *>(slw + (reg == 0 ? kMmaStWx : (reg == 1 ? kMmaStWy : kMmaStWz)))
                             [t * kMmaWS + lane] = in ? wv : 0.f;
                     }
-                    asm volatile("bar.sync 1, %0;" ::"n"(kMmaBuilders * 32) : "memory");
+                    asm volatile("bar.sync 1, %0;" ::"n"(NB * 32) : "memory");
                 }
                 // the MMAs of batch k - 2 (same operand buffer) have completed
                 if (k >= 2 && !mbar_wait_bounded(&done[buf], (uint32_t)(((k >> 1) - 1) & 1)) && lane == 0)
@@ -381,15 +391,15 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
                     if (k >= 2) {
                         // batch k - 2's accumulator D[k % 2] into S, C before batch k overwrites it
                         tc_fence_after();
-                        mma_drain_kahan(tl, hk, kMmaColD + 64u * buf, k == 2);
+                        mma_drain_kahan<CPW / 16>(tl, CPW * hk, kMmaColD + 64u * buf, k == 2);
                     }
                 }
                 const unsigned char *sl = stage + (size_t)slot * kMmaSlotBytes;
-                // A: cells (y, z) of this lane, samples 16 hk .. 16 hk + 15
-                const float4 *wy4 = reinterpret_cast<const float4 *>(sl + kMmaStWy) + (y * kMmaWS + 16 * hk) / 4;
-                const float4 *wz4 = reinterpret_cast<const float4 *>(sl + kMmaStWz) + (z * kMmaWS + 16 * hk) / 4;
+                // A: cells (y, z) of this lane, samples SPW hk .. SPW hk + SPW - 1
+                const float4 *wy4 = reinterpret_cast<const float4 *>(sl + kMmaStWy) + (y * kMmaWS + SPW * hk) / 4;
+                const float4 *wz4 = reinterpret_cast<const float4 *>(sl + kMmaStWz) + (z * kMmaWS + SPW * hk) / 4;
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {  // 8 samples at a time: fewer live registers
+                for (int h = 0; h < SPW / 8; ++h) {  // 8 samples at a time: fewer live registers
                     float hi[8], lo[8];
 #pragma unroll
                     for (int i = 0; i < 2; ++i) {
@@ -406,16 +416,16 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
                         lo[4 * i + 2] = l1.x;
                         lo[4 * i + 3] = l1.y;
                     }
-                    tmem_st_x8(tl + 64u * buf + 16u * hk + 8u * h, hi);
-                    tmem_st_x8(tl + 64u * buf + 32u + 16u * hk + 8u * h, lo);
+                    tmem_st_x8(tl + 64u * buf + SPW * hk + 8u * h, hi);
+                    tmem_st_x8(tl + 64u * buf + 32u + SPW * hk + 8u * h, lo);
                 }
                 const float2 *vs = reinterpret_cast<const float2 *>(sl + kMmaStV);
                 unsigned char *bh = opB + (size_t)(2 * buf) * kBOp, *bl = bh + kBOp;
                 if constexpr (D == 3) {
-                    // B: rows (x = bx, coils bc0 .. bc0 + 3, re/im) for sample `lane`
+                    // B: rows (x = bx, coils bc0 .. bc0 + RPW / 2 - 1, re/im) for sample `lane`
                     const float wxk = reinterpret_cast<const float *>(sl + kMmaStWx)[bx * kMmaWS + lane];
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) {
+                    for (int cc = 0; cc < RPW / 2; ++cc) {
                         const float2 vv = vs[(bc0 + cc) * B + lane];
                         const int nre = bx * 16 + (bc0 + cc) * 2;
                         float2 h, l;
@@ -461,7 +471,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
                 if constexpr (KAHAN) {
                     // the last two batches' accumulators, in order
                     for (int j = max(0, nb - 2); j < nb; ++j) {
-                        mma_drain_kahan(tl, hk, kMmaColD + 64u * (j & 1), j == 0);
+                        mma_drain_kahan<CPW / 16>(tl, CPW * hk, kMmaColD + 64u * (j & 1), j == 0);
                         tmem_wait_st();  // S and C stored before the next drain reads them
                     }
                 }
@@ -474,24 +484,24 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
             const bool split = (su.w & kSplitFlag) != 0;
             const bool inside = y < e[T::DY] && z < e[T::DZ];
             if constexpr (D == 3) {
-                // this warp: lanes of quarter q, columns 32 hk .. 32 hk + 31 (x = 2 hk, 2 hk + 1)
+                // this warp: lanes of quarter q, columns CPW hk .. (x planes CPW hk / 16 ..)
                 const int64_t cell_yz = (int64_t)(o[1] + y) * g.nf[2] + (o[2] + z);
 #pragma unroll
-                for (int xi = 0; xi < 2; ++xi) {
-                    // columns 32 hk + 16 xi ..: cell x = 2 hk + xi, (coil, re/im) pairs
+                for (int xi = 0; xi < CPW / 16; ++xi) {
+                    // columns CPW hk + 16 xi ..: cell x = (CPW / 16) hk + xi, (coil, re/im) pairs
                     float dv[16];
                     if (nb > 0 && KAHAN) {
                         float cv[16];
-                        tmem_ld_x16(tl + kMmaColSK + 32u * hk + 16u * xi, dv);
-                        tmem_ld_x16(tl + kMmaColCK + 32u * hk + 16u * xi, cv);
+                        tmem_ld_x16(tl + kMmaColSK + CPW * hk + 16u * xi, dv);
+                        tmem_ld_x16(tl + kMmaColCK + CPW * hk + 16u * xi, cv);
                         tmem_wait_ld();
 #pragma unroll
                         for (int i = 0; i < 16; ++i) dv[i] -= cv[i];
                     } else if (nb > 0) {
-                        tmem_ld_x16(tl + kMmaColD + 32u * hk + 16u * xi, dv);
+                        tmem_ld_x16(tl + kMmaColD + CPW * hk + 16u * xi, dv);
                         if (nb > kMmaGroup) {  // plus the drained groups
                             float sv[16];
-                            tmem_ld_x16(tl + kMmaColD + N + 32u * hk + 16u * xi, sv);
+                            tmem_ld_x16(tl + kMmaColD + N + CPW * hk + 16u * xi, sv);
                             tmem_wait_ld();
 #pragma unroll
                             for (int i = 0; i < 16; ++i) dv[i] += sv[i];
@@ -502,7 +512,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
 #pragma unroll
                         for (int i = 0; i < 16; ++i) dv[i] = 0.f;
                     }
-                    const int x = 2 * hk + xi;
+                    const int x = (CPW / 16) * hk + xi;
                     if (!inside || x >= e[0]) continue;
                     const int64_t cell = (int64_t)(o[0] + x) * g.nf[1] * g.nf[2] + cell_yz;
 #pragma unroll
@@ -556,7 +566,7 @@ __global__ void __launch_bounds__(kMmaThreads, KAHAN ? 1 : 2) k_spread_mma(Sprea
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == kMmaWarp) tmem_dealloc(tbase, kCols);
+    if (warp == WM) tmem_dealloc(tbase, kCols);
 }
 
 
