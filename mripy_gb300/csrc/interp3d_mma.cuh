@@ -137,7 +137,9 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
         // ---------------------------------------------------------------- MMA warp
         if (lane == 0) {
             constexpr uint32_t idesc = tc_idesc_tf32(kImBatch, kMmaN);
-            const uint32_t b_hi = smem_addr(bh), b_lo = smem_addr(bl);
+            // descriptors of B's first K step; a K step's offset adds (bytes / 16) to the
+            // address field (shared addresses stay far below its 14-bit range)
+            const uint64_t dbh = tc_desc_sw128(smem_addr(bh)), dbl = tc_desc_sw128(smem_addr(bl));
             for (int b = 0; b < nb; ++b) {
                 const int tb = b & 1;
                 // T[tb] was read out by the builders (batch b - 2)
@@ -152,10 +154,10 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
                     const uint32_t ah = tbase + 64u * buf, al = ah + 32u;
 #pragma unroll
                     for (int ks = 0; ks < 4; ++ks) {
-                        const uint32_t kb = (uint32_t)ch * kImBAtom + 32u * ks;
-                        tc_mma_tf32_ts(d, ah + 8u * ks, tc_desc_sw128(b_hi + kb), idesc, (ch | ks) != 0);
-                        tc_mma_tf32_ts(d, ah + 8u * ks, tc_desc_sw128(b_lo + kb), idesc, 1u);
-                        tc_mma_tf32_ts(d, al + 8u * ks, tc_desc_sw128(b_hi + kb), idesc, 1u);
+                        const uint64_t kb = ((uint64_t)ch * kImBAtom + 32u * ks) >> 4;
+                        tc_mma_tf32_ts(d, ah + 8u * ks, dbh + kb, idesc, (ch | ks) != 0);
+                        tc_mma_tf32_ts(d, ah + 8u * ks, dbl + kb, idesc, 1u);
+                        tc_mma_tf32_ts(d, al + 8u * ks, dbh + kb, idesc, 1u);
                     }
                     tc_commit(&done[buf]);
                 }

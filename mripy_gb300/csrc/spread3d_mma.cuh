@@ -334,14 +334,17 @@ __global__ void __launch_bounds__(mma_threads<KAHAN>(), KAHAN ? 1 : 2) k_spread_
                     tc_fence_after();
                     const uint32_t ah = tbase + 64u * buf, al = ah + 32u;
                     const uint32_t d = tbase + kMmaColD + (KAHAN ? 64u * buf : 0u);
-                    const uint32_t bh = b0 + 2u * buf * kBOp, bl = bh + kBOp;
+                    // K step jk starts 32 jk bytes further: + 2 jk in the descriptor's address
+                    // field (16-byte units; shared addresses stay far below its 14-bit range)
+                    const uint64_t dbh = tc_desc_sw128(b0 + 2u * buf * kBOp), dbl = tc_desc_sw128(b0 + (2u * buf + 1u) * kBOp);
+                    // plain: a group's first MMA starts D afresh; compensated: every batch's
+                    const uint32_t acc0 = KAHAN ? 0u : (uint32_t)((k % kMmaGroup) != 0);
 #pragma unroll
                     for (int jk = 0; jk < B / 8; ++jk) {
-                        // plain: a group's first MMA starts D afresh; compensated: every batch's
-                        tc_mma_tf32_ts(d, ah + 8u * jk, tc_desc_sw128(bh + 32u * jk), idesc,
-                                       KAHAN ? jk != 0 : ((k % kMmaGroup) != 0 || jk != 0));
-                        tc_mma_tf32_ts(d, ah + 8u * jk, tc_desc_sw128(bl + 32u * jk), idesc, 1u);
-                        tc_mma_tf32_ts(d, al + 8u * jk, tc_desc_sw128(bh + 32u * jk), idesc, 1u);
+                        const uint64_t xh = dbh + (uint64_t)(2 * jk), xl = dbl + (uint64_t)(2 * jk);
+                        tc_mma_tf32_ts(d, ah + 8u * jk, xh, idesc, jk == 0 ? acc0 : 1u);
+                        tc_mma_tf32_ts(d, ah + 8u * jk, xl, idesc, 1u);
+                        tc_mma_tf32_ts(d, al + 8u * jk, xh, idesc, 1u);
                     }
                     tc_commit(&done[buf]);
                 }
