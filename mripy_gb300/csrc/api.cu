@@ -260,9 +260,10 @@ int spread_cg(const gbn_plan *p) {
     return cg;
 }
 
-// the 3-D cube kernel runs this plan's spreads; it alone reads interleaved work items, so
-// set_points builds them exactly when this holds
-bool spread_interleaved(const gbn_plan *p) { return spread_cube_applies(p->gs, spread_cg(p), p->spread_variant); }
+// the cube or tensor-core kernel runs this plan's spreads; they alone read interleaved work
+// items (the tensor-core interp reads them too), so set_points builds them exactly when this
+// holds
+bool spread_interleaved(const gbn_plan *p) { return spread_reads_interleaved(p->gs, spread_cg(p), p->spread_variant); }
 
 int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, float2 *grid, cudaStream_t s) {
     NvtxRange range("gbn spread");

@@ -175,8 +175,9 @@ cudaError_t launch_zero_split(const Geom &g, const uint32_t *split_tiles, int64_
                               cudaStream_t s);
 cudaError_t launch_spread(const SpreadArgs &a, int64_t n_sub, int coil_group, int threads,
                           cudaStream_t s);
-// the 3-D cube spread runs these arguments (the kernel that reads interleaved work items)
-bool spread_cube_applies(const Geom &g, int coil_group, int variant);
+// the cube or tensor-core spread runs these arguments (the kernels that read interleaved
+// work items)
+bool spread_reads_interleaved(const Geom &g, int coil_group, int variant);
 // the 3-D 8-coil spread kernel launch_spread runs: 3 tensor cores, 2 cubes, 1 warp rows, 0 other
 int spread_path_kind(const Geom &g, int coil_group, int variant, int threads);
 // kernels launch_spread runs for these arguments (the 3-D register path adds a Kahan instance)

@@ -67,7 +67,7 @@ static bool mma_path(const Geom &g, int coil_group, int variant) {
 }
 
 // the cube and tensor-core kernels read interleaved work items
-bool spread_cube_applies(const Geom &g, int coil_group, int variant) {
+bool spread_reads_interleaved(const Geom &g, int coil_group, int variant) {
     return cube_path(g, coil_group, variant) != 0 || mma_path(g, coil_group, variant);
 }
 

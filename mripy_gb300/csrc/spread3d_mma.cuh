@@ -1,4 +1,5 @@
-// 3-D spread (type-1 gridding) of 8 coils on the tensor cores.
+// Spread (type-1 gridding) of 8 coils on the tensor cores: k_spread_mma<D, WT, KAHAN>, 3-D
+// (the default for 8 coils) and 2-D (selectable).
 //
 // The adjoint gridding of one tile is a sum of outer products over its samples s:
 //     G[x, y, z, c] = sum_s wx_s[x] wy_s[y] wz_s[z] v_s[c]
@@ -7,39 +8,43 @@
 //     D[(y, z), (x, c, re/im)] = sum_s A[(y, z), s] * B[s, (x, c, re/im)]
 //     A[(y, z), s] = wy_s[y] wz_s[z]                      (M = 8 x 16 = 128 cells)
 //     B[s, (x, c, ri)] = wx_s[x] * (re, im)(v_s[c])       (N = 4 x 8 x 2 = 64)
-// on tiles of 4 x 8 x 16 cells.  The accumulator D lives in tensor memory (TMEM); A is built
-// in TMEM (tcgen05.st), B in shared memory (K-major, 128-byte swizzle); one
-// tcgen05.mma.kind::tf32 covers 8 samples.  Each FP32 operand is split as x = hi + lo with
-// hi on the TF32 grid, and three MMAs (hi*hi + hi*lo + lo*hi) give products within ~1e-6 of
-// FP32 (the lo*lo term, below 2^-22 relative, is left out).  The tensor core evaluates the
-// whole tile for every sample (a 12-tap stencil covers ~22 % of a 4 x 8 x 16 tile on
-// average) but needs no per-cell instruction: the CUDA cores build 192 operand values per
-// (sample, tile) pair instead of issuing the stencil's FMAs.
+// on tiles of 4 x 8 x 16 cells (2-D: tiles of 8 x 16 cells, the two grid axes in the roles
+// of y and z, and B the coil values alone, N = 16).  The accumulator D lives in tensor memory
+// (TMEM); A is built in TMEM (tcgen05.st), B in shared memory (K-major, 128-byte swizzle);
+// one tcgen05.mma.kind::tf32 covers 8 samples.  Each FP32 operand is split as x = hi + lo
+// with hi on the TF32 grid, and three MMAs (hi*hi + hi*lo + lo*hi) give products within
+// ~1e-6 of FP32 (the lo*lo term, below 2^-22 relative, is left out).  The tensor core
+// evaluates the whole tile for every sample (a 12-tap stencil covers ~22 % of a 4 x 8 x 16
+// tile on average) but needs no per-cell instruction: the CUDA cores build 192 operand
+// values per (sample, tile) pair instead of issuing the stencil's FMAs.
 //
-// One (work item, coil group) unit per block, 12 warps:
-// * 3 loader warps fill a ring of kMmaSlots 32-sample batches (loader l: batches l, l + 3,
+// One (work item, coil group) unit per block; 3 loader warps, NB builder warps (8 in the
+// plain instance, 16 in the compensated one) and 1 MMA warp:
+// * the loader warps fill a ring of kMmaSlots 32-sample batches (loader l: batches l, l + 3,
 //   ...): per sample and dimension the first tap's tile plane and the distance of plane 0,
 //   and the 8 coil values times the optional density weight ([coil][sample]); `full` /
 //   `empty` mbarriers per slot.
-// * 8 builder warps first compute the batch's 28 tile-plane weights per sample together
+// * the builder warps first compute the batch's tile-plane weights per sample together
 //   (stored [plane][sample]; a named barrier among them), then turn the batch into the MMA
-//   operands: warp b writes A's hi and lo parts
-//   for the 32 TMEM lanes of its quarter (b % 4) and 16 of the 32 samples (b / 4), and 8 of
-//   B's 64 rows into shared memory; two operand buffers, the one of batch t reused by batch
-//   t + 2 after the MMAs of batch t completed (`done` mbarrier, signalled by tcgen05.commit).
-//   After the last batch they read D back (tcgen05.ld) and write the tile.
-// * 1 MMA warp: allocates TMEM, and its lane 0 issues 12 MMAs per batch once the builders
+//   operands: warp b writes A's hi and lo parts for the 32 TMEM lanes of its quarter (b % 4)
+//   and 128 / NB of the 32 samples, and N / NB of B's rows into shared memory; two operand
+//   buffers, the one of batch t reused by batch t + 2 after the MMAs of batch t completed
+//   (`done` mbarrier, signalled by tcgen05.commit).  After the last batch they read D back
+//   (tcgen05.ld) and write the tile.
+// * the MMA warp allocates TMEM, and its lane 0 issues 12 MMAs per batch once the builders
 //   arrived on the buffer's `ops` mbarrier, then commits to the buffer's `done` mbarrier.
 // Summation: the tensor core's FP32 accumulation rounds less carefully than FP32 adds (its
 // error grew with the number of accumulated MMAs: 1.6e-6 relative to the FP32 kernel with
-// 1024-sample work items, 4.9e-6 with 8192, on the 3-D radial workload), so it sums groups
-// of kMmaGroup batches (256 samples, 96 MMAs) only; the builders then add the accumulator
-// into a running sum S in TMEM with FP32 adds before the next group's first MMA overwrites
-// it.  The order is fixed for a given trajectory and tiling.
+// 1024-sample work items, 4.9e-6 with 8192, on the 3-D radial workload), so the plain
+// instance sums groups of kMmaGroup batches (256 samples, 96 MMAs) only; the builders then
+// add the accumulator into a running sum S in TMEM with FP32 adds before the next group's
+// first MMA overwrites it.  The compensated instance (KAHAN: the 3-D dense, k-space-centre
+// units, one block per SM) drains every batch's accumulator (two of them alternate) into a
+// Kahan-compensated sum S, C in TMEM.  The order is fixed for a given trajectory and tiling.
 //
 // Every wait is bounded (kTmaWaitLimit probes); one that gives up sets kStatusSpreadTimeout
-// in the plan's status word and goes on, so no launch can hang.  Only the units without the
-// dense flag run here: dense (k-space centre) units take the Kahan-compensated cube kernel.
+// in the plan's status word and goes on, so no launch can hang.  Each instance runs the
+// units of its own kind (dense or not) and skips the others.
 #pragma once
 
 #include "common.cuh"
