@@ -8,8 +8,8 @@ batch's accumulator; its centre-cell error against FP64 on 3-D radial data), lon
 items (many passes over the batch ring and both operand buffers), stencils across the
 periodic edge, odd oversampled grids with partial edge tiles, a grid
 buffer that is not 16-byte aligned, density weights, empty work items (zeros written
-without an MMA), run-to-run bit equality, agreement with the FP32 cube kernel, and the
-status word (clean after every call).
+without an MMA), ragged trajectory groups, run-to-run bit equality, agreement with the FP32
+cube kernel, and the status word (clean after every call).
 
 Tolerance: TOL_REF = 2e-5 relative L2 against the FP64 oracle (the 3-term TF32 products are
 within ~1e-6 of FP32); 5e-6 relative L2 against the FP32 cube kernel.
@@ -178,3 +178,24 @@ def test_mma_compensated_centre_tiles_3d_radial():
         p.close()
     assert errs[2048] < 6e-7
     assert errs[2048] < 0.4 * errs[-1]
+
+
+def test_mma_ragged_trajectory_groups():
+    """Three trajectory groups of unequal size (one of 30 samples) in one plan: each group's
+    grid against the oracle, through the work items' group index."""
+    rng = np.random.default_rng(75)
+    shape, nc = (28, 28, 28), 8
+    counts = [6000, 30, 4000]
+    off = np.concatenate([[0], np.cumsum(counts)])
+    xs = _points(rng, int(off[-1]))
+    c = cvec(rng, (int(off[-1]), nc))
+    p = NufftPlan(3, shape, n_coil=nc, n_traj=3, eps=5e-6, max_nspread=6, tuning=MMA)
+    p.set_points([cuda(v) for v in xs], traj_offsets=[int(v) for v in off])
+    assert p.info()["spread_tile"] == (4, 8, 16)
+    F = p.type1(cuda(c))
+    p.status()
+    for k in range(3):
+        a, b = int(off[k]), int(off[k + 1])
+        Fo = O.nufft_type1(tuple(x[a:b] for x in xs), c[a:b].astype(np.complex128), shape, eps=5e-6)
+        assert rel(F[k], Fo) < TOL_REF
+    p.close()
