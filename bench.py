@@ -397,7 +397,11 @@ def run_gpu(args, wl):
     t_interp, _ = event_time(torch, lambda: plan.interp(grid_copy, out=samples), reps, stream, flush)
     t_spread, _ = event_time(torch, lambda: plan.spread(samples, grid), reps, stream, flush)
     t_pad, _ = event_time(torch, lambda: plan.pad_deapod(img, grid), reps, stream, flush)
-    t_fft, _ = event_time(torch, lambda: plan.fft(grid, N.GBN_FFT_FORWARD), reps, stream, flush)
+    # the step's transforms: pruned to the image band where the plan says so (fft_variant 2)
+    t_fft, _ = event_time(torch, lambda: plan.fft_band(grid, N.GBN_FFT_FORWARD, N.GBN_BAND_INPUT), reps, stream, flush)
+    t_fft_inv, _ = event_time(torch, lambda: plan.fft_band(grid, N.GBN_FFT_INVERSE, N.GBN_BAND_OUTPUT), reps, stream,
+                              flush)
+    t_fft_full, _ = event_time(torch, lambda: plan.fft(grid, N.GBN_FFT_FORWARD), reps, stream, flush)
     t_crop, _ = event_time(torch, lambda: plan.crop_deapod(grid, out_img), reps, stream, flush)
     del grid_copy
     G = info["grid_cells"]
@@ -469,7 +473,9 @@ def run_gpu(args, wl):
             "stencil_fp32_tflops": round(fl / (t_spread * 1e-3) / 1e12, 2),
             "stencil_fp32_frac": round(fl / (t_spread * 1e-3) / 1e12 / fp32_peak, 4)}
     result["kernels_ms"] = {"interp": round(t_interp, 4), "spread": round(t_spread, 4), "pad_deapod": round(t_pad, 4),
-                            "fft": round(t_fft, 4), "crop_deapod": round(t_crop, 4)}
+                            "fft": round(t_fft, 4), "fft_inverse": round(t_fft_inv, 4),
+                            "fft_full_transform": round(t_fft_full, 4), "crop_deapod": round(t_crop, 4),
+                            "fft_pruned_to_band": info["fft_variant"] == 2}
     # this library's kernels per step (cuFFT and memsets not counted): pad, interp, crop and
     # what the spread launched in the eager step before capture (split-tile zeroing unless the
     # grid is cleared by a memset; the 3-D compensated instance for dense tiles)
@@ -922,9 +928,10 @@ def step_kernels(torch, wl, coords, tuning, reps=3):
     out = torch.empty_like(img)
     grid = plan.grid()
     stream = torch.cuda.current_stream()
-    stages = {"pad_deapod": lambda: plan.pad_deapod(img, grid), "fft": lambda: plan.fft(grid, N.GBN_FFT_FORWARD),
+    stages = {"pad_deapod": lambda: plan.pad_deapod(img, grid),
+              "fft": lambda: plan.fft_band(grid, N.GBN_FFT_FORWARD, N.GBN_BAND_INPUT),
               "interp": lambda: plan.interp(grid, out=samples), "spread": lambda: plan.spread(samples, grid),
-              "fft_inverse": lambda: plan.fft(grid, N.GBN_FFT_INVERSE),
+              "fft_inverse": lambda: plan.fft_band(grid, N.GBN_FFT_INVERSE, N.GBN_BAND_OUTPUT),
               "crop_deapod": lambda: plan.crop_deapod(grid, out)}
     for f in stages.values():
         f()

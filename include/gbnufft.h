@@ -52,6 +52,9 @@ typedef struct CUstream_st *gbn_stream_t; /* == cudaStream_t; NULL = legacy defa
 #define GBN_FFT_FORWARD (-1) /* exp(-i ...), numpy.fft.fftn, unnormalised */
 #define GBN_FFT_INVERSE (+1) /* exp(+i ...), unnormalised                  */
 
+#define GBN_BAND_INPUT 1  /* gbn_fft_band: the grid is zero outside the image band (as the pad leaves it) */
+#define GBN_BAND_OUTPUT 2 /* gbn_fft_band: only the image band of the result is read (as the crop reads it) */
+
 typedef struct gbn_plan gbn_plan;   /* opaque */
 typedef struct gbn_graph gbn_graph; /* opaque captured CUDA graph */
 
@@ -94,6 +97,14 @@ typedef struct {
                                    kernels on the interp's own bins, 2 = tensor cores where
                                    the spread's tiles allow (per tile a TF32 GEMM over the
                                    tile's samples, partial sums added with float atomics) */
+    int32_t fft_variant;        /* FFT of the composite calls (type 1/2/21, SENSE): 0 = library
+                                   choice (pruned on 3-D grids of >= 2^21 cells per instance,
+                                   <= 256 instances), 1 = the full transform, 2 = pruned
+                                   wherever the image band is narrower than the grid (2-D and
+                                   3-D, <= 4096 instances).  Pruned: the trailing axes are
+                                   transformed only on the grid planes inside the image band
+                                   along x, which hold every non-zero cell of the pad and
+                                   every cell the crop reads (see gbn_fft_band) */
 } gbn_plan_desc;
 
 typedef struct {
@@ -123,6 +134,7 @@ typedef struct {
     int32_t interp_variant;    /* 2 when the interp runs on the tensor cores (3-D, 8 coils per
                                   group; partial sums added with float atomics, so the
                                   samples agree run to run to rounding), else 1 */
+    int32_t fft_variant;       /* 2 when the composite calls run the pruned transform, else 1 */
 } gbn_plan_info;
 
 /* element strides (in complex64 elements) of a strided complex array */
@@ -184,6 +196,15 @@ int gbn_interp(gbn_plan *plan, const void *grid, void *c, gbn_layout c_layout, c
 
 /* batched in-place C2C FFT of the grid over all instances (cuFFT). */
 int gbn_fft(gbn_plan *plan, void *grid, int direction, gbn_stream_t stream);
+/* The transform the composite calls run between the pad and the interp (band =
+ * GBN_BAND_INPUT) and between the spread and the crop (GBN_BAND_OUTPUT).  With the plan's
+ * pruned transform (gbn_plan_info.fft_variant 2) the trailing axes are transformed only on the
+ * grid planes inside the image band along x, x in [0, m - m/2) and [nf - m/2, nf):
+ * GBN_BAND_INPUT assumes every other plane is zero and gives the full transform;
+ * GBN_BAND_OUTPUT leaves the cells of the other planes holding the x pass only.  Otherwise
+ * it is gbn_fft.  No counterpart in the reference (numpy / cuFFT full transforms,
+ * fft/nufft_func.py:751-764, fft/nufft_func_cuda.py). */
+int gbn_fft_band(gbn_plan *plan, void *grid, int direction, int band, gbn_stream_t stream);
 
 /* image -> zero-padded grid with (pi/tau)^(d/2) exp(tau|k|^2) / N
  * (nufft_func.py:751-764) */

@@ -15,13 +15,15 @@ GBN_COORD_F32 = 0
 GBN_COORD_F64 = 1
 GBN_FFT_FORWARD = -1
 GBN_FFT_INVERSE = 1
+GBN_BAND_INPUT = 1    # gbn_fft_band: the grid is zero outside the image band (after the pad)
+GBN_BAND_OUTPUT = 2   # gbn_fft_band: only the image band of the result is read (by the crop)
 
 # every function the header declares, for the export check in the CPU tests
 EXPORTED = (
     "gbn_version", "gbn_status_string", "gbn_last_error", "gbn_grid_params",
     "gbn_plan_create", "gbn_plan_destroy", "gbn_plan_get_info", "gbn_plan_status", "gbn_plan_check_wait_expiry",
     "gbn_set_points", "gbn_plan_grid",
-    "gbn_spread", "gbn_interp", "gbn_fft", "gbn_pad_deapod", "gbn_crop_deapod",
+    "gbn_spread", "gbn_interp", "gbn_fft", "gbn_fft_band", "gbn_pad_deapod", "gbn_crop_deapod",
     "gbn_type1", "gbn_type2", "gbn_type21",
     "gbn_sense_forward", "gbn_sense_adjoint", "gbn_sense_normal",
     "gbn_interp_grad_coords",
@@ -44,6 +46,7 @@ class PlanDesc(ctypes.Structure):
         ("interp_threads", ctypes.c_int32), ("interp_coil_group", ctypes.c_int32),
         ("interp_staging", ctypes.c_int32), ("dense_tile_samples", ctypes.c_int32),
         ("spread_variant", ctypes.c_int32), ("interp_variant", ctypes.c_int32),
+        ("fft_variant", ctypes.c_int32),
     ]
 
 
@@ -57,7 +60,7 @@ class PlanInfo(ctypes.Structure):
         ("interp_threads", ctypes.c_int32), ("max_subproblem", ctypes.c_int32), ("device_bytes", ctypes.c_int64),
         ("interp_coil_group", ctypes.c_int32), ("dense_subproblems", ctypes.c_int64),
         ("spread_kernels", ctypes.c_int32), ("split_tiles", ctypes.c_int64), ("spread_variant", ctypes.c_int32),
-        ("interp_variant", ctypes.c_int32),
+        ("interp_variant", ctypes.c_int32), ("fft_variant", ctypes.c_int32),
     ]
 
 
@@ -103,6 +106,7 @@ def _declare(lib):
         "gbn_spread": ([_vp, _vp, Layout, _vp, _vp], _i32),
         "gbn_interp": ([_vp, _vp, _vp, Layout, _vp, _vp], _i32),
         "gbn_fft": ([_vp, _vp, _i32, _vp], _i32),
+        "gbn_fft_band": ([_vp, _vp, _i32, _i32, _vp], _i32),
         "gbn_pad_deapod": ([_vp, _vp, Layout, _vp, _vp], _i32),
         "gbn_crop_deapod": ([_vp, _vp, _vp, Layout, _vp], _i32),
         "gbn_type1": ([_vp, _vp, Layout, _vp, _vp, Layout, _vp], _i32),

@@ -99,6 +99,17 @@ struct gbn_plan {
     uint32_t *kstatus = nullptr;  // device status word: bits set by kernels whose bounded waits gave up
     cufftHandle fft = 0;
     bool fft_ok = false;
+    // The pruned transform of the composite calls (fft_variant): transforms of the trailing
+    // axes over the grid planes inside the image band along x (a plan per run length), and a
+    // strided pass along x per instance.  The plans share one work area.
+    int fft_variant = 0;  // 0 library choice, 1 the full transform, 2 pruned where it applies
+    bool fft_band = false;
+    cufftHandle fft_planes[3] = {0, 0, 0};
+    int fft_planes_batch[3] = {0, 0, 0};
+    int fft_n_planes = 0;
+    cufftHandle fft_x = 0;
+    bool fft_x_ok = false;
+    void *fft_work = nullptr;
 
     // tensor map of the last grid the TMA interp read (re-encoded when the grid changes)
     CUtensorMap tmap{};
@@ -242,6 +253,51 @@ int fft_exec(gbn_plan *p, float2 *grid, int direction, cudaStream_t s) {
     GBN_FFT(cufftExecC2C(p->fft, (cufftComplex *)grid, (cufftComplex *)grid,
                          direction < 0 ? CUFFT_FORWARD : CUFFT_INVERSE));
     return GBN_OK;
+}
+
+// The FFT of the composite calls.  The pad leaves every grid plane outside the image band
+// along x (x in [m - m/2, nf - m/2)) zero, and the crop reads only the band, so:
+//   band input (after the pad):   trailing-axes transforms of the band planes, then x;
+//   band output (before the crop): x, then trailing-axes transforms of the band planes.
+// The other planes' trailing-axes transforms are skipped (zero in and zero out, or never
+// read).  Plane g = instance * nf0 + x: instance i's upper band run [nf0 - m/2, nf0) and
+// instance i+1's lower run [0, m - m/2) are adjacent, so the band planes form n_inst + 1
+// runs of m - m/2, m (n_inst - 1 times) and m/2 planes.  Without a pruned transform
+// (fft_variant 1, or where it does not apply) this is the full transform.
+int fft_band_exec(gbn_plan *p, float2 *grid, int direction, int band, cudaStream_t s) {
+    if (!p->fft_band) return fft_exec(p, grid, direction, s);
+    NvtxRange range("gbn fft band");
+    const int dirc = direction < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
+    const int64_t nf0 = p->nf[0], P = p->G / nf0;
+    const int lo = p->m[0] - p->m[0] / 2, hi = p->m[0] / 2;
+    auto planes = [&]() -> int {
+        for (int64_t k = 0; k <= p->n_inst; ++k) {
+            const int64_t start = k == 0 ? 0 : k * nf0 - hi;
+            const int len = k == 0 ? lo : (k == p->n_inst ? hi : lo + hi);
+            if (len == 0) continue;
+            int j = 0;
+            while (j < p->fft_n_planes && p->fft_planes_batch[j] != len) ++j;
+            if (j == p->fft_n_planes) return fail(GBN_ERR_INTERNAL, "no FFT plan for a band run");
+            cufftComplex *ptr = (cufftComplex *)(grid + start * P);
+            GBN_FFT(cufftSetStream(p->fft_planes[j], s));
+            GBN_FFT(cufftExecC2C(p->fft_planes[j], ptr, ptr, dirc));
+        }
+        return GBN_OK;
+    };
+    auto xpass = [&]() -> int {
+        GBN_FFT(cufftSetStream(p->fft_x, s));
+        for (int64_t i = 0; i < p->n_inst; ++i) {
+            cufftComplex *ptr = (cufftComplex *)(grid + i * p->G);
+            GBN_FFT(cufftExecC2C(p->fft_x, ptr, ptr, dirc));
+        }
+        return GBN_OK;
+    };
+    if (band == GBN_BAND_INPUT) {
+        GBN_TRY(planes());
+        return xpass();
+    }
+    GBN_TRY(xpass());
+    return planes();
 }
 
 // shared memory a block may take when choosing coils per block: in 3-D two blocks per SM
@@ -676,6 +732,69 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
     return GBN_OK;
 }
 
+// Whether the composite calls run the pruned transform.  Library choice: 3-D grids of at
+// least 2^21 cells per instance (a transform pass moves >= 16 MB per instance there, so the
+// 2 n_inst + 1 plan executions of a pruned transform cost little next to it), at most 256
+// instances.  fft_variant 2 asks for it wherever the band is narrower than the grid (2-D and
+// 3-D, at most 4096 instances).
+bool fft_band_wanted(const gbn_plan *p) {
+    if (p->fft_variant == 1 || p->dim < 2 || p->m[0] >= p->nf[0] || p->G > 0x7FFFFFFF) return false;
+    if (p->fft_variant == 2) return p->n_inst <= 4096;
+    return p->dim == 3 && p->G >= ((int64_t)1 << 21) && p->n_inst <= 256;
+}
+
+// The pruned transform's plans (used by fft_band_exec): one trailing-axes plan per distinct
+// band-run length, batched over the run's planes, and the x pass (stride = plane size,
+// batched over the plane's cells), all on one work area.
+int make_fft_band(gbn_plan *p) {
+    const int lo = p->m[0] - p->m[0] / 2, hi = p->m[0] / 2;
+    const int runs[3] = {lo, p->n_inst > 1 ? lo + hi : 0, hi};
+    int n_tr[2] = {p->nf[1], p->nf[2]};
+    const int P = (int)(p->G / p->nf[0]);
+    size_t ws_max = 0;
+    auto check = [&](cufftResult r, const char *what) {
+        return r == CUFFT_SUCCESS ? GBN_OK
+                                  : fail(GBN_ERR_CUFFT, std::string(what) + " failed, cufftResult " + std::to_string((int)r));
+    };
+    for (int len : runs) {
+        if (len == 0) continue;
+        bool have = false;
+        for (int j = 0; j < p->fft_n_planes; ++j) have |= p->fft_planes_batch[j] == len;
+        if (have) continue;
+        cufftHandle h = 0;
+        GBN_TRY(check(cufftCreate(&h), "cufftCreate"));
+        p->fft_planes[p->fft_n_planes] = h;
+        p->fft_planes_batch[p->fft_n_planes] = len;
+        p->fft_n_planes += 1;
+        size_t ws = 0;
+        GBN_TRY(check(cufftSetAutoAllocation(h, 0), "cufftSetAutoAllocation"));
+        GBN_TRY(check(cufftMakePlanMany(h, p->dim - 1, n_tr, nullptr, 1, P, nullptr, 1, P, CUFFT_C2C, len, &ws),
+                      "cufftMakePlanMany (band planes)"));
+        ws_max = std::max(ws_max, ws);
+    }
+    GBN_TRY(check(cufftCreate(&p->fft_x), "cufftCreate"));
+    p->fft_x_ok = true;
+    int nx[1] = {p->nf[0]};
+    size_t ws = 0;
+    GBN_TRY(check(cufftSetAutoAllocation(p->fft_x, 0), "cufftSetAutoAllocation"));
+    GBN_TRY(check(cufftMakePlanMany(p->fft_x, 1, nx, nx, P, 1, nx, P, 1, CUFFT_C2C, P, &ws),
+                  "cufftMakePlanMany (x pass)"));
+    ws_max = std::max(ws_max, ws);
+    if (ws_max > 0) {
+        if (cudaMalloc(&p->fft_work, ws_max) != cudaSuccess) {
+            cudaGetLastError();
+            p->fft_work = nullptr;
+            return fail(GBN_ERR_ALLOC, "FFT work area allocation failed");
+        }
+        for (int j = 0; j < p->fft_n_planes; ++j)
+            GBN_TRY(check(cufftSetWorkArea(p->fft_planes[j], p->fft_work), "cufftSetWorkArea"));
+        GBN_TRY(check(cufftSetWorkArea(p->fft_x, p->fft_work), "cufftSetWorkArea"));
+        p->device_bytes += ws_max;
+    }
+    p->fft_band = true;
+    return GBN_OK;
+}
+
 int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     if (!desc || !out) return fail(GBN_ERR_ARG, "null argument");
     *out = nullptr;
@@ -751,6 +870,11 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         return fail(GBN_ERR_ARG, "spread_variant must be 0, 1, 2 or 3");
     }
     p->spread_variant = desc->spread_variant;
+    if (desc->fft_variant < 0 || desc->fft_variant > 2) {
+        delete p;
+        return fail(GBN_ERR_ARG, "fft_variant must be 0, 1 or 2");
+    }
+    p->fft_variant = desc->fft_variant;
     p->dense_min = desc->dense_tile_samples > 0 ? desc->dense_tile_samples
                                                 : (desc->dense_tile_samples < 0 ? 0 : kDenseDefault);
     p->threads = desc->threads > 0 ? desc->threads : 256;
@@ -861,6 +985,10 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     p->fft_ok = true;
     size_t ws = 0;
     if (cufftGetSize(p->fft, &ws) == CUFFT_SUCCESS) p->device_bytes += ws;
+    if (fft_band_wanted(p)) {
+        const int st = make_fft_band(p);
+        if (st != GBN_OK) return bail(st);
+    }
     *out = p;
     return GBN_OK;
 }
@@ -910,6 +1038,9 @@ int gbn_plan_create(const gbn_plan_desc *desc, gbn_plan **out) {
 int gbn_plan_destroy(gbn_plan *p) {
     if (!p) return GBN_OK;
     if (p->fft_ok) cufftDestroy(p->fft);
+    for (int i = 0; i < p->fft_n_planes; ++i) cufftDestroy(p->fft_planes[i]);
+    if (p->fft_x_ok) cufftDestroy(p->fft_x);
+    if (p->fft_work) cudaFree(p->fft_work);
     if (p->grid) cudaFree(p->grid);
     if (p->kstatus) cudaFree(p->kstatus);
     for (int d = 0; d < 3; ++d)
@@ -990,6 +1121,7 @@ int gbn_plan_get_info(const gbn_plan *p, gbn_plan_info *o) {
     o->split_tiles = p->n_split;
     o->spread_variant = spread_path_kind(p->gs, spread_cg(p), p->spread_variant, p->threads);
     o->interp_variant = interp_on_tensor_cores(p) ? 2 : 1;
+    o->fft_variant = p->fft_band ? 2 : 1;
     o->device_bytes = (int64_t)p->device_bytes;
     return GBN_OK;
 }
@@ -1023,6 +1155,14 @@ int gbn_fft(gbn_plan *p, void *grid, int direction, gbn_stream_t stream) {
     return fft_exec(p, (float2 *)grid, direction, (cudaStream_t)stream);
 }
 
+int gbn_fft_band(gbn_plan *p, void *grid, int direction, int band, gbn_stream_t stream) {
+    GBN_TRY(check_plan(p, false));
+    if (!grid) return fail(GBN_ERR_ARG, "null buffer");
+    if (band != GBN_BAND_INPUT && band != GBN_BAND_OUTPUT)
+        return fail(GBN_ERR_ARG, "band must be GBN_BAND_INPUT or GBN_BAND_OUTPUT");
+    return fft_band_exec(p, (float2 *)grid, direction, band, (cudaStream_t)stream);
+}
+
 int gbn_pad_deapod(gbn_plan *p, const void *img, gbn_layout L, void *grid, gbn_stream_t stream) {
     GBN_TRY(check_plan(p, false));
     if (!img || !grid) return fail(GBN_ERR_ARG, "null buffer");
@@ -1043,7 +1183,7 @@ int gbn_type1(gbn_plan *p, const void *c, gbn_layout cl, const float *weight, vo
     if ((!c && p->M > 0) || !img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     GBN_TRY(run_spread(p, c, cl, weight, p->grid, s));
-    GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
+    GBN_TRY(fft_band_exec(p, p->grid, dir_type1(p), GBN_BAND_OUTPUT, s));
     GBN_CUDA(launch_crop(deapod_args(p, true), p->grid, (float2 *)img, il, s));
     return GBN_OK;
 }
@@ -1053,7 +1193,7 @@ int gbn_type2(gbn_plan *p, const void *img, gbn_layout il, void *c, gbn_layout c
     if ((!c && p->M > 0) || !img) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     GBN_CUDA(launch_pad(deapod_args(p, false), (const float2 *)img, il, p->grid, s));
-    GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
+    GBN_TRY(fft_band_exec(p, p->grid, dir_type2(p), GBN_BAND_INPUT, s));
     GBN_TRY(run_interp(p, p->grid, c, cl, nullptr, s));
     return GBN_OK;
 }
@@ -1065,10 +1205,10 @@ int gbn_type21(gbn_plan *p, const void *img, gbn_layout il, void *out, gbn_layou
     cudaStream_t s = (cudaStream_t)stream;
     const gbn_layout sl = {0, 1, p->desc.n_coil};
     GBN_CUDA(launch_pad(deapod_args(p, false), (const float2 *)img, il, p->grid, s));
-    GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
+    GBN_TRY(fft_band_exec(p, p->grid, dir_type2(p), GBN_BAND_INPUT, s));
     GBN_TRY(run_interp(p, p->grid, p->scratch.p, sl, dcf, s));
     GBN_TRY(run_spread(p, p->scratch.p, sl, nullptr, p->grid, s));
-    GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
+    GBN_TRY(fft_band_exec(p, p->grid, dir_type1(p), GBN_BAND_OUTPUT, s));
     GBN_CUDA(launch_crop(deapod_args(p, true), p->grid, (float2 *)out, ol, s));
     return GBN_OK;
 }
@@ -1079,7 +1219,7 @@ int gbn_sense_forward(gbn_plan *p, const void *x, gbn_layout xl, const void *sen
     if (!x || !sens || (!kdata && p->M > 0)) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     GBN_CUDA(launch_pad_sense(deapod_args(p, false), (const float2 *)x, xl, (const float2 *)sens, sl, p->grid, s));
-    GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
+    GBN_TRY(fft_band_exec(p, p->grid, dir_type2(p), GBN_BAND_INPUT, s));
     GBN_TRY(run_interp(p, p->grid, kdata, kl, nullptr, s));
     return GBN_OK;
 }
@@ -1090,7 +1230,7 @@ int gbn_sense_adjoint(gbn_plan *p, const void *kdata, gbn_layout kl, const float
     if (!x || !sens || (!kdata && p->M > 0)) return fail(GBN_ERR_ARG, "null buffer");
     cudaStream_t s = (cudaStream_t)stream;
     GBN_TRY(run_spread(p, kdata, kl, dcf, p->grid, s));
-    GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
+    GBN_TRY(fft_band_exec(p, p->grid, dir_type1(p), GBN_BAND_OUTPUT, s));
     GBN_CUDA(launch_crop_sense(deapod_args(p, true), p->grid, (const float2 *)sens, sl, (float2 *)x, xl, s));
     return GBN_OK;
 }
@@ -1102,10 +1242,10 @@ int gbn_sense_normal(gbn_plan *p, const void *x, gbn_layout xl, const void *sens
     cudaStream_t s = (cudaStream_t)stream;
     const gbn_layout scl = {0, 1, p->desc.n_coil};
     GBN_CUDA(launch_pad_sense(deapod_args(p, false), (const float2 *)x, xl, (const float2 *)sens, sl, p->grid, s));
-    GBN_TRY(fft_exec(p, p->grid, dir_type2(p), s));
+    GBN_TRY(fft_band_exec(p, p->grid, dir_type2(p), GBN_BAND_INPUT, s));
     GBN_TRY(run_interp(p, p->grid, p->scratch.p, scl, dcf, s));
     GBN_TRY(run_spread(p, p->scratch.p, scl, nullptr, p->grid, s));
-    GBN_TRY(fft_exec(p, p->grid, dir_type1(p), s));
+    GBN_TRY(fft_band_exec(p, p->grid, dir_type1(p), GBN_BAND_OUTPUT, s));
     GBN_CUDA(launch_crop_sense(deapod_args(p, true), p->grid, (const float2 *)sens, sl, (float2 *)x_out, ol, s));
     return GBN_OK;
 }

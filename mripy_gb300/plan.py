@@ -59,7 +59,8 @@ class Tuning:
     """Kernel tiling chosen by the autotuner (0 = library default)."""
 
     def __init__(self, spread_tile=(0, 0, 0), interp_tile=(0, 0, 0), max_subproblem=0, coil_group=0, threads=0,
-                 interp_threads=0, interp_coil_group=0, interp_staging=0, spread_variant=0, interp_variant=0):
+                 interp_threads=0, interp_coil_group=0, interp_staging=0, spread_variant=0, interp_variant=0,
+                 fft_variant=0):
         self.spread_tile = tuple(spread_tile) + (0,) * (3 - len(spread_tile))
         self.interp_tile = tuple(interp_tile) + (0,) * (3 - len(interp_tile))
         self.max_subproblem = max_subproblem
@@ -70,19 +71,20 @@ class Tuning:
         self.interp_staging = interp_staging  # 0 tensor copies (TMA) where possible, 1 thread loads
         self.spread_variant = spread_variant  # 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes, 3 tensor cores
         self.interp_variant = interp_variant  # 3-D, 8 coils: 0 library choice, 1 plane streaming, 2 tensor cores
+        self.fft_variant = fft_variant  # composite calls' FFT: 0 library choice, 1 full, 2 pruned to the image band
 
     def key(self):
         return (self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
                 self.interp_threads, self.interp_coil_group, self.interp_staging, self.spread_variant,
-                self.interp_variant)
+                self.interp_variant, self.fft_variant)
 
     def __repr__(self):
         return ("Tuning(spread_tile=%s, interp_tile=%s, max_subproblem=%d, coil_group=%d, threads=%d, "
                 "interp_threads=%d, interp_coil_group=%d, interp_staging=%d, spread_variant=%d, "
-                "interp_variant=%d)" % (
+                "interp_variant=%d, fft_variant=%d)" % (
                     self.spread_tile, self.interp_tile, self.max_subproblem, self.coil_group, self.threads,
                     self.interp_threads, self.interp_coil_group, self.interp_staging, self.spread_variant,
-                    self.interp_variant))
+                    self.interp_variant, self.fft_variant))
 
 
 class Graph:
@@ -146,6 +148,7 @@ class NufftPlan:
         d.dense_tile_samples = int(dense_tile_samples)
         d.spread_variant = int(getattr(self.tuning, "spread_variant", 0))
         d.interp_variant = int(getattr(self.tuning, "interp_variant", 0))
+        d.fft_variant = int(getattr(self.tuning, "fft_variant", 0))
         self._lib = N.lib()
         h = ctypes.c_void_p()
         N.check(self._lib.gbn_plan_create(ctypes.byref(d), ctypes.byref(h)))
@@ -180,6 +183,7 @@ class NufftPlan:
             "dense_subproblems": inf.dense_subproblems,
             "spread_kernels": inf.spread_kernels, "split_tiles": inf.split_tiles,
             "spread_variant": inf.spread_variant, "interp_variant": inf.interp_variant,
+            "fft_variant": inf.fft_variant,
         }
 
     def status(self, stream=None):
@@ -332,6 +336,14 @@ class NufftPlan:
 
     def fft(self, grid, direction, stream=None):
         N.check(self._lib.gbn_fft(self._h, _ptr(grid), int(direction), _stream(stream)))
+        return grid
+
+    def fft_band(self, grid, direction, band, stream=None):
+        """The transform of the composite calls: ``band`` = ``GBN_BAND_INPUT`` after the pad
+        (the grid is zero outside the image band along x), ``GBN_BAND_OUTPUT`` before the crop
+        (only the band is read afterwards).  The full transform unless ``info()["fft_variant"]``
+        is 2."""
+        N.check(self._lib.gbn_fft_band(self._h, _ptr(grid), int(direction), int(band), _stream(stream)))
         return grid
 
     def pad_deapod(self, img, grid=None, stream=None):
