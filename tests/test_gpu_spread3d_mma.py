@@ -3,8 +3,9 @@ tile's samples, operands split into hi + lo parts, A built in TMEM, B in swizzle
 memory, the accumulator in TMEM) against the FP64 oracle.
 
 Covered: coil counts that fill one group of 8 and that leave a partial second group, split
-tiles (global-atomic flush), dense tiles (the compensated instance: Kahan sums of every
-batch's accumulator; its centre-cell error against FP64 on 3-D radial data), long work
+tiles (global-atomic flush), dense tiles (the compensated instance: the batches'
+accumulators summed in FP32 groups folded into Kahan sums; its centre-cell error against
+FP64 on 3-D radial data), long work
 items (many passes over the batch ring and both operand buffers), stencils across the
 periodic edge, odd oversampled grids with partial edge tiles, a grid
 buffer that is not 16-byte aligned, density weights, empty work items (zeros written
@@ -154,9 +155,10 @@ def test_mma_bitwise_repeatable_and_close_to_cube_kernel():
 
 def test_mma_compensated_centre_tiles_3d_radial():
     """Dense k-space-centre tiles of 3-D centre-out radial data (8 coils) run the compensated
-    tensor-core instance: every batch's accumulator is drained into a Kahan-compensated FP32
-    sum.  Against the FP64 oracle spread the centre cells' error drops (measured on GB300:
-    1.7e-6 uncompensated -> 3.8e-7; the FP32 cube kernel: 7.5e-7 -> 1.3e-7)."""
+    tensor-core instance: every batch's accumulator is drained into an FP32 group sum that is
+    folded every 8 batches into a Kahan-compensated FP32 sum.  Against the FP64 oracle spread
+    the centre cells' error drops (measured on GB300: 1.7e-6 uncompensated -> 3.8e-7; the FP32
+    cube kernel: 7.5e-7 -> 1.3e-7)."""
     from mripy_gb300 import synth
     rng = np.random.default_rng(30)
     n, nc = 32, 8
