@@ -123,7 +123,7 @@ struct gbn_plan {
     DevBuf traj_off_d, grp_scale, pts, home_key, home_keys_sorted, touch_count, touch_off, home_count,
         iota, home_idx, home_pts, dup_keys, dup_vals, dup_keys_sorted, dup_idx, dup_pts, spread_count,
         spread_tile_off, home_tile_off, nsub, sub_off, nsub_i, sub_off_i, spread_subs, interp_subs, cub_tmp, scratch,
-        stage_in, stage_out, stage_w, split_tiles;
+        stage_in, stage_out, stage_w, split_tiles, dense_subs;
     int64_t n_dup = 0, n_spread_sub = 0, n_interp_sub = 0;
     int spread_kernels = 0;   // kernels the last spread launched (split-tile zeroing included)
     uint64_t points_gen = 0;  // bumped by every gbn_set_points: captured graphs hold its buffers
@@ -342,6 +342,8 @@ int run_spread(gbn_plan *p, const void *c, gbn_layout L, const float *weight, fl
     a.weight = weight;
     a.grid = grid;
     a.any_dense = p->n_dense_sub > 0 ? 1 : 0;
+    a.dense_subs = p->dense_subs.as<uint32_t>();
+    a.n_dense = p->n_dense_sub;
     a.variant = p->spread_variant;
     a.status = p->kstatus;
     const int cg = spread_cg(p);
@@ -557,13 +559,14 @@ int subs_count(gbn_plan *p, SubsJob &j, uint32_t last[2], cudaStream_t s) {
 
 // after the synchronisation: allocate and fill the work items
 int subs_build(gbn_plan *p, const SubsJob &j, const uint32_t last[2], DevBuf &subs, uint32_t *split_list,
-               uint32_t *split_cursor, int64_t *n_sub_out, cudaStream_t s) {
+               uint32_t *split_cursor, uint32_t *dense_list, uint32_t *dense_cursor, int64_t *n_sub_out,
+               cudaStream_t s) {
     const int64_t n_sub = (int64_t)last[0] + last[1];
     if (n_sub > 0x7FFFFFFF) return fail(GBN_ERR_CAPACITY, "too many subproblems");
     GBN_TRY(ensure(p, subs, sizeof(int4) * (size_t)std::max<int64_t>(n_sub, 1)));
     GBN_CUDA(launch_build_subs(j.count, j.tile_off->as<uint32_t>(), j.sub_off->as<uint32_t>(), j.T, j.max_sub,
-                               j.every_tile, j.dense_min, j.interleave, split_list, split_cursor, subs.as<int4>(),
-                               s));
+                               j.every_tile, j.dense_min, j.interleave, split_list, split_cursor, dense_list,
+                               dense_cursor, subs.as<int4>(), s));
     *n_sub_out = n_sub;
     return GBN_OK;
 }
@@ -662,7 +665,7 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
                nullptr};
     uint32_t sizes[6] = {0, 0, 0, 0, 0, 0};  // spread last offset / count, interp ditto, dense, split
     auto queue_counts = [&]() -> int {
-        GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, 3 * sizeof(uint32_t), s));
+        GBN_CUDA(cudaMemsetAsync(p->kstatus + 1, 0, 4 * sizeof(uint32_t), s));
         GBN_TRY(subs_count(p, js, sizes, s));
         GBN_TRY(subs_count(p, ji, sizes + 2, s));
         GBN_CUDA(cudaMemcpyAsync(sizes + 4, p->kstatus + 1, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -721,9 +724,10 @@ int set_points_impl(gbn_plan *p, int dtype, const void *x, const void *y, const 
         GBN_TRY(queue_counts());
         GBN_CUDA(cudaStreamSynchronize(s));
     }
+    GBN_TRY(ensure(p, p->dense_subs, sizeof(uint32_t) * (size_t)std::max<uint32_t>(sizes[4], 1)));
     GBN_TRY(subs_build(p, js, sizes, p->spread_subs, p->split_tiles.as<uint32_t>(), p->kstatus + 3,
-                       &p->n_spread_sub, s));
-    GBN_TRY(subs_build(p, ji, sizes + 2, p->interp_subs, nullptr, nullptr, &p->n_interp_sub, s));
+                       p->dense_subs.as<uint32_t>(), p->kstatus + 4, &p->n_spread_sub, s));
+    GBN_TRY(subs_build(p, ji, sizes + 2, p->interp_subs, nullptr, nullptr, nullptr, nullptr, &p->n_interp_sub, s));
     const uint32_t counts[2] = {sizes[4], sizes[5]};
     p->n_dense_sub = counts[0];
     p->n_split = counts[1];
@@ -963,14 +967,15 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
         p->device_bytes += sizeof(float) * p->m[d];
     }
     // word 0: kernel status bits; words 1, 2: dense spread subproblems and split spread
-    // tiles (counted by set_points)
-    e = cudaMalloc((void **)&p->kstatus, 4 * sizeof(uint32_t));
+    // tiles (counted by set_points); words 3, 4: the cursors of the split-tile and
+    // dense-subproblem lists
+    e = cudaMalloc((void **)&p->kstatus, 8 * sizeof(uint32_t));
     if (e != cudaSuccess) {
         cudaGetLastError();
         p->kstatus = nullptr;
         return bail(fail(GBN_ERR_ALLOC, "status word allocation failed"));
     }
-    e = cudaMemset(p->kstatus, 0, 4 * sizeof(uint32_t));
+    e = cudaMemset(p->kstatus, 0, 8 * sizeof(uint32_t));
     if (e == cudaSuccess) e = launch_build_tables(p->dim, p->m, p->nf, p->tau, p->tab[0], p->tab[1], p->tab[2], 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return bail(fail(GBN_ERR_CUDA, std::string("table build: ") + cudaGetErrorString(e)));
@@ -1050,7 +1055,7 @@ int gbn_plan_destroy(gbn_plan *p) {
                       &p->dup_keys, &p->dup_vals, &p->dup_keys_sorted, &p->dup_idx, &p->dup_pts,
                       &p->spread_count, &p->spread_tile_off, &p->home_tile_off, &p->nsub, &p->sub_off, &p->nsub_i, &p->sub_off_i,
                       &p->spread_subs, &p->interp_subs, &p->cub_tmp, &p->scratch, &p->stage_in,
-                      &p->stage_out, &p->stage_w, &p->split_tiles, &p->solve_ws, &p->dcf_ws};
+                      &p->stage_out, &p->stage_w, &p->split_tiles, &p->dense_subs, &p->solve_ws, &p->dcf_ws};
     for (gbn_plan::SolveGraph &sg : p->solve_graph)
         if (sg.exec) cudaGraphExecDestroy(sg.exec);
     for (DevBuf *b : bufs) release(*b);

@@ -111,9 +111,12 @@ cudaError_t launch_gather_pts(const float4 *pts, const uint32_t *idx, int64_t n,
 // split_list (may be null): the indices of the tiles covered by more than one subproblem
 // are appended at *split_cursor (zeroed by the caller).
 // interleave: split tiles' items take every s-th entry (only for the 3-D cube spread)
+// dense_list (may be null): the indices of the items with kDenseFlag are appended at
+// *dense_cursor (zeroed by the caller), in no particular order.
 cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
                               int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min, int interleave,
-                              uint32_t *split_list, uint32_t *split_cursor, int4 *subs, cudaStream_t s);
+                              uint32_t *split_list, uint32_t *split_cursor, uint32_t *dense_list,
+                              uint32_t *dense_cursor, int4 *subs, cudaStream_t s);
 // work items per tile; n_dense (may be null) accumulates the items of tiles with at least
 // dense_min samples, n_split (may be null) the tiles split over several items
 cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int every_tile, uint32_t dense_min,
@@ -132,6 +135,8 @@ struct SpreadArgs {
     const float *weight;      // per sample (original index) or null: density compensation
     float2 *grid;
     int any_dense;            // some subproblems carry kDenseFlag (compensated accumulation)
+    const uint32_t *dense_subs;  // the indices of those subproblems (n_dense of them)
+    int64_t n_dense;
     int variant;              // 3-D, 8 coils: 0 library choice, 1 warp rows, 2 cubes (gbn_plan_desc)
     uint32_t *status;         // the plan's status word (bounded waits of the cube kernel)
 };

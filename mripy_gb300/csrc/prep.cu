@@ -160,7 +160,8 @@ __global__ void k_count_subs(const uint32_t *__restrict__ count, int64_t n, int 
 __global__ void k_build_subs(const uint32_t *__restrict__ count, const uint32_t *__restrict__ tile_off,
                              const uint32_t *__restrict__ sub_off, int64_t n, int max_sub, int every_tile,
                              uint32_t dense_min, int interleave, uint32_t *__restrict__ split_list,
-                             uint32_t *__restrict__ split_cursor, int4 *__restrict__ subs) {
+                             uint32_t *__restrict__ split_cursor, uint32_t *__restrict__ dense_list,
+                             uint32_t *__restrict__ dense_cursor, int4 *__restrict__ subs) {
     int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= n) return;
     uint32_t c = count[t];
@@ -169,6 +170,10 @@ __global__ void k_build_subs(const uint32_t *__restrict__ count, const uint32_t 
     uint32_t o = sub_off[t];
     const bool dense = dense_min > 0 && c >= dense_min;
     if (s > 1 && split_list) split_list[atomicAdd(split_cursor, 1u)] = (uint32_t)t;  // order is irrelevant
+    if (dense && s > 0 && dense_list) {
+        const uint32_t d = atomicAdd(dense_cursor, s);
+        for (uint32_t k = 0; k < s; ++k) dense_list[d + k] = o + k;
+    }
     for (uint32_t k = 0; k < s; ++k) {
         int flags = (s > 1 ? kSplitFlag : 0) | (k == 0 ? kFirstFlag : 0) | (dense ? kDenseFlag : 0);
         if (interleave && s > 1) {
@@ -230,11 +235,12 @@ cudaError_t launch_count_subs(const uint32_t *count, int64_t n, int max_sub, int
 
 cudaError_t launch_build_subs(const uint32_t *count, const uint32_t *tile_off, const uint32_t *sub_off,
                               int64_t ntiles_total, int max_sub, int every_tile, uint32_t dense_min, int interleave,
-                              uint32_t *split_list, uint32_t *split_cursor, int4 *subs, cudaStream_t s) {
+                              uint32_t *split_list, uint32_t *split_cursor, uint32_t *dense_list,
+                              uint32_t *dense_cursor, int4 *subs, cudaStream_t s) {
     if (ntiles_total == 0) return cudaSuccess;
     k_build_subs<<<blocks_for(ntiles_total, 256), 256, 0, s>>>(count, tile_off, sub_off, ntiles_total, max_sub,
                                                                every_tile, dense_min, interleave, split_list,
-                                                               split_cursor, subs);
+                                                               split_cursor, dense_list, dense_cursor, subs);
     return cudaGetLastError();
 }
 

@@ -115,15 +115,18 @@ static cudaError_t launch_cube(const SpreadArgs &a, int64_t n_sub, cudaStream_t 
     return e;
 }
 
-// tensor-core kernel (one unit per block): plain instance, then the compensated one for the
-// dense units
+// tensor-core kernel: the plain instance (one block per unit), then the compensated one (one
+// block per dense unit)
 template <int WT, bool KAHAN>
 static cudaError_t launch_mma_instance(const SpreadArgs &a, int64_t n_units, int n_cg, cudaStream_t s) {
     auto kern = k_spread_mma<3, WT, KAHAN>;
     const size_t smem = KAHAN ? kMmaSmemBytesK : kMmaSmemBytes;
     cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
-    kern<<<(unsigned)n_units, mma_threads<KAHAN>(), smem, s>>>(a, a.status, n_cg);
+    // the compensated instance: one block per (dense subproblem, coil group) only
+    const int64_t blocks = KAHAN ? a.n_dense * n_cg : n_units;
+    if (blocks == 0) return cudaSuccess;
+    kern<<<(unsigned)blocks, mma_threads<KAHAN>(), smem, s>>>(a, a.status, n_cg);
     return cudaGetLastError();
 }
 

@@ -45,8 +45,9 @@
 // 3.8e-7, in 1.5 % less time).  The order is fixed for a given trajectory and tiling.
 //
 // Every wait is bounded (kTmaWaitLimit probes); one that gives up sets kStatusSpreadTimeout
-// in the plan's status word and goes on, so no launch can hang.  Each instance runs the
-// units of its own kind (dense or not) and skips the others.
+// in the plan's status word and goes on, so no launch can hang.  The plain instance runs a
+// block per unit and leaves the dense ones at once; the compensated instance runs a block
+// per dense unit only, through the plan's list of dense subproblems.
 #pragma once
 
 #include "common.cuh"
@@ -274,6 +275,14 @@ __global__ void __launch_bounds__(mma_threads<KAHAN>(), KAHAN ? 1 : 2) k_spread_
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int W = WT ? WT : g.W;
 
+    // the plain instance runs a block per unit, the compensated one a block per dense unit
+    // (through the list of dense subproblems); a block whose unit is of the other kind leaves
+    // before it takes TMEM (all its threads alike)
+    const int64_t unit = KAHAN ? (int64_t)a.dense_subs[blockIdx.x / n_cg] * n_cg + blockIdx.x % n_cg
+                               : (int64_t)blockIdx.x;
+    int4 sub;
+    if (!cube_unit(a.subs, unit, n_cg, KAHAN, sub)) return;
+
     if (warp == WM) {
         tmem_alloc(tslot, kCols);
         tmem_relinquish();
@@ -294,9 +303,7 @@ __global__ void __launch_bounds__(mma_threads<KAHAN>(), KAHAN ? 1 : 2) k_spread_
     tc_fence_after();
     const uint32_t tbase = *tslot;
 
-    const int64_t unit = blockIdx.x;
-    int4 sub;
-    if (cube_unit(a.subs, unit, n_cg, KAHAN, sub)) {
+    {
         const int nb = (sub.z + B - 1) / B;
         const int cg0 = (int)(unit % n_cg) * CG;
 
