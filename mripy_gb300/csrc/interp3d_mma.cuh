@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
     int o[3], e[3];
     tile_coords<3>(g, sub.x % g.ntiles, o, e);
     const int nb = (sub.z + kImBatch - 1) / kImBatch;
+    if (nb == 0) return;  // an empty work item: no sample to add to (the launcher zeroed them)
 
     if (warp == kImWarp) {
         tmem_alloc(tslot, kImTmemCols);
@@ -94,37 +95,34 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
     }
     // B: the tile's cells (x, y, z) of the 8 coils; cells past the grid edge and padded
     // coils are 0.  z fastest across threads: 128-byte runs of each (coil, x, y) row.
-    // (Nothing to do for an empty work item.)
     // Loads are issued 8 at a time before any is used, so a thread waits for one memory
     // latency per 8 cells rather than per cell.
-    if (nb > 0) {
-        constexpr int kCells = CG * kMmaTX * kMmaTY * kMmaTZ;
-        const float2 *base = a.grid + (int64_t)grp * g.n_coil * g.G;
-        for (int r0 = threadIdx.x; r0 < kCells; r0 += 8 * kImThreads) {
-            float2 v[8];
+    constexpr int kCells = CG * kMmaTX * kMmaTY * kMmaTZ;
+    const float2 *base = a.grid + (int64_t)grp * g.n_coil * g.G;
+    for (int r0 = threadIdx.x; r0 < kCells; r0 += 8 * kImThreads) {
+        float2 v[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int i = r0 + u * kImThreads;
-                const int z = i & 15, y = (i >> 4) & 7, x = (i >> 7) & 3, c = i >> 9;
-                v[u] = make_float2(0.f, 0.f);
-                if (i < kCells && cg0 + c < g.n_coil && x < e[0] && y < e[1] && z < e[2])
-                    v[u] = base[(int64_t)(cg0 + c) * g.G + ((int64_t)(o[0] + x) * g.nf[1] + (o[1] + y)) * g.nf[2] +
-                                (o[2] + z)];
-            }
+        for (int u = 0; u < 8; ++u) {
+            const int i = r0 + u * kImThreads;
+            const int z = i & 15, y = (i >> 4) & 7, x = (i >> 7) & 3, c = i >> 9;
+            v[u] = make_float2(0.f, 0.f);
+            if (i < kCells && cg0 + c < g.n_coil && x < e[0] && y < e[1] && z < e[2])
+                v[u] = base[(int64_t)(cg0 + c) * g.G + ((int64_t)(o[0] + x) * g.nf[1] + (o[1] + y)) * g.nf[2] +
+                            (o[2] + z)];
+        }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int i = r0 + u * kImThreads;
-                if (i >= kCells) break;
-                const int z = i & 15, y = (i >> 4) & 7, x = (i >> 7) & 3, c = i >> 9;
-                float2 h, l;
-                tf32_split2(v[u], make_float2(1.f, 1.f), h, l);
-                const int n = x * 16 + c * 2, k = y * 16 + z;
-                const uint32_t ore = im_b_offset(n, k), oim = im_b_offset(n + 1, k);
-                *reinterpret_cast<float *>(bh + ore) = h.x;
-                *reinterpret_cast<float *>(bl + ore) = l.x;
-                *reinterpret_cast<float *>(bh + oim) = h.y;
-                *reinterpret_cast<float *>(bl + oim) = l.y;
-            }
+        for (int u = 0; u < 8; ++u) {
+            const int i = r0 + u * kImThreads;
+            if (i >= kCells) break;
+            const int z = i & 15, y = (i >> 4) & 7, x = (i >> 7) & 3, c = i >> 9;
+            float2 h, l;
+            tf32_split2(v[u], make_float2(1.f, 1.f), h, l);
+            const int n = x * 16 + c * 2, k = y * 16 + z;
+            const uint32_t ore = im_b_offset(n, k), oim = im_b_offset(n + 1, k);
+            *reinterpret_cast<float *>(bh + ore) = h.x;
+            *reinterpret_cast<float *>(bl + ore) = l.x;
+            *reinterpret_cast<float *>(bh + oim) = h.y;
+            *reinterpret_cast<float *>(bl + oim) = l.y;
         }
     }
     fence_proxy_async_smem();

@@ -2,15 +2,14 @@
 tile's samples, operands split into hi + lo parts, A built in TMEM, B in swizzled shared
 memory, the accumulator in TMEM) against the FP64 oracle.
 
-Covered: coil counts that fill one group of 8 and that leave a partial second group, split
-tiles (global-atomic flush), dense tiles (the compensated instance: the batches'
-accumulators summed in FP32 groups folded into Kahan sums; its centre-cell error against
-FP64 on 3-D radial data), long work
-items (many passes over the batch ring and both operand buffers), stencils across the
-periodic edge, odd oversampled grids with partial edge tiles, a grid
-buffer that is not 16-byte aligned, density weights, empty work items (zeros written
-without an MMA), ragged trajectory groups, run-to-run bit equality, agreement with the FP32
-cube kernel, and the status word (clean after every call).
+Covered: coil counts that fill one group of 8 and that leave a partial second group (also
+with dense tiles), split tiles (global-atomic flush), dense tiles (the compensated instance:
+the batches' accumulators summed in FP32 groups folded into Kahan sums; its centre-cell
+error against FP64 on 3-D radial data), long work items (many passes over the batch ring and
+both operand buffers), stencils across the periodic edge, odd oversampled grids with partial
+edge tiles, a grid buffer that is not 16-byte aligned, density weights, empty work items
+(zeros written without an MMA), ragged trajectory groups, run-to-run bit equality, agreement
+with the FP32 cube kernel, and the status word (clean after every call).
 
 Tolerance: TOL_REF = 2e-5 relative L2 against the FP64 oracle (the 3-term TF32 products are
 within ~1e-6 of FP32); 5e-6 relative L2 against the FP32 cube kernel.
@@ -86,6 +85,23 @@ def test_mma_split_dense_and_long_items(dense_tile_samples, max_subproblem):
         assert inf["dense_subproblems"] > 0
     if max_subproblem == 64:
         assert inf["split_tiles"] > 0
+    c = cvec(rng, (M, nc))
+    F = p.type1(cuda(c))
+    p.status()
+    assert rel(F[0], O.nufft_type1(tuple(xs), c.astype(np.complex128), shape, eps=5e-6)) < TOL_REF
+    p.close()
+
+
+@pytest.mark.parametrize("nc", [12, 16])
+def test_mma_dense_tiles_with_two_coil_groups(nc):
+    """Dense tiles (low threshold) with two coil groups: the compensated instance runs one
+    block per (dense subproblem, coil group) through the plan's list of dense subproblems."""
+    rng = np.random.default_rng(76 + nc)
+    M, shape = 15000, (24, 24, 24)
+    xs = _points(rng, M, dense=0.6)
+    p = _plan(shape, nc, xs, tuning=Tuning(coil_group=8, spread_variant=3, max_subproblem=512),
+              dense_tile_samples=300)
+    assert p.info()["dense_subproblems"] > 0
     c = cvec(rng, (M, nc))
     F = p.type1(cuda(c))
     p.status()
