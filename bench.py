@@ -48,6 +48,10 @@ sys.path.insert(0, ROOT)
 METRIC = "batched NUFFT fwd+adj Msamples/s vs per-instance plain at ≤1e-4 rel err"
 UNIT = "Msamples/s"
 L2_BYTES = 129 * 2 ** 20
+# plan info's spread_variant -> the spread kernel that ran
+SPREAD_KERNELS = {3: "k_spread_mma: tensor cores (+ compensated instance for dense tiles)",
+                  2: "k_spread3d_cube: FP32 register cubes", 1: "k_spread3d_reg: warp rows",
+                  0: "register tiles (2-D) or shared-memory tiles"}
 
 
 def dist_env():
@@ -380,6 +384,10 @@ def run_gpu(args, wl):
                          "interp_coils_per_block": info["interp_coil_group"],
                          "spread_threads": info["threads"], "interp_threads": info["interp_threads"],
                          "max_subproblem": info["max_subproblem"],
+                         "spread_kernel": SPREAD_KERNELS.get(info["spread_variant"], "shared-memory tiles"),
+                         "interp_kernel": ("k_interp3d_mma: tensor cores on the spread's tiles (8 coils per block; "
+                                           "interp_tile and interp_* above do not apply)"
+                                           if info["interp_variant"] == 2 else "interp bins (interp_tile)"),
                          "chosen_by": "autotuner (%.1f s, untimed)" % tune_s if tuning is not None
                          else "library defaults"},
               "wall_s_timed": round(t_wall, 3)}
