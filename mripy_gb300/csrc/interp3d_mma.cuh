@@ -93,6 +93,12 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
         }
         fence_barrier_init();
     }
+    // the builders' first sample indices, read before the tile so that their latency
+    // overlaps its loads (each builder lane: sample 32 q + lane of the first batch)
+    const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
+    uint32_t jn = 0;
+    bool okn = warp != kImWarp && 32 * (warp & 3) + lane < sub.z;
+    if (okn) jn = a.idx[(int64_t)sub.y + (int64_t)(32 * (warp & 3) + lane) * stride];
     // B: the tile's cells (x, y, z) of the 8 coils; cells past the grid edge and padded
     // coils are 0.  z fastest across threads: 128-byte runs of each (coil, x, y) row.
     // Loads are issued 8 at a time before any is used, so a thread waits for one memory
@@ -168,20 +174,14 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
         const int q = warp & 3, h = warp >> 2;
         const uint32_t tl = tmem_lane_base(tbase, q);
         const int ns = g.ns;
-        const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
         // the previous batch's sample for the deferred epilogue
         float wxp[4] = {0.f, 0.f, 0.f, 0.f};
         uint32_t jp = 0;
         bool okp = false;
         // records are read one batch ahead: the next batch's entry early in the batch, its
         // sample record half way through, so neither load is waited for where it is used
-        uint32_t jn = 0;
-        bool okn = 32 * q + lane < sub.z;
         float4 ptn = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (okn) {
-            jn = a.idx[(int64_t)sub.y + (int64_t)(32 * q + lane) * stride];
-            ptn = a.pts_by_sample[jn];
-        }
+        if (okn) ptn = a.pts_by_sample[jn];
         for (int b = 0; b <= nb; ++b) {
             float wx[4] = {0.f, 0.f, 0.f, 0.f};
             uint32_t j = 0;
