@@ -282,6 +282,12 @@ __global__ void __launch_bounds__(mma_threads<KAHAN>(), KAHAN ? 1 : 2) k_spread_
                                : (int64_t)blockIdx.x;
     int4 sub;
     if (!cube_unit(a.subs, unit, n_cg, KAHAN, sub)) return;
+    // a loader warp's first sample indices (its first batch: k = loader index), read before
+    // the set-up below so that their latency overlaps it
+    const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
+    uint32_t j0 = 0;
+    if (warp >= NB && warp < WM && (warp - NB) * B + lane < sub.z)
+        j0 = a.idx[(int64_t)sub.y + (int64_t)((warp - NB) * B + lane) * stride];
 
     if (warp == WM) {
         tmem_alloc(tslot, kCols);
@@ -313,7 +319,6 @@ __global__ void __launch_bounds__(mma_threads<KAHAN>(), KAHAN ? 1 : 2) k_spread_
             tile_coords<D>(g, sub.x % g.ntiles, o, e);
             const int lw = warp - NB;
             const int ns = g.ns;
-            const int64_t stride = max(1, sub.w >> kStrideShift);  // interleaved item of a split tile
             for (int k = lw; k < nb; k += kMmaLoaders) {
                 const int slot = k % kMmaSlots;
                 const int n = min(B, sub.z - k * B);
@@ -321,7 +326,7 @@ __global__ void __launch_bounds__(mma_threads<KAHAN>(), KAHAN ? 1 : 2) k_spread_
                 float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
                 uint32_t j = 0;
                 if (ok) {
-                    j = a.idx[(int64_t)sub.y + (int64_t)(k * B + lane) * stride];
+                    j = k == lw ? j0 : a.idx[(int64_t)sub.y + (int64_t)(k * B + lane) * stride];
                     pt = a.pts_by_sample[j];
                 }
                 float sw = 1.f;
