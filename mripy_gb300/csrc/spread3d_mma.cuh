@@ -21,9 +21,9 @@
 // One (work item, coil group) unit per block; 3 loader warps, NB builder warps (8 in the
 // plain instance, 16 in the compensated one) and 1 MMA warp:
 // * the loader warps fill a ring of kMmaSlots 32-sample batches (loader l: batches l, l + 3,
-//   ...): per sample and dimension the first tap's tile plane and the distance of plane 0,
-//   and the 8 coil values times the optional density weight ([coil][sample]); `full` /
-//   `empty` mbarriers per slot.
+//   ...; the sample indices of batch l are read before the block's set-up): per sample and
+//   dimension the first tap's tile plane and the distance of plane 0, and the 8 coil values
+//   times the optional density weight ([coil][sample]); `full` / `empty` mbarriers per slot.
 // * the builder warps first compute the batch's tile-plane weights per sample together
 //   (stored [plane][sample]; a named barrier among them), then turn the batch into the MMA
 //   operands: warp b writes A's hi and lo parts for the 32 TMEM lanes of its quarter (b % 4)
