@@ -99,7 +99,8 @@ typedef struct {
                                    tile's samples, partial sums added with float atomics) */
     int32_t fft_variant;        /* FFT of the composite calls (type 1/2/21, SENSE): 0 = library
                                    choice (pruned on 3-D grids of >= 2^21 cells per instance,
-                                   <= 256 instances), 1 = the full transform, 2 = pruned
+                                   <= 256 instances; the full transform if cuFFT cannot make
+                                   the pruned plans), 1 = the full transform, 2 = pruned
                                    wherever the image band is narrower than the grid (2-D and
                                    3-D, <= 4096 instances).  Pruned: the trailing axes are
                                    transformed only on the grid planes inside the image band

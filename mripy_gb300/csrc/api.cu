@@ -799,6 +799,17 @@ int make_fft_band(gbn_plan *p) {
     return GBN_OK;
 }
 
+// releases the pruned transform's plans and work area (the full transform stays)
+void drop_fft_band(gbn_plan *p) {
+    for (int i = 0; i < p->fft_n_planes; ++i) cufftDestroy(p->fft_planes[i]);
+    p->fft_n_planes = 0;
+    if (p->fft_x_ok) cufftDestroy(p->fft_x);
+    p->fft_x_ok = false;
+    if (p->fft_work) cudaFree(p->fft_work);
+    p->fft_work = nullptr;
+    p->fft_band = false;
+}
+
 int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     if (!desc || !out) return fail(GBN_ERR_ARG, "null argument");
     *out = nullptr;
@@ -992,7 +1003,10 @@ int plan_create_impl(const gbn_plan_desc *desc, gbn_plan **out) {
     if (cufftGetSize(p->fft, &ws) == CUFFT_SUCCESS) p->device_bytes += ws;
     if (fft_band_wanted(p)) {
         const int st = make_fft_band(p);
-        if (st != GBN_OK) return bail(st);
+        if (st != GBN_OK) {
+            if (p->fft_variant == 2) return bail(st);  // asked for: its failure is the plan's
+            drop_fft_band(p);  // the library's choice: the full transform instead
+        }
     }
     *out = p;
     return GBN_OK;
