@@ -4,6 +4,8 @@ No kernel is launched: these run without a GPU."""
 import ctypes
 import os
 import re
+import shutil
+import subprocess
 
 import pytest
 
@@ -22,6 +24,37 @@ def header_functions():
 
 def test_header_and_binding_agree():
     assert header_functions() == sorted(N.EXPORTED)
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="needs gcc")
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of gbn_plan_desc, gbn_plan_info and gbn_layout have the header's
+    fields in its order (read from the header) at its offsets and sizes (printed by a C
+    program built against include/gbnufft.h)."""
+    structs = {"gbn_plan_desc": N.PlanDesc, "gbn_plan_info": N.PlanInfo, "gbn_layout": N.Layout}
+    # the field names, in order, from the header's struct definitions
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    for cname, cls in structs.items():
+        body = re.search(r"typedef struct \{([^}]*)\}\s*" + cname + r"\s*;", text).group(1)
+        names = [re.match(r"\w+", d.strip()).group(0)
+                 for decl in body.split(";") if decl.strip()
+                 for d in decl.split(None, 1)[1].split(",")]
+        assert names == [f for f, _ in cls._fields_], cname
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gbnufft.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append('printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("return 0; }")
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {(ln.split()[0], ln.split()[1]): int(ln.split()[2]) for ln in out if ln.strip()}
+    for cname, cls in structs.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
 
 
 def test_library_exports_every_declared_symbol():
