@@ -141,7 +141,10 @@ cudaError_t launch_interp3d_mma(const MmaInterpArgs &a, int64_t n_sub, uint32_t 
     const int n_cg = (a.g.n_coil + 7) / 8;
     // float4 atomics (two coils each) when the coils of a sample are adjacent and every
     // coil group starts on a 16-byte boundary (8-coil groups: an even element stride)
-    const int vec = a.c_coil == 1 && a.c_elem % 2 == 0 && (uintptr_t)a.c % 16 == 0;
+    // bit 0: two coils per atomicAdd(float4) into the samples; bit 1: the tile's grid values
+    // loaded two z cells per 16-byte load (every such pair starts on a 16-byte boundary)
+    const int vec = (a.c_coil == 1 && a.c_elem % 2 == 0 && (uintptr_t)a.c % 16 == 0 ? 1 : 0) |
+                    ((uintptr_t)a.grid % 16 == 0 && a.g.nf[2] % 2 == 0 && a.g.G % 2 == 0 ? 2 : 0);
     cudaError_t err = cudaSuccess;
     GBN_DISPATCH_W(a.g.W, {
         auto kern = k_interp3d_mma<WT>;

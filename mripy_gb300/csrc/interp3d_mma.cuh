@@ -106,6 +106,37 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
     // latency per 8 cells rather than per cell.
     constexpr int kCells = CG * kMmaTX * kMmaTY * kMmaTZ;
     const float2 *base = a.grid + (int64_t)grp * g.n_coil * g.G;
+    if (vec_atomic & 2) {
+        // pairs of z cells, one 16-byte load each: a partial tile's z extent is even too
+        static_assert(kCells / 2 <= 8 * kImThreads, "one round of loads");
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = threadIdx.x + u * kImThreads;  // pair index
+            const int z = 2 * (i & 7), y = (i >> 3) & 7, x = (i >> 6) & 3, c = i >> 8;
+            v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (i < kCells / 2 && cg0 + c < g.n_coil && x < e[0] && y < e[1] && z < e[2])
+                v[u] = *reinterpret_cast<const float4 *>(
+                    base + (int64_t)(cg0 + c) * g.G + ((int64_t)(o[0] + x) * g.nf[1] + (o[1] + y)) * g.nf[2] + (o[2] + z));
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = threadIdx.x + u * kImThreads;
+            if (i >= kCells / 2) break;
+            const int z = 2 * (i & 7), y = (i >> 3) & 7, x = (i >> 6) & 3, c = i >> 8;
+#pragma unroll
+            for (int hz = 0; hz < 2; ++hz) {
+                float2 h, l;
+                tf32_split2(hz ? make_float2(v[u].z, v[u].w) : make_float2(v[u].x, v[u].y), make_float2(1.f, 1.f), h, l);
+                const int n = x * 16 + c * 2, k = y * 16 + z + hz;
+                const uint32_t ore = im_b_offset(n, k), oim = im_b_offset(n + 1, k);
+                *reinterpret_cast<float *>(bh + ore) = h.x;
+                *reinterpret_cast<float *>(bl + ore) = l.x;
+                *reinterpret_cast<float *>(bh + oim) = h.y;
+                *reinterpret_cast<float *>(bl + oim) = l.y;
+            }
+        }
+    } else
     for (int r0 = threadIdx.x; r0 < kCells; r0 += 8 * kImThreads) {
         float2 v[8];
 #pragma unroll
@@ -286,7 +317,7 @@ __global__ void __launch_bounds__(kImThreads, 2) k_interp3d_mma(MmaInterpArgs a,
                     }
                     const int coil0 = cg0 + 4 * h;
                     float2 *dst = a.c + (int64_t)jp * a.c_elem + (int64_t)coil0 * a.c_coil;
-                    if (vec_atomic && coil0 + 4 <= g.n_coil) {
+                    if ((vec_atomic & 1) && coil0 + 4 <= g.n_coil) {
                         // coils adjacent and 16-byte aligned: two coils per atomic
                         atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(pr[0], pr[1], pr[2], pr[3]));
                         atomicAdd(reinterpret_cast<float4 *>(dst + 2), make_float4(pr[4], pr[5], pr[6], pr[7]));
