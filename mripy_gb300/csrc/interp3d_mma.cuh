@@ -12,7 +12,8 @@
 //
 // One (work item, coil group) unit per block, 9 warps; a block whose work item is empty
 // leaves at once.  At the start the builders issue their first samples' index loads, then all
-// threads load the tile's 8 coils x 512 cells, split them into TF32 hi + lo parts and write B
+// threads load the tile's 8 coils x 512 cells (two z cells per 16-byte load where the grid's
+// alignment allows), split them into TF32 hi + lo parts and write B
 // into shared memory (K-major, 128-byte swizzle, four 32-column K atoms of two y rows each).
 // Then per batch of 128 of the unit's samples:
 // * 8 builder warps: warp (q, h) takes samples 32 q .. 32 q + 31 of the batch, one per lane
