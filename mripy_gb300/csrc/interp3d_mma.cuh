@@ -11,11 +11,11 @@
 // spread's (sample, tile) work lists), added into the zeroed output with float atomics.
 //
 // One (work item, coil group) unit per block, 9 warps; a block whose work item is empty
-// leaves at once.  At the start the builders issue their first samples' index loads, then all
-// threads load the tile's 8 coils x 512 cells (two z cells per 16-byte load where the grid's
-// alignment allows), split them into TF32 hi + lo parts and write B
-// into shared memory (K-major, 128-byte swizzle, four 32-column K atoms of two y rows each).
-// Then per batch of 128 of the unit's samples:
+// leaves at once.  At the start the builders issue their first samples' index loads, then
+// all threads load the tile's 8 coils x 512 cells (two z cells per 16-byte load where the
+// grid's alignment allows), split them into TF32 hi + lo parts and write B into shared
+// memory (K-major, 128-byte swizzle, four 32-column K atoms of two y rows each). Then per
+// batch of 128 of the unit's samples:
 // * 8 builder warps: warp (q, h) takes samples 32 q .. 32 q + 31 of the batch, one per lane
 //   (TMEM lane = sample), reads its record, computes its plane weights (ex2.approx) and writes
 //   A in four chunks of 32 columns (y rows 2 c and 2 c + 1; warp h writes row 2 c + h) into
