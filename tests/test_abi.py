@@ -102,6 +102,21 @@ def test_null_arguments_are_rejected_without_touching_the_device():
     assert buf.value  # message of the last failure
 
 
+@pytest.mark.parametrize("field,value", [("spread_variant", 4), ("interp_variant", 3), ("fft_variant", 3),
+                                         ("fft_variant", -1), ("coil_group", 3), ("threads", 100)])
+def test_plan_create_rejects_bad_tuning_before_touching_the_device(field, value):
+    """Out-of-range tuning fields are GBN_ERR_ARG, checked before any CUDA call (so the same
+    with or without a GPU), and no plan is returned."""
+    d = N.PlanDesc()
+    d.dim, d.ms, d.mt, d.mu, d.eps, d.iflag, d.df, d.n_coil, d.n_traj = 3, 16, 16, 16, 5e-6, 1, 1.0, 1, 1
+    d.max_nspread = 6
+    setattr(d, field, value)
+    h = ctypes.c_void_p()
+    assert N.lib().gbn_plan_create(ctypes.byref(d), ctypes.byref(h)) == 1  # GBN_ERR_ARG
+    assert field.split("_")[0] in N.last_error()
+    assert not h.value
+
+
 def test_plan_create_reports_missing_device():
     import torch
     if torch.cuda.is_available():
